@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark: aggregation + breakage RHS evaluations per second at n = 16384, FP64.
+
+Workload (single instance, one GPU): n = 16384 pivots x_i = 1e-21 * 2^(i/512) m^3,
+lognormal N (median bin 2048, sigma_ln = 1, total 1e14 m^-3), Brownian+shear
+aggregation (beta_br = 6.73e-18, beta_sh = 4 G / 3, G = 50 1/s) plus threshold
+breakage (S0 = 1e-3 1/s, v_min = x_8192) with the symmetric-binary daughter
+written as n_quad = 16 coincident quadrature entries. Synthetic inputs.
+
+One step = zero rhs + aggregation RHS + breakage RHS (the source term an ODE
+integrator asks for once per stage).
+
+  value : steps/s with N, x, tables resident in HBM; each step timed with CUDA
+          events on the launching stream; L2 (126 MiB) is flushed by writing a
+          512 MiB buffer before every timed step (outside the events).
+  e2e   : the same step through the C ABI from pinned HOST buffers: H2D copy of
+          N, the RHS, D2H copy of rhs, all inside the timed events.
+
+--impl reference runs the reference's own CUDA kernels (built unmodified from
+its sources into oracle/_ref/, launched with its launch geometry) on the same
+GPU, config and timing. The reference has no CPU implementation of the path.
+
+Multi-GPU: the single-instance RHS does not shard; with torchrun each rank runs
+an independent replica on its own GPU ("replicas only"), value = total steps/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "pbe-fixed-pivot-cuda_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N_BINS = 16384
+N_QUAD = 16
+PAIRS = N_BINS * (N_BINS + 1) // 2
+FRAGMENTS = N_BINS * N_QUAD
+FLOPS_PER_PAIR = 22      # algorithmic FP64 flops per pair interaction
+FLOPS_PER_FRAGMENT = 8   # per breakage fragment
+L2_FLUSH_BYTES = 512 << 20
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload():
+    import pbe_gb300 as pg
+
+    c = pg.grids.config_n16384()
+    x, N = c["x"], c["N"]
+    ap = pg.AggregationParams(n=N_BINS, kernel_type=pg.AGG_BROWNIAN_SHEAR, beta0=0.0,
+                              beta_br=c["beta_br"], beta_sh=c["beta_sh"])
+    ap.log_x0, ap.inv_log_r = pg.grids.geometric_params(x)
+    t_q, bw_q = pg.quadrature.symmetric_binary_split(N_QUAD)
+    bp = pg.BreakageParams(n=N_BINS, n_quad=N_QUAD, selection=pg.SEL_THRESHOLD, S0=c["S0"],
+                           v_min=c["v_min"])
+    return x, N, t_q, bw_q, ap, bp
+
+
+def fp64_peak_tflops(stream) -> float | None:
+    import ctypes
+
+    import pbe_gb300 as pg
+
+    path = os.path.join(os.path.dirname(pg.LIB_PATH), "libpbe_probe.so")
+    if not os.path.isfile(path):
+        return None
+    lib = ctypes.CDLL(path)
+    lib.pbe_probe_dfma_tflops.restype = ctypes.c_double
+    lib.pbe_probe_dfma_tflops.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    v = lib.pbe_probe_dfma_tflops(5, stream.cuda_stream)
+    return v if v > 0 else None
+
+
+def cpu_baseline(x, N, t_q, bw_q, ap, bp, seconds=3.0):
+    """Oracle port (serial C++ restatement), all host threads for aggregation.
+    Sample: whole n = 16384 RHS evaluations, repeated until `seconds` elapsed."""
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    evals = 0
+    while True:
+        pyoracle.aggregation_rhs_mt(N, x, ap.kernel_type, ap.beta0, ap.beta_br, ap.beta_sh,
+                                    ap.log_x0, ap.inv_log_r, nthreads=threads)
+        pyoracle.breakage_rhs(N, x, t_q, bw_q, bp.selection, bp.S0, bp.v_ref, bp.alpha, bp.v_min)
+        evals += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return {"value": evals / el, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": "%d full n=16384 agg+brk RHS evaluations (%.1f s wall, OpenMP over "
+                      "aggregation rows, breakage serial)" % (evals, el)}
+
+
+def main():
+    ap_ = argparse.ArgumentParser()
+    ap_.add_argument("--gpus", type=int, default=1)
+    ap_.add_argument("--steps", type=int, default=200)
+    ap_.add_argument("--warmup", type=int, default=5)
+    ap_.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap_.add_argument("--mode", choices=["gather", "scatter"], default="gather")
+    ap_.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap_.parse_args()
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference" and world > 1 and rank != 0:
+        return  # the reference arm runs on rank 0 only
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import pbe_gb300 as pg
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    x, N, t_q, bw_q, ap, bp = workload()
+    f64 = dict(dtype=torch.float64, device=dev)
+    dN, dx = torch.tensor(N, **f64), torch.tensor(x, **f64)
+    dt, db = torch.tensor(t_q, **f64), torch.tensor(bw_q, **f64)
+    rhs = torch.zeros(N_BINS, **f64)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    hN = torch.tensor(N, dtype=torch.float64).pin_memory()
+    hR = torch.empty(N_BINS, dtype=torch.float64).pin_memory()
+
+    mode = pg.MODE_GATHER if args.mode == "gather" else pg.MODE_SCATTER
+    if args.impl == "reference":
+        import pyoracle
+
+        ref = pyoracle.RefRunner()
+
+        def step(n_dev):
+            rhs.zero_()
+            pg.check(ref.aggregation_rhs(n_dev, dx, rhs, ap, stream), "reference aggregation")
+            pg.check(ref.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream), "reference breakage")
+        launches_per_step = 3
+    else:
+        def step(n_dev):
+            rhs.zero_()
+            pg.check(pg.aggregation_rhs(n_dev, dx, rhs, ap, stream=stream, mode=mode), "aggregation")
+            pg.check(pg.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream=stream, mode=mode), "breakage")
+        launches_per_step = 4 + (2 if mode == pg.MODE_GATHER else 1)
+
+    clocks = ClockSampler(local)
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step(dN)
+        stream.synchronize()
+        clocks.start()
+        time.sleep(0.3)
+
+        # ---- value: device-resident inputs, L2 flushed before each step ----
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        main_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                    for _ in range(args.steps)]
+        for a, b in main_evs:   # torch creates the CUDA events on first record
+            a.record(stream)
+            b.record(stream)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            if args.impl == "ours":
+                pg.load().pbe_set_profile_events(main_evs[k][0].cuda_event, main_evs[k][1].cuda_event)
+            evs[k][0].record(stream)
+            step(dN)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        if args.impl == "ours":
+            pg.load().pbe_set_profile_events(None, None)
+        step_ms = [a.elapsed_time(b) for a, b in evs]
+        total_ms = sum(step_ms)
+        main_ms = [a.elapsed_time(b) for a, b in main_evs] if args.impl == "ours" else []
+
+        # ---- e2e: host buffers through the C ABI, copies inside the timing ----
+        e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+        dN2 = torch.empty_like(dN)
+        for k in range(args.steps):
+            flush.zero_()
+            e2e_evs[k][0].record(stream)
+            dN2.copy_(hN, non_blocking=True)
+            step(dN2)
+            hR.copy_(rhs, non_blocking=True)
+            e2e_evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs)
+        time.sleep(0.2)
+        clk = clocks.stop()
+
+    if dist is not None:
+        t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_ms = float(t[0]), float(t[1])
+    n_gpus = world if dist is not None else 1
+    value = n_gpus * args.steps / (total_ms / 1e3)
+    e2e_value = n_gpus * args.steps / (e2e_ms / 1e3)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    out = {
+        "metric": "Agg+br RHS evals/s at N=16384 FP64",
+        "value": round(value, 3),
+        "unit": "evals/s",
+        "n_gpus": n_gpus,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": round(total_ms / args.steps, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded lognormal N on the stated grid)",
+        "config": {"workload": "single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), "
+                               "Brownian+shear (beta_br=6.73e-18, beta_sh=4*50/3) + threshold "
+                               "breakage (S0=1e-3, v_min=x_8192), symmetric daughter as n_quad=16",
+                   "n": N_BINS, "n_quad": N_QUAD, "mode": args.mode if args.impl == "ours" else "reference",
+                   "pairs_per_eval": PAIRS, "fragments_per_eval": FRAGMENTS,
+                   "l2": "flushed before every timed step (512 MiB write)",
+                   "parallelism": "replicas" if n_gpus > 1 else "single GPU"},
+        "pair_interactions_per_s": round(value * PAIRS, 1),
+        "wall_s_timed_loop": round(wall, 4),
+        "e2e": {"value": round(e2e_value, 3), "unit": "evals/s",
+                "h2d_bytes_per_step": N_BINS * 8, "d2h_bytes_per_step": N_BINS * 8},
+        "gpu_launches": launches_per_step * args.steps if args.impl == "ours" else 0,
+        "clocks": clk,
+    }
+    if args.impl == "reference":
+        out["impl"] = "reference"
+        out["reference_build"] = ("acuoci/pbe-fixed-pivot-cuda src/aggregation.cu + src/breakage.cu, "
+                                  "unmodified, nvcc -O3 for sm_103a (oracle/build_ref.sh), "
+                                  "launched with the reference launch geometry")
+        out["reference_kernel_launches"] = launches_per_step * args.steps
+    else:
+        peak = fp64_peak_tflops(stream)
+        mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
+        achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
+        out["roofline"] = {
+            "bound": "fp64",
+            "kernel": "agg_main_kernel<5>",
+            "achieved": round(achieved, 4) if achieved else None,
+            "peak": round(peak, 4) if peak else None,
+            "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4) if (achieved and peak) else None,
+            "traffic": None,
+            "kernel_ms": round(mk * 1e3, 5) if mk else None,
+            "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
+            "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so); no FP64 entry in "
+                           "MEASURED_PEAKS.json",
+        }
+    if n_gpus == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(x, N, t_q, bw_q, ap, bp)
+    print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,279 @@
+// =============================================================================
+// oracle/pbe_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// Serial FP64 CPU restatement of the fixed-pivot population-balance RHS of
+// acuoci/pbe-fixed-pivot-cuda. It is the checker for the CUDA library in this
+// repository: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+// leg load it. The product never links, calls or falls back to it.
+//
+// Every function states the reference lines it follows (paths relative to the
+// reference project). The algorithm is restated pair by pair / fragment by
+// fragment in plain loops, in the reference's arithmetic order, so that the
+// result differs from the reference only by summation order and by libm
+// versus CUDA ulp differences in cbrt/log/pow.
+//
+// Besides rhs the functions can accumulate scale[i] = sum of |contribution|
+// deposited into bin i (death and birth terms alike). Parity tests use it to
+// define the per-bin tolerance |gpu_i - ref_i| <= tol * scale_i, which stays
+// meaningful in bins where birth and death nearly cancel.
+//
+// Pinning: tests/test_oracle_golden.py checks these functions against rhs
+// vectors produced by the reference's own CUDA kernels (built unmodified from
+// its sources by oracle/build_ref.sh) and against the known-answer tests of
+// tests/unit/test_aggregation.cpp and tests/unit/test_breakage.cpp.
+// =============================================================================
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// Aggregation frequency beta(xj, xk):
+// src/aggregation_kernels.cuh:56-89 (eval_kernel_t<0..5>).
+inline double beta_ref(int kernel, double xj, double xk,
+                       double b0, double b_br, double b_sh)
+{
+    switch (kernel) {
+    case 0: return b0;
+    case 1: return b0 * (xj + xk);
+    case 2: return b0 * xj * xk;
+    case 3: {
+        double xj3 = std::cbrt(xj), xk3 = std::cbrt(xk);
+        return b_br * (xj3 / xk3 + xk3 / xj3 + 2.0);
+    }
+    case 4: {
+        double s = std::cbrt(xj) + std::cbrt(xk);
+        return b_sh * s * s * s;
+    }
+    case 5: {
+        double xj3 = std::cbrt(xj), xk3 = std::cbrt(xk);
+        double br = b_br * (xj3 / xk3 + xk3 / xj3 + 2.0);
+        double sh = b_sh * (xj3 + xk3) * (xj3 + xk3) * (xj3 + xk3);
+        return br + sh;
+    }
+    default: return 0.0;
+    }
+}
+
+// Right bracket of v: src/aggregation_kernels.cuh:118-134 (bin_index).
+// Geometric grids (inv_log_r != 0) use the logarithm formula with a clamp
+// and no verification; generic grids use binary search (x[lo] <= v < x[hi]).
+inline int bin_index_ref(const double* x, int n, double v,
+                         double log_x0, double inv_log_r)
+{
+    if (inv_log_r != 0.0) {
+        double pos = (std::log(v) - log_x0) * inv_log_r;
+        int hi = static_cast<int>(std::floor(pos)) + 1;
+        return std::min(n - 1, std::max(1, hi));
+    }
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) / 2;
+        if (x[mid] <= v) lo = mid; else hi = mid;
+    }
+    return hi;
+}
+
+// Left bracket: src/breakage_kernels.cuh:95-105 (bin_search).
+inline int bin_search_ref(const double* x, int n, double v)
+{
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (x[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Selection function: src/breakage_kernels.cuh:51-65 (eval_selection_t<0..3>).
+inline double selection_ref(int sel, double v, double S0, double v_ref,
+                            double alpha, double v_min)
+{
+    switch (sel) {
+    case 0: return S0;
+    case 1: return S0 * v / v_ref;
+    case 2: return S0 * std::pow(v / v_ref, alpha);
+    case 3: return (v > v_min) ? S0 : 0.0;
+    default: return 0.0;
+    }
+}
+
+inline void dep(double* rhs, double* scale, int i, double val)
+{
+    rhs[i] += val;
+    if (scale) scale[i] += std::fabs(val);
+}
+
+// One upper-triangle row j of the aggregation sum (pairs j <= k < n):
+// src/aggregation_kernels.cuh:176-231 for every k of the row.
+void aggregation_row(const double* N, const double* x, double* rhs,
+                     double* scale, int n, int j, double log_x0,
+                     double inv_log_r, int kernel, double b0, double b_br,
+                     double b_sh)
+{
+    const double xj = x[j], Nj = N[j];
+    for (int k = j; k < n; ++k) {
+        const double xk = x[k], Nk = N[k];
+        double rate = beta_ref(kernel, xj, xk, b0, b_br, b_sh) * Nj * Nk;
+        const bool diagonal = (j == k);
+        if (diagonal) rate *= 0.5;
+        // death (:213-221)
+        if (diagonal) {
+            dep(rhs, scale, j, -2.0 * rate);
+        } else {
+            dep(rhs, scale, j, -rate);
+            dep(rhs, scale, k, -rate);
+        }
+        // birth (:190-200, :223-231)
+        const double v = xj + xk;
+        if (v >= x[n - 1]) {
+            dep(rhs, scale, n - 1, rate);
+        } else if (v <= x[0]) {
+            dep(rhs, scale, 0, rate);
+        } else {
+            int hi = bin_index_ref(x, n, v, log_x0, inv_log_r);
+            int lo = hi - 1;
+            double w = (v - x[lo]) / (x[hi] - x[lo]);
+            dep(rhs, scale, lo, (1.0 - w) * rate);
+            dep(rhs, scale, hi, w * rate);
+        }
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+// Aggregation RHS, accumulated into rhs (+=) like launch_aggregation_rhs
+// (include/pbe_cuda/aggregation.cuh:115-120; kernel src/aggregation_kernels.cuh:145-239).
+// scale may be null. Returns 0, or 1 for n <= 0 / null pointers / bad kernel
+// (src/aggregation.cu:23-24, :54).
+int oracle_aggregation_rhs(const double* N, const double* x, double* rhs,
+                           double* scale, int n, double log_x0,
+                           double inv_log_r, int kernel, double beta0,
+                           double beta_br, double beta_sh)
+{
+    if (n <= 0 || !N || !x || !rhs || kernel < 0 || kernel > 5) return 1;
+    for (int j = 0; j < n; ++j)
+        aggregation_row(N, x, rhs, scale, n, j, log_x0, inv_log_r, kernel,
+                        beta0, beta_br, beta_sh);
+    return 0;
+}
+
+// Same sum, rows j split over threads with thread-private rhs buffers that are
+// summed in thread order at the end. Used only as the all-cores CPU baseline.
+int oracle_aggregation_rhs_mt(const double* N, const double* x, double* rhs,
+                              int n, double log_x0, double inv_log_r,
+                              int kernel, double beta0, double beta_br,
+                              double beta_sh, int nthreads)
+{
+    if (n <= 0 || !N || !x || !rhs || kernel < 0 || kernel > 5) return 1;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    std::vector<double> priv(static_cast<size_t>(nthreads) * n, 0.0);
+    #pragma omp parallel num_threads(nthreads)
+    {
+        const int t = omp_get_thread_num();
+        double* r = priv.data() + static_cast<size_t>(t) * n;
+        // rows are of unequal length (n - j): cyclic distribution balances them
+        #pragma omp for schedule(dynamic, 16)
+        for (int j = 0; j < n; ++j)
+            aggregation_row(N, x, r, nullptr, n, j, log_x0, inv_log_r, kernel,
+                            beta0, beta_br, beta_sh);
+    }
+    for (int t = 0; t < nthreads; ++t)
+        for (int i = 0; i < n; ++i) rhs[i] += priv[static_cast<size_t>(t) * n + i];
+    return 0;
+#else
+    (void)nthreads;
+    for (int j = 0; j < n; ++j)
+        aggregation_row(N, x, rhs, nullptr, n, j, log_x0, inv_log_r, kernel,
+                        beta0, beta_br, beta_sh);
+    return 0;
+#endif
+}
+
+// Breakage RHS (+=) like launch_breakage_rhs (include/pbe_cuda/breakage.cuh:122-129).
+// Death: src/breakage_kernels.cuh:115-133. Birth: :160-251. Guard
+// S != 0 && N > 2.2e-308 on both (:131, :195). Returns 1 on the argument
+// errors of src/breakage.cu:23-24, :46, :74.
+int oracle_breakage_rhs(const double* N, const double* x, const double* t_q,
+                        const double* bw_q, double* rhs, double* scale, int n,
+                        int n_quad, int selection, double S0, double v_ref,
+                        double alpha, double v_min)
+{
+    if (n <= 0 || n_quad <= 0) return 1;
+    if (!N || !x || !t_q || !bw_q || !rhs) return 1;
+    if (selection < 0 || selection > 3) return 1;
+    // death kernel runs first on the stream (src/breakage.cu:30-50)
+    for (int j = 0; j < n; ++j) {
+        double Sj = selection_ref(selection, x[j], S0, v_ref, alpha, v_min);
+        if (Sj != 0.0 && N[j] > 2.2e-308) dep(rhs, scale, j, -(Sj * N[j]));
+    }
+    for (int j = 0; j < n; ++j) {
+        const double xj = x[j], Nj = N[j];
+        const double Sj = selection_ref(selection, xj, S0, v_ref, alpha, v_min);
+        if (!(Sj != 0.0 && Nj > 2.2e-308)) continue;
+        for (int q = 0; q < n_quad; ++q) {
+            const double contrib = Sj * Nj * bw_q[q];
+            const double v = xj * t_q[q];
+            if (v <= x[0]) {
+                dep(rhs, scale, 0, contrib);
+            } else if (v >= x[n - 1]) {
+                dep(rhs, scale, n - 1, contrib);
+            } else {
+                int lo = bin_search_ref(x, n, v);
+                int hi = lo + 1;
+                double eta = (v - x[lo]) / (x[hi] - x[lo]);
+                dep(rhs, scale, lo, (1.0 - eta) * contrib);
+                dep(rhs, scale, hi, eta * contrib);
+            }
+        }
+    }
+    return 0;
+}
+
+// Classical RK4 step on the host (examples/common/pbe_examples_utils.hpp:409-456):
+// k1 = R(N), k2 = R(N + dt/2 k1), k3 = R(N + dt/2 k2), k4 = R(N + dt k3),
+// N += dt/6 (k1 + 2k2 + 2k3 + k4), where R = aggregation + breakage into a
+// zeroed rhs (examples/flocculation_two_stage/main.cpp:333-351). A negative
+// agg_kernel skips aggregation; n_quad <= 0 skips breakage.
+int oracle_rk4_step(double* N, const double* x, int n, double dt,
+                    int agg_kernel, double log_x0, double inv_log_r,
+                    double beta0, double beta_br, double beta_sh,
+                    const double* t_q, const double* bw_q, int n_quad,
+                    int selection, double S0, double v_ref, double alpha,
+                    double v_min)
+{
+    if (n <= 0 || !N || !x) return 1;
+    std::vector<double> k1(n), k2(n), k3(n), k4(n), stage(n);
+    auto R = [&](const double* Nin, double* out) {
+        std::fill(out, out + n, 0.0);
+        if (agg_kernel >= 0)
+            oracle_aggregation_rhs(Nin, x, out, nullptr, n, log_x0, inv_log_r,
+                                   agg_kernel, beta0, beta_br, beta_sh);
+        if (n_quad > 0)
+            oracle_breakage_rhs(Nin, x, t_q, bw_q, out, nullptr, n, n_quad,
+                                selection, S0, v_ref, alpha, v_min);
+    };
+    R(N, k1.data());
+    for (int i = 0; i < n; ++i) stage[i] = N[i] + 0.5 * dt * k1[i];
+    R(stage.data(), k2.data());
+    for (int i = 0; i < n; ++i) stage[i] = N[i] + 0.5 * dt * k2[i];
+    R(stage.data(), k3.data());
+    for (int i = 0; i < n; ++i) stage[i] = N[i] + dt * k3[i];
+    R(stage.data(), k4.data());
+    for (int i = 0; i < n; ++i)
+        N[i] += (dt / 6.0) * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]);
+    return 0;
+}
+
+int oracle_version(void) { return 1; }
+
+} // extern "C"

@@ -1,0 +1,167 @@
+"""ctypes binding of the CPU oracle and of the reference-kernel runner.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py (CPU-baseline leg and reference arm). The library never imports it.
+
+  * liboracle.so (oracle/pbe_oracle.cpp): serial FP64 restatement of the
+    reference RHS; returns rhs and the per-bin scale sum |contribution|.
+  * libref_runner.so (oracle/ref_runner.cpp): launches the reference's own
+    kernels from oracle/_ref/*.cubin (built by oracle/build_ref.sh).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
+RUNNER_LIB = os.path.join(HERE, "_build", "libref_runner.so")
+REF_AGG_CUBIN = os.path.join(HERE, "_ref", "ref_aggregation.cubin")
+REF_BRK_CUBIN = os.path.join(HERE, "_ref", "ref_breakage.cubin")
+
+_D = ctypes.POINTER(ctypes.c_double)
+_o = None
+
+
+def _lib():
+    global _o
+    if _o is None:
+        if not os.path.isfile(ORACLE_LIB):
+            raise ImportError("oracle not built: %s (run build())" % ORACLE_LIB)
+        lib = ctypes.CDLL(ORACLE_LIB)
+        lib.oracle_aggregation_rhs.restype = ctypes.c_int
+        lib.oracle_aggregation_rhs.argtypes = [_D, _D, _D, _D, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double]
+        lib.oracle_aggregation_rhs_mt.restype = ctypes.c_int
+        lib.oracle_aggregation_rhs_mt.argtypes = [_D, _D, _D, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        lib.oracle_breakage_rhs.restype = ctypes.c_int
+        lib.oracle_breakage_rhs.argtypes = [_D, _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_double]
+        lib.oracle_rk4_step.restype = ctypes.c_int
+        lib.oracle_rk4_step.argtypes = [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, _D, _D, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double]
+        _o = lib
+    return _o
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def aggregation_rhs(N, x, kernel, beta0=1.0, beta_br=0.0, beta_sh=0.0, log_x0=0.0,
+                    inv_log_r=0.0, rhs=None, n=None):
+    """Returns (rhs, scale, code); rhs is accumulated into a copy of `rhs` (zeros if None)."""
+    N = _f64(N)
+    x = _f64(x)
+    n = len(x) if n is None else n
+    out = np.zeros(max(n, 1)) if rhs is None else _f64(rhs).copy()
+    scale = np.zeros_like(out)
+    code = _lib().oracle_aggregation_rhs(_dp(N), _dp(x), _dp(out), _dp(scale), int(n),
+                                         float(log_x0), float(inv_log_r), int(kernel),
+                                         float(beta0), float(beta_br), float(beta_sh))
+    return out, scale, code
+
+
+def aggregation_rhs_mt(N, x, kernel, beta0=1.0, beta_br=0.0, beta_sh=0.0, log_x0=0.0,
+                       inv_log_r=0.0, nthreads=0):
+    N = _f64(N)
+    x = _f64(x)
+    out = np.zeros(len(x))
+    code = _lib().oracle_aggregation_rhs_mt(_dp(N), _dp(x), _dp(out), len(x), float(log_x0),
+                                            float(inv_log_r), int(kernel), float(beta0),
+                                            float(beta_br), float(beta_sh), int(nthreads))
+    return out, code
+
+
+def breakage_rhs(N, x, t_q, bw_q, selection, S0=1.0, v_ref=1.0, alpha=1.0, v_min=0.0,
+                 rhs=None, n=None, n_quad=None):
+    N = _f64(N)
+    x = _f64(x)
+    t_q = _f64(t_q)
+    bw_q = _f64(bw_q)
+    n = len(x) if n is None else n
+    nq = len(t_q) if n_quad is None else n_quad
+    out = np.zeros(max(n, 1)) if rhs is None else _f64(rhs).copy()
+    scale = np.zeros_like(out)
+    code = _lib().oracle_breakage_rhs(_dp(N), _dp(x), _dp(t_q), _dp(bw_q), _dp(out), _dp(scale),
+                                      int(n), int(nq), int(selection), float(S0), float(v_ref),
+                                      float(alpha), float(v_min))
+    return out, scale, code
+
+
+def rk4_step(N, x, dt, agg=None, brk=None):
+    """One classical RK4 step; agg = dict(kernel, beta0, beta_br, beta_sh[, log_x0, inv_log_r]),
+    brk = dict(t_q, bw_q, selection, S0, v_ref, alpha, v_min). Returns the new N."""
+    N = _f64(N).copy()
+    x = _f64(x)
+    a = agg or {}
+    b = brk or {}
+    tq = _f64(b["t_q"]) if brk else None
+    bw = _f64(b["bw_q"]) if brk else None
+    code = _lib().oracle_rk4_step(
+        _dp(N), _dp(x), len(x), float(dt), int(a.get("kernel", -1)) if agg else -1,
+        float(a.get("log_x0", 0.0)), float(a.get("inv_log_r", 0.0)), float(a.get("beta0", 1.0)),
+        float(a.get("beta_br", 0.0)), float(a.get("beta_sh", 0.0)), _dp(tq), _dp(bw),
+        len(tq) if brk else 0, int(b.get("selection", 0)), float(b.get("S0", 1.0)),
+        float(b.get("v_ref", 1.0)), float(b.get("alpha", 1.0)), float(b.get("v_min", 0.0)))
+    if code:
+        raise RuntimeError("oracle_rk4_step failed")
+    return N
+
+
+class RefRunner:
+    """The reference's CUDA kernels (unmodified, from oracle/_ref) on the GPU."""
+
+    def __init__(self):
+        if not (os.path.isfile(RUNNER_LIB) and os.path.isfile(REF_AGG_CUBIN)
+                and os.path.isfile(REF_BRK_CUBIN)):
+            raise FileNotFoundError("reference runner or cubins missing under oracle/")
+        import torch  # noqa: F401  (initialises the runtime's primary context)
+
+        torch.cuda.init()
+        torch.zeros(1, device="cuda")
+        from pbe_gb300 import AggregationParams, BreakageParams
+
+        self._AP, self._BP = AggregationParams, BreakageParams
+        lib = ctypes.CDLL(RUNNER_LIB)
+        lib.ref_init.restype = ctypes.c_int
+        lib.ref_init.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        lib.ref_aggregation_rhs.restype = ctypes.c_int
+        lib.ref_aggregation_rhs.argtypes = [ctypes.c_void_p] * 3 + [ctypes.POINTER(AggregationParams),
+                                                                     ctypes.c_void_p]
+        lib.ref_breakage_rhs.restype = ctypes.c_int
+        lib.ref_breakage_rhs.argtypes = [ctypes.c_void_p] * 5 + [ctypes.POINTER(BreakageParams),
+                                                                  ctypes.c_void_p]
+        code = lib.ref_init(REF_AGG_CUBIN.encode(), REF_BRK_CUBIN.encode())
+        if code:
+            raise RuntimeError("ref_init failed: %d" % code)
+        self.lib = lib
+
+    @staticmethod
+    def _stream(stream):
+        import torch
+
+        s = torch.cuda.current_stream() if stream is None else stream
+        return s.cuda_stream or None
+
+    def aggregation_rhs(self, N, x, rhs, params, stream=None):
+        return self.lib.ref_aggregation_rhs(N.data_ptr(), x.data_ptr(), rhs.data_ptr(), params,
+                                            self._stream(stream))
+
+    def breakage_rhs(self, N, x, t_q, bw_q, rhs, params, stream=None):
+        return self.lib.ref_breakage_rhs(N.data_ptr(), x.data_ptr(), t_q.data_ptr(),
+                                         bw_q.data_ptr(), rhs.data_ptr(), params,
+                                         self._stream(stream))

@@ -1,0 +1,162 @@
+// =============================================================================
+// breakage.cu -- fixed-pivot breakage RHS for GB300 (sm_103a), FP64.
+//
+// Reference semantics (acuoci/pbe-fixed-pivot-cuda src/breakage_kernels.cuh):
+//   death (:115-133): rhs[j] -= S(x_j) N_j       if S != 0 && N_j > 2.2e-308
+//   birth (:160-251): for every parent j and quadrature point q with the same
+//     guard, contrib = S_j N_j bw_q, v = x_j t_q; v <= x[0] -> bin 0,
+//     v >= x[n-1] -> bin n-1, else split onto lo, lo+1 with
+//     eta = (v - x_lo)/(x_{lo+1} - x_lo) (lo from a binary search, :95-105).
+//   selection S (:51-65): S0 | S0 v/v_ref | S0 (v/v_ref)^alpha | (v > v_min) S0.
+//
+// GATHER (deterministic): one thread per fragment (q, j) computes its bracket
+// and its two shares; since v = x_j t_q grows with j, the fragments of one q
+// landing on bracket m form a contiguous run of j, whose first index is
+// recorded in first[q][m]. One thread per output bin i then adds, in fixed
+// order: -S_i N_i, then for every q the hi-shares of bracket i-1 and the
+// lo-shares of bracket i (bin 0 also takes the fragments clipped below x[0]).
+// SCATTER: one thread per fragment adds its shares with FP64 atomicAdd.
+// =============================================================================
+#include "pbe_internal.cuh"
+
+namespace pbe_gb300 {
+namespace {
+
+template <int F>
+__device__ __forceinline__ double selection(double v, double S0, double v_ref, double alpha,
+                                            double v_min)
+{
+    if constexpr (F == 0) return S0;
+    else if constexpr (F == 1) return S0 * v / v_ref;
+    else if constexpr (F == 2) return S0 * pow(v / v_ref, alpha);
+    else return (v > v_min) ? S0 : 0.0;
+}
+
+// Bracket of a fragment volume: -1 when clipped to bin 0 (v <= x[0]), n-1 when
+// clipped to bin n-1 (v >= x[n-1]), else lo with x[lo] <= v < x[lo+1].
+__device__ __forceinline__ int frag_bracket(const double* __restrict__ x, int n, double v)
+{
+    if (dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
+    if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
+    return bracket_lo(x, n, v);
+}
+
+// Shares of one fragment: (to lo, to lo+1). Clipped fragments put everything
+// into the first share.
+__device__ __forceinline__ void frag_shares(const double* __restrict__ x, int n, int lo, double v,
+                                            double contrib, double& clo, double& chi)
+{
+    if (lo < 0 || lo >= n - 1) { clo = contrib; chi = 0.0; return; }
+    const double xl = __ldg(x + lo), xh = __ldg(x + lo + 1);
+    const double q = contrib / (xh - xl);
+    clo = q * (xh - v);
+    chi = q * (v - xl);
+}
+
+template <int F>
+__global__ void __launch_bounds__(256)
+brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                const double* __restrict__ t_q, const double* __restrict__ bw_q, int n, int nq,
+                BrkWs ws, double S0, double v_ref, double alpha, double v_min)
+{
+    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long long>(n) * nq) return;
+    const int q = static_cast<int>(idx / n);
+    const int j = static_cast<int>(idx - static_cast<long long>(q) * n);
+    const double xj = x[j], Nj = N[j];
+    const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
+    const bool active = (S != 0.0) && (Nj > kBreakageNMin);
+    const double tq = t_q[q];
+    const double contrib = active ? S * Nj * bw_q[q] : 0.0;
+    const double v = xj * tq;
+    const int lo = frag_bracket(x, n, v);
+    double clo, chi;
+    frag_shares(x, n, lo, v, contrib, clo, chi);
+    ws.lo[idx] = lo;
+    ws.clo[idx] = clo;
+    ws.chi[idx] = chi;
+    // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
+    int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+    const int lo_prev = (j == 0) ? -2 : frag_bracket(x, n, x[j - 1] * tq);
+    for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
+    if (j == n - 1)
+        for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
+    if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
+}
+
+__global__ void __launch_bounds__(256)
+brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = rhs[i] - ws.SN[i];
+    for (int q = 0; q < nq; ++q) {
+        const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+        const long long base = static_cast<long long>(q) * n;
+        // clamp: entries are in [0, n] for monotone brackets (t_q > 0)
+        const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
+        const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
+        const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
+        if (i == 0) { for (int j = 0; j < fb; ++j) acc += ws.clo[base + j]; }   // lo == -1
+        else        { for (int j = fa; j < fb; ++j) acc += ws.chi[base + j]; }  // lo == i-1
+        for (int j = fb; j < fc; ++j) acc += ws.clo[base + j];                  // lo == i
+    }
+    rhs[i] = acc;
+}
+
+template <int F>
+__global__ void __launch_bounds__(256)
+brk_scatter_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                   const double* __restrict__ t_q, const double* __restrict__ bw_q, double* rhs,
+                   int n, int nq, double S0, double v_ref, double alpha, double v_min)
+{
+    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long long>(n) * nq) return;
+    const int q = static_cast<int>(idx / n);
+    const int j = static_cast<int>(idx - static_cast<long long>(q) * n);
+    const double xj = x[j], Nj = N[j];
+    const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
+    if (!((S != 0.0) && (Nj > kBreakageNMin))) return;
+    if (q == 0) atomicAdd(rhs + j, -(S * Nj));
+    const double contrib = S * Nj * bw_q[q];
+    const double v = xj * t_q[q];
+    const int lo = frag_bracket(x, n, v);
+    double clo, chi;
+    frag_shares(x, n, lo, v, contrib, clo, chi);
+    if (lo < 0) { atomicAdd(rhs, clo); return; }
+    atomicAdd(rhs + lo, clo);
+    if (lo < n - 1) atomicAdd(rhs + lo + 1, chi);
+}
+
+template <int F>
+cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s)
+{
+    const long long m = static_cast<long long>(a.n) * a.n_quad;
+    const int grid = static_cast<int>((m + 255) / 256);
+    if (scatter) {
+        brk_scatter_kernel<F><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.rhs, a.n, a.n_quad,
+                                                   a.S0, a.v_ref, a.alpha, a.v_min);
+    } else {
+        BrkWs ws;
+        brk_ws_layout(a.n, a.n_quad, static_cast<char*>(ws_base), &ws);
+        brk_prep_kernel<F><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n, a.n_quad, ws, a.S0,
+                                                a.v_ref, a.alpha, a.v_min);
+        brk_gather_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.rhs, a.n, a.n_quad, ws);
+    }
+    return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t brk_launch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s)
+{
+    switch (a.selection) {
+    case 0: return launch_f<0>(a, scatter, ws_base, s);
+    case 1: return launch_f<1>(a, scatter, ws_base, s);
+    case 2: return launch_f<2>(a, scatter, ws_base, s);
+    case 3: return launch_f<3>(a, scatter, ws_base, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace pbe_gb300

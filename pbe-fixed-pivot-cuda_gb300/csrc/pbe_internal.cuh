@@ -1,0 +1,144 @@
+// =============================================================================
+// pbe_internal.cuh -- device helpers and scratch layouts shared by the
+// aggregation and breakage kernels of libpbe_gb300 (sm_103a, FP64).
+//
+// Design notes that the kernels rely on:
+//  * GB300 executes FP64 at 2 DFMA/clk/SM (1.2 TFLOP/s measured; FP64 MMA is
+//    no faster). Every FP64 instruction on the per-pair path counts, so
+//    comparisons of positive doubles are done on their bit patterns (INT pipe)
+//    and per-pair transcendental functions are hoisted to per-bin / per-lag
+//    tables computed once per call.
+//  * Positive IEEE doubles order like their int64 bit patterns.
+// =============================================================================
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace pbe_gb300 {
+
+// ---- launch geometry --------------------------------------------------------
+constexpr int kTileW        = 16;    // output bins owned by one task
+constexpr int kMainThreads  = 256;   // threads per aggregation task CTA
+constexpr int kPrepThreads  = 256;
+constexpr int kClipWarps    = 8;     // warps per block of the clip kernel
+constexpr int kScatterChunk = 2048;  // lags per task in scatter mode
+constexpr int kRedRows      = 2 * (kTileW + 1);   // R[0..W], TH[0..W]
+
+// A grid is treated as geometric when |log(x_i/x_0) - i*log(r)| <= kGeoTol for
+// every i (r fitted from the end points). Then the pivot ratio x_{j+d}/x_j
+// equals x_d/x_0 to ~4*kGeoTol, which keeps the lag tables within 1e-13 of
+// the per-pair values.
+constexpr double kGeoTol = 5e-14;
+constexpr int kLagClipAll = 0x3fffffff;   // lag d whose every pair is clipped
+
+// Guard of the reference breakage kernels (src/breakage_kernels.cuh:131, :195).
+constexpr double kBreakageNMin = 2.2e-308;
+
+__device__ __forceinline__ long long dbits(double v) { return __double_as_longlong(v); }
+
+// Left bracket lo in [0, n-2] with x[lo] <= v < x[lo+1], for x[0] < v < x[n-1]
+// (same result as the reference's binary searches, src/breakage_kernels.cuh:95-105
+// and src/aggregation_kernels.cuh:125-132), comparing bit patterns.
+__device__ __forceinline__ int bracket_lo(const double* __restrict__ x, int n, double v)
+{
+    const long long vb = dbits(v);
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (dbits(__ldg(x + mid)) <= vb) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ---- aggregation scratch ----------------------------------------------------
+struct AggWs {
+    double* h;         // [n]  x_i N_i
+    double* a;         // [n]  x_i^(1/3)
+    double* ia;        // [n]  1 / x_i^(1/3)
+    double* inv_dx;    // [n]  1 / (x_{i+1} - x_i)   (entry n-1 unused)
+    double* Bd;        // [n]  per-lag factor (see agg_prep_kernel)
+    double* Sd;        // [n]  per-lag factor multiplying x_j
+    int*    Ld;        // [n]  bracket offset of lag d: lo(j, j+d) = j + Ld[d]
+    double* mom_part;  // [nb_prep * 8] per-block moment partials
+    double* mom;       // [8]  M_{-1/3}, M_0, M_{1/3}, M_{2/3}, M_1, geo flag, max dev
+    double* clip_part; // [nb_clip] per-block sums of clipped pair rates
+    int*    counter;   // [8]  task counter(s)
+};
+
+inline int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
+inline int agg_clip_blocks(int n) { return (n + kClipWarps - 1) / kClipWarps; }
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Carves the aggregation scratch out of `base` (may be null to query the size).
+inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align256(bytes); return p; };
+    const size_t dn = sizeof(double) * static_cast<size_t>(n);
+    AggWs w{};
+    w.h         = reinterpret_cast<double*>(take(dn));
+    w.a         = reinterpret_cast<double*>(take(dn));
+    w.ia        = reinterpret_cast<double*>(take(dn));
+    w.inv_dx    = reinterpret_cast<double*>(take(dn));
+    w.Bd        = reinterpret_cast<double*>(take(dn));
+    w.Sd        = reinterpret_cast<double*>(take(dn));
+    w.Ld        = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(n)));
+    w.mom_part  = reinterpret_cast<double*>(take(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n))));
+    w.mom       = reinterpret_cast<double*>(take(sizeof(double) * 8));
+    w.clip_part = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(agg_clip_blocks(n))));
+    w.counter   = reinterpret_cast<int*>(take(sizeof(int) * 8));
+    if (ws) *ws = w;
+    return off;
+}
+
+// ---- breakage scratch (gather mode) ------------------------------------------
+struct BrkWs {
+    int*    lo;    // [nq * n]  left bracket of fragment (q, j); -1 = clipped to bin 0
+    double* clo;   // [nq * n]  share deposited at lo (whole contribution when clipped)
+    double* chi;   // [nq * n]  share deposited at lo + 1
+    int*    first; // [nq * (n + 2)]  first[q][m+1] = first j with lo(q, j) >= m, m in [-1, n]
+    double* SN;    // [n]  S(x_j) N_j (0 where the guard skips bin j)
+};
+
+inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align256(bytes); return p; };
+    const size_t m = static_cast<size_t>(n) * static_cast<size_t>(nq);
+    BrkWs w{};
+    w.lo    = reinterpret_cast<int*>(take(sizeof(int) * m));
+    w.clo   = reinterpret_cast<double*>(take(sizeof(double) * m));
+    w.chi   = reinterpret_cast<double*>(take(sizeof(double) * m));
+    w.first = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(nq) * (static_cast<size_t>(n) + 2)));
+    w.SN    = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(n)));
+    if (ws) *ws = w;
+    return off;
+}
+
+// ---- profiling hook ----------------------------------------------------------
+// When both are non-null the aggregation launcher records g_prof_start right
+// before and g_prof_stop right after its main (pair) kernel, on the call's
+// stream. Set through pbe_set_profile_events(); process-wide, not thread-safe.
+extern cudaEvent_t g_prof_start;
+extern cudaEvent_t g_prof_stop;
+
+// ---- host-side launchers (defined in aggregation.cu / breakage.cu) ----------
+struct AggArgs {
+    const double* N; const double* x; double* rhs;
+    int n; int kernel; double beta0, beta_br, beta_sh;
+};
+struct BrkArgs {
+    const double* N; const double* x; const double* t_q; const double* bw_q; double* rhs;
+    int n; int n_quad; int selection; double S0, v_ref, alpha, v_min;
+};
+
+// Launch the aggregation kernels with a scratch buffer `ws_base` of at least
+// agg_ws_layout(n) bytes. scatter selects the atomic-flush variant.
+cudaError_t agg_launch(const AggArgs& a, bool scatter, void* ws_base, int num_sms, cudaStream_t s);
+// Breakage: scatter needs no scratch (ws_base may be null).
+cudaError_t brk_launch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s);
+
+} // namespace pbe_gb300

@@ -1,0 +1,40 @@
+"""pbe_gb300 -- GB300 (sm_103a) fixed-pivot population-balance RHS.
+
+Python face of libpbe_gb300.so. The operator interface mirrors the reference
+pbe_cuda API (AggregationParams / BreakageParams, aggregation_rhs /
+breakage_rhs adding into a pre-zeroed rhs and returning a cudaError_t code).
+"""
+from ._lib import (  # noqa: F401
+    AGG_BROWNIAN,
+    AGG_BROWNIAN_SHEAR,
+    AGG_CONSTANT,
+    AGG_PRODUCT,
+    AGG_SHEAR,
+    AGG_SUM,
+    ERR_INVALID_CONFIGURATION,
+    ERR_INVALID_DEVICE_POINTER,
+    ERR_INVALID_VALUE,
+    LIB_PATH,
+    MODE_DEFAULT,
+    MODE_GATHER,
+    MODE_SCATTER,
+    SEL_CONSTANT,
+    SEL_LINEAR,
+    SEL_POWERLAW,
+    SEL_THRESHOLD,
+    AggregationParams,
+    BreakageParams,
+    PbeError,
+    check,
+    error_string,
+    load,
+)
+from .rhs import (  # noqa: F401
+    aggregation_rhs,
+    aggregation_workspace_bytes,
+    breakage_rhs,
+    breakage_workspace_bytes,
+)
+from . import grids, quadrature  # noqa: F401
+
+__version__ = "0.1.0"
