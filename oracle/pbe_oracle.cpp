@@ -112,10 +112,19 @@ inline void dep(double* rhs, double* scale, int i, double val)
 
 // One upper-triangle row j of the aggregation sum (pairs j <= k < n):
 // src/aggregation_kernels.cuh:176-231 for every k of the row.
+//
+// exact_bracket = 0 follows the reference literally: on a geometric grid
+// (inv_log_r != 0) the bracket comes from the floating-point logarithm, which
+// near a tie (v within a few ulps of a pivot) can select the neighbouring
+// bracket and extrapolate (w slightly outside [0, 1]). exact_bracket = 1 uses
+// the exact bracket x[lo] <= v < x[lo+1] (the reference's own generic-grid
+// search, :125-132) on every grid. When `misplaced` is non-null it receives,
+// per bin, |deposit(log bracket) - deposit(exact bracket)| summed over the
+// pairs where the two brackets differ: the reference's own rounding noise.
 void aggregation_row(const double* N, const double* x, double* rhs,
-                     double* scale, int n, int j, double log_x0,
-                     double inv_log_r, int kernel, double b0, double b_br,
-                     double b_sh)
+                     double* scale, double* misplaced, int n, int j,
+                     double log_x0, double inv_log_r, int kernel, double b0,
+                     double b_br, double b_sh, int exact_bracket)
 {
     const double xj = x[j], Nj = N[j];
     for (int k = j; k < n; ++k) {
@@ -137,11 +146,26 @@ void aggregation_row(const double* N, const double* x, double* rhs,
         } else if (v <= x[0]) {
             dep(rhs, scale, 0, rate);
         } else {
-            int hi = bin_index_ref(x, n, v, log_x0, inv_log_r);
-            int lo = hi - 1;
+            const int hi_log = bin_index_ref(x, n, v, log_x0, inv_log_r);
+            const int hi_ex = bin_index_ref(x, n, v, log_x0, 0.0);
+            const int hi = exact_bracket ? hi_ex : hi_log;
+            const int lo = hi - 1;
             double w = (v - x[lo]) / (x[hi] - x[lo]);
             dep(rhs, scale, lo, (1.0 - w) * rate);
             dep(rhs, scale, hi, w * rate);
+            if (misplaced && hi_log != hi_ex) {
+                const int h2 = exact_bracket ? hi_log : hi_ex;
+                const double w2 = (v - x[h2 - 1]) / (x[h2] - x[h2 - 1]);
+                // the two deposit vectors over bins {lo, hi} and {h2-1, h2}
+                double d[4] = {(1.0 - w) * rate, w * rate, -(1.0 - w2) * rate, -w2 * rate};
+                int b[4] = {lo, hi, h2 - 1, h2};
+                for (int a = 0; a < 4; ++a) {
+                    double s = 0.0;
+                    bool first = true;
+                    for (int c = 0; c < 4; ++c) if (b[c] == b[a]) { if (c < a) first = false; s += d[c]; }
+                    if (first) misplaced[b[a]] += std::fabs(s);
+                }
+            }
         }
     }
 }
@@ -152,17 +176,18 @@ extern "C" {
 
 // Aggregation RHS, accumulated into rhs (+=) like launch_aggregation_rhs
 // (include/pbe_cuda/aggregation.cuh:115-120; kernel src/aggregation_kernels.cuh:145-239).
-// scale may be null. Returns 0, or 1 for n <= 0 / null pointers / bad kernel
-// (src/aggregation.cu:23-24, :54).
+// scale / misplaced may be null (see aggregation_row). Returns 0, or 1 for
+// n <= 0 / null pointers / bad kernel (src/aggregation.cu:23-24, :54).
 int oracle_aggregation_rhs(const double* N, const double* x, double* rhs,
-                           double* scale, int n, double log_x0,
-                           double inv_log_r, int kernel, double beta0,
-                           double beta_br, double beta_sh)
+                           double* scale, double* misplaced, int n,
+                           double log_x0, double inv_log_r, int kernel,
+                           double beta0, double beta_br, double beta_sh,
+                           int exact_bracket)
 {
     if (n <= 0 || !N || !x || !rhs || kernel < 0 || kernel > 5) return 1;
     for (int j = 0; j < n; ++j)
-        aggregation_row(N, x, rhs, scale, n, j, log_x0, inv_log_r, kernel,
-                        beta0, beta_br, beta_sh);
+        aggregation_row(N, x, rhs, scale, misplaced, n, j, log_x0, inv_log_r,
+                        kernel, beta0, beta_br, beta_sh, exact_bracket);
     return 0;
 }
 
@@ -184,8 +209,8 @@ int oracle_aggregation_rhs_mt(const double* N, const double* x, double* rhs,
         // rows are of unequal length (n - j): cyclic distribution balances them
         #pragma omp for schedule(dynamic, 16)
         for (int j = 0; j < n; ++j)
-            aggregation_row(N, x, r, nullptr, n, j, log_x0, inv_log_r, kernel,
-                            beta0, beta_br, beta_sh);
+            aggregation_row(N, x, r, nullptr, nullptr, n, j, log_x0, inv_log_r,
+                            kernel, beta0, beta_br, beta_sh, 0);
     }
     for (int t = 0; t < nthreads; ++t)
         for (int i = 0; i < n; ++i) rhs[i] += priv[static_cast<size_t>(t) * n + i];
@@ -193,8 +218,8 @@ int oracle_aggregation_rhs_mt(const double* N, const double* x, double* rhs,
 #else
     (void)nthreads;
     for (int j = 0; j < n; ++j)
-        aggregation_row(N, x, rhs, nullptr, n, j, log_x0, inv_log_r, kernel,
-                        beta0, beta_br, beta_sh);
+        aggregation_row(N, x, rhs, nullptr, nullptr, n, j, log_x0, inv_log_r,
+                        kernel, beta0, beta_br, beta_sh, 0);
     return 0;
 #endif
 }
@@ -256,8 +281,8 @@ int oracle_rk4_step(double* N, const double* x, int n, double dt,
     auto R = [&](const double* Nin, double* out) {
         std::fill(out, out + n, 0.0);
         if (agg_kernel >= 0)
-            oracle_aggregation_rhs(Nin, x, out, nullptr, n, log_x0, inv_log_r,
-                                   agg_kernel, beta0, beta_br, beta_sh);
+            oracle_aggregation_rhs(Nin, x, out, nullptr, nullptr, n, log_x0,
+                                   inv_log_r, agg_kernel, beta0, beta_br, beta_sh, 0);
         if (n_quad > 0)
             oracle_breakage_rhs(Nin, x, t_q, bw_q, out, nullptr, n, n_quad,
                                 selection, S0, v_ref, alpha, v_min);

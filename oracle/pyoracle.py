@@ -32,9 +32,9 @@ def _lib():
             raise ImportError("oracle not built: %s (run build())" % ORACLE_LIB)
         lib = ctypes.CDLL(ORACLE_LIB)
         lib.oracle_aggregation_rhs.restype = ctypes.c_int
-        lib.oracle_aggregation_rhs.argtypes = [_D, _D, _D, _D, ctypes.c_int, ctypes.c_double,
+        lib.oracle_aggregation_rhs.argtypes = [_D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_int, ctypes.c_double,
-                                               ctypes.c_double, ctypes.c_double]
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_int]
         lib.oracle_aggregation_rhs_mt.restype = ctypes.c_int
         lib.oracle_aggregation_rhs_mt.argtypes = [_D, _D, _D, ctypes.c_int, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_int, ctypes.c_double,
@@ -62,16 +62,27 @@ def _f64(a):
 
 
 def aggregation_rhs(N, x, kernel, beta0=1.0, beta_br=0.0, beta_sh=0.0, log_x0=0.0,
-                    inv_log_r=0.0, rhs=None, n=None):
-    """Returns (rhs, scale, code); rhs is accumulated into a copy of `rhs` (zeros if None)."""
+                    inv_log_r=0.0, rhs=None, n=None, exact_bracket=False,
+                    with_misplaced=False):
+    """Returns (rhs, scale, code) -- or (rhs, scale, misplaced, code) with
+    with_misplaced -- accumulated into a copy of `rhs` (zeros if None).
+
+    exact_bracket=False restates the reference literally (logarithm bracket on
+    geometric grids); True uses the exact bracket x[lo] <= v < x[lo+1]
+    everywhere. `misplaced` is the per-bin size of the reference's near-tie
+    bracket misplacements (see oracle/pbe_oracle.cpp)."""
     N = _f64(N)
     x = _f64(x)
     n = len(x) if n is None else n
     out = np.zeros(max(n, 1)) if rhs is None else _f64(rhs).copy()
     scale = np.zeros_like(out)
-    code = _lib().oracle_aggregation_rhs(_dp(N), _dp(x), _dp(out), _dp(scale), int(n),
+    mis = np.zeros_like(out)
+    code = _lib().oracle_aggregation_rhs(_dp(N), _dp(x), _dp(out), _dp(scale), _dp(mis), int(n),
                                          float(log_x0), float(inv_log_r), int(kernel),
-                                         float(beta0), float(beta_br), float(beta_sh))
+                                         float(beta0), float(beta_br), float(beta_sh),
+                                         1 if exact_bracket else 0)
+    if with_misplaced:
+        return out, scale, mis, code
     return out, scale, code
 
 

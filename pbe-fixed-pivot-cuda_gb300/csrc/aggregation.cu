@@ -19,8 +19,9 @@
 //  * Geometric grids (verified on the device, see agg_prep_kernel): the
 //    bracket offset lo - j, the Brownian factor and the shear factor depend on
 //    the lag d = k - j only. They come from per-lag tables, so a pair costs
-//    3-7 FP64 operations. v - x_lo is formed from the actual pivots, exactly
-//    as the reference forms it; when lo = k the numerator is x_j itself.
+//    2-5 FP64 operations plus the weight. The weight numerator is
+//    fl(x_j + x_k) - x_lo from the actual pivots, exactly as the reference
+//    forms it (in 2^s-scaled units, see AggWs).
 //  * Generic grids: per-pair brackets by a monotone walk over k, beta from
 //    per-bin cube roots.
 //  * Pairs clipped at x[n-1] are summed by a separate kernel (per lag on a
@@ -150,10 +151,13 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         const double hi = xi * Ni;
         const double ai = cbrt(xi);
         const double iai = 1.0 / ai;
+        const int s = -ilogb(x[n - 1]);
+        const double xsi = scalbn(xi, s);
         ws.h[i] = hi;
         ws.a[i] = ai;
         ws.ia[i] = iai;
-        ws.inv_dx[i] = (i < n - 1) ? 1.0 / (x[i + 1] - xi) : 0.0;
+        ws.xs[i] = xsi;
+        ws.inv_dx[i] = (i < n - 1) ? 1.0 / (scalbn(x[i + 1], s) - xsi) : 0.0;
         m[0] = iai * Ni; m[1] = Ni; m[2] = ai * Ni; m[3] = (ai * ai) * Ni; m[4] = hi;
 
         const double x0 = x[0];
@@ -244,12 +248,12 @@ agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, doub
             }
         } else {
             const int j = w;
-            const double xj = x[j];
-            const long long tb = dbits(x[n - 1]);
+            const double xj = ws.xs[j];
+            const long long tb = dbits(ws.xs[n - 1]);
             int lo = j, hi = n - 1;   // xj + x[n-1] >= x[n-1] always holds
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (dbits(xj + x[mid]) >= tb) hi = mid; else lo = mid + 1;
+                if (dbits(xj + ws.xs[mid]) >= tb) hi = mid; else lo = mid + 1;
             }
             const double Nj = N[j], hj = ws.h[j], aj = ws.a[j], iaj = ws.ia[j];
             for (int k = lo + lane; k < n; k += 32)
@@ -305,8 +309,13 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 
         if (tid < W + 2) {
             const int s = I - 1 + tid;
-            xs[tid] = (s >= 0 && s < n) ? x[s] : 0.0;
+            xs[tid] = (s >= 0 && s < n) ? ws.xs[s] : 0.0;
         }
+        // Per-task exponent shift of the weight numerators: th ~ x_I (r-1) is
+        // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
+        // the reference's w*rate even on grids spanning hundreds of octaves.
+        const int St = -ilogb(ws.xs[I]);
+        const int St20 = St << 20;
         __syncthreads();
 
         if (geo) {
@@ -317,7 +326,6 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
             for (int d = d_begin + tid; d < d_end; d += kMainThreads) {
                 const int L = __ldg(ws.Ld + d);
                 if (L > smax) break;           // Ld is nondecreasing in d
-                const int e = L - d;           // lo - k
                 const double B = __ldg(ws.Bd + d), S = __ldg(ws.Sd + d);
                 const int jb = I - 1 - L;      // j of slot t is jb + t, k = jb + d + t
                 const int tlo = max(0, -jb);
@@ -329,9 +337,9 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                         const double hj = NeedH<K>::j ? __ldg(ws.h + j) : 0.0;
                         const double hk = NeedH<K>::k ? __ldg(ws.h + k) : 0.0;
                         const double rate = rate_geo<K>(B, S, Nj, hj, Nk, hk);
-                        double th;
-                        if (e == 0) th = __ldg(x + j);                      // v - x_k = x_j
-                        else th = (__ldg(x + j) + __ldg(x + k)) - xs[t];    // fl(v) - x_lo
+                        // fl(x_j + x_k) - x_lo, the reference's weight numerator
+                        const double th =
+                            scale_pow2((__ldg(ws.xs + j) + __ldg(ws.xs + k)) - xs[t], St20);
                         if (t > 0) R[t] += rate;
                         TH[t] = fma(rate, th, TH[t]);
                     }
@@ -351,21 +359,22 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const int t_last = smax - (I - 1);
                 const long long blo = dbits(xs[t_first]);
                 const long long bhi = dbits(xs[t_last + 1]);
-                const double xlast = x[n - 1];
+                const double* __restrict__ xsc = ws.xs;      // scaled pivots (bracket
+                const double xlast = xsc[n - 1];            // decisions are unchanged)
                 for (int j = tid; j <= smax; j += kMainThreads) {
-                    const double xj = x[j];
+                    const double xj = xsc[j];
                     if (dbits(xj + xj) >= bhi) break;          // v >= 2 x_j grows with j
                     if (dbits(xj + xlast) < blo) continue;     // this row never reaches the tile
                     int lo = j, hi = n - 1;
                     while (lo < hi) {
                         const int mid = (lo + hi) >> 1;
-                        if (dbits(xj + x[mid]) >= blo) hi = mid; else lo = mid + 1;
+                        if (dbits(xj + xsc[mid]) >= blo) hi = mid; else lo = mid + 1;
                     }
                     const int ka = lo;
                     hi = n;
                     while (lo < hi) {
                         const int mid = (lo + hi) >> 1;
-                        if (dbits(xj + x[mid]) >= bhi) hi = mid; else lo = mid + 1;
+                        if (dbits(xj + xsc[mid]) >= bhi) hi = mid; else lo = mid + 1;
                     }
                     const int kb = lo;
                     if (ka >= kb) continue;
@@ -373,7 +382,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                     int t = t_first;
                     double Rc = 0.0, THc = 0.0;
                     for (int k = ka; k < kb; ++k) {
-                        const double v = xj + x[k];
+                        const double v = xj + xsc[k];
                         const long long vb = dbits(v);
                         while (t < t_last && dbits(xs[t + 1]) <= vb) {
                             red[t * kMainThreads + tid] += Rc;
@@ -383,7 +392,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                         const double rate = rate_gen<K>(j == k, b0, bbr, bsh, Nj, hj, aj, iaj,
                                                         N[k], ws.h[k], ws.a[k], ws.ia[k]);
                         Rc += rate;
-                        THc = fma(rate, v - xs[t], THc);
+                        THc = fma(rate, scale_pow2(v - xs[t], St20), THc);
                     }
                     red[t * kMainThreads + tid] += Rc;
                     red[(W + 1 + t) * kMainThreads + tid] += THc;
@@ -418,8 +427,10 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
             const int i = I + tid;
             if (i < n) {
                 double birth = 0.0;
-                if (i <= n - 2) birth = fma(-fin[W + 1 + tid + 1], ws.inv_dx[i], fin[tid + 1]);
-                if (i >= 1) birth = fma(fin[W + 1 + tid], ws.inv_dx[i - 1], birth);
+                // TH is carried times 2^St: undo it on the (per-bin) inverse widths
+                if (i <= n - 2)
+                    birth = fma(-fin[W + 1 + tid + 1], scalbn(ws.inv_dx[i], -St), fin[tid + 1]);
+                if (i >= 1) birth = fma(fin[W + 1 + tid], scalbn(ws.inv_dx[i - 1], -St), birth);
                 const bool first = !(SCATTER && geo) || chunk == 0;
                 const double death = first ? N[i] * death_factor<K>(x[i], ws.a[i], ws.ia[i], M, b0, bbr, bsh)
                                            : 0.0;

@@ -12,9 +12,10 @@
 // GATHER (deterministic): one thread per fragment (q, j) computes its bracket
 // and its two shares; since v = x_j t_q grows with j, the fragments of one q
 // landing on bracket m form a contiguous run of j, whose first index is
-// recorded in first[q][m]. One thread per output bin i then adds, in fixed
-// order: -S_i N_i, then for every q the hi-shares of bracket i-1 and the
-// lo-shares of bracket i (bin 0 also takes the fragments clipped below x[0]).
+// recorded in first[q][m]. One warp per output bin i then adds, in a fixed
+// order, for every q the hi-shares of bracket i-1 and the lo-shares of
+// bracket i (bin 0 also takes the fragments clipped below x[0]) and finally
+// the death term -S_i N_i.
 // SCATTER: one thread per fragment adds its shares with FP64 atomicAdd.
 // =============================================================================
 #include "pbe_internal.cuh"
@@ -72,7 +73,6 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     const int lo = frag_bracket(x, n, v);
     double clo, chi;
     frag_shares(x, n, lo, v, contrib, clo, chi);
-    ws.lo[idx] = lo;
     ws.clo[idx] = clo;
     ws.chi[idx] = chi;
     // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
@@ -84,24 +84,31 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
 }
 
+// One warp per output bin: the lanes stride over the fragment runs (bin 0 can
+// collect every fragment clipped below x[0], thousands per quadrature point),
+// then a fixed butterfly sums the lanes -> deterministic.
 __global__ void __launch_bounds__(256)
 brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double acc = rhs[i] - ws.SN[i];
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;                      // whole warp
+    double acc = 0.0;
     for (int q = 0; q < nq; ++q) {
         const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-        const long long base = static_cast<long long>(q) * n;
+        const double* clo = ws.clo + static_cast<long long>(q) * n;
+        const double* chi = ws.chi + static_cast<long long>(q) * n;
         // clamp: entries are in [0, n] for monotone brackets (t_q > 0)
         const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
         const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
         const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
-        if (i == 0) { for (int j = 0; j < fb; ++j) acc += ws.clo[base + j]; }   // lo == -1
-        else        { for (int j = fa; j < fb; ++j) acc += ws.chi[base + j]; }  // lo == i-1
-        for (int j = fb; j < fc; ++j) acc += ws.clo[base + j];                  // lo == i
+        if (i == 0) { for (int j = lane; j < fb; j += 32) acc += clo[j]; }       // lo == -1
+        else        { for (int j = fa + lane; j < fb; j += 32) acc += chi[j]; }  // lo == i-1
+        for (int j = fb + lane; j < fc; j += 32) acc += clo[j];                  // lo == i
     }
-    rhs[i] = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) rhs[i] = (rhs[i] - ws.SN[i]) + acc;
 }
 
 template <int F>
@@ -141,7 +148,7 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
         brk_ws_layout(a.n, a.n_quad, static_cast<char*>(ws_base), &ws);
         brk_prep_kernel<F><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n, a.n_quad, ws, a.S0,
                                                 a.v_ref, a.alpha, a.v_min);
-        brk_gather_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a.rhs, a.n, a.n_quad, ws);
+        brk_gather_kernel<<<(a.n + 7) / 8, 256, 0, s>>>(a.rhs, a.n, a.n_quad, ws);
     }
     return cudaGetLastError();
 }

@@ -38,6 +38,17 @@ constexpr double kBreakageNMin = 2.2e-308;
 
 __device__ __forceinline__ long long dbits(double v) { return __double_as_longlong(v); }
 
+// v * 2^s for a normal (or zero) double, by adding s to the exponent field:
+// three integer instructions instead of an FP64 multiply. s20 = s << 20.
+// Zero stays zero; callers keep |v| 2^s inside the normal range.
+__device__ __forceinline__ double scale_pow2(double v, int s20)
+{
+    int hi = __double2hiint(v);
+    const int lo = __double2loint(v);
+    hi = (hi & 0x7ff00000) ? hi + s20 : hi;
+    return __hiloint2double(hi, lo);
+}
+
 // Left bracket lo in [0, n-2] with x[lo] <= v < x[lo+1], for x[0] < v < x[n-1]
 // (same result as the reference's binary searches, src/breakage_kernels.cuh:95-105
 // and src/aggregation_kernels.cuh:125-132), comparing bit patterns.
@@ -53,11 +64,18 @@ __device__ __forceinline__ int bracket_lo(const double* __restrict__ x, int n, d
 }
 
 // ---- aggregation scratch ----------------------------------------------------
+// Pivot volumes enter the weights only through differences v - x_lo. They are
+// carried in units scaled by 2^s, s = -ilogb(x[n-1]) (exact: a power of two
+// commutes with rounding), and each task shifts its numerators v - x_lo once
+// more by the exponent of its own tile (scale_pow2), so sum rate*(v - x_lo)
+// neither overflows nor underflows earlier than the reference's (1-w)*rate and
+// w*rate would, whatever range the grid spans.
 struct AggWs {
     double* h;         // [n]  x_i N_i
     double* a;         // [n]  x_i^(1/3)
     double* ia;        // [n]  1 / x_i^(1/3)
-    double* inv_dx;    // [n]  1 / (x_{i+1} - x_i)   (entry n-1 unused)
+    double* xs;        // [n]  x_i 2^s
+    double* inv_dx;    // [n]  1 / (xs_{i+1} - xs_i)   (entry n-1 unused)
     double* Bd;        // [n]  per-lag factor (see agg_prep_kernel)
     double* Sd;        // [n]  per-lag factor multiplying x_j
     int*    Ld;        // [n]  bracket offset of lag d: lo(j, j+d) = j + Ld[d]
@@ -82,6 +100,7 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.h         = reinterpret_cast<double*>(take(dn));
     w.a         = reinterpret_cast<double*>(take(dn));
     w.ia        = reinterpret_cast<double*>(take(dn));
+    w.xs        = reinterpret_cast<double*>(take(dn));
     w.inv_dx    = reinterpret_cast<double*>(take(dn));
     w.Bd        = reinterpret_cast<double*>(take(dn));
     w.Sd        = reinterpret_cast<double*>(take(dn));
@@ -95,9 +114,10 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
 }
 
 // ---- breakage scratch (gather mode) ------------------------------------------
+// Fragment (q, j) has the bracket lo = -1 (clipped to bin 0), n-1 (clipped to
+// bin n-1) or x[lo] <= x_j t_q < x[lo+1].
 struct BrkWs {
-    int*    lo;    // [nq * n]  left bracket of fragment (q, j); -1 = clipped to bin 0
-    double* clo;   // [nq * n]  share deposited at lo (whole contribution when clipped)
+    double* clo;   // [nq * n]  share of fragment (q, j) deposited at lo (all of it when clipped)
     double* chi;   // [nq * n]  share deposited at lo + 1
     int*    first; // [nq * (n + 2)]  first[q][m+1] = first j with lo(q, j) >= m, m in [-1, n]
     double* SN;    // [n]  S(x_j) N_j (0 where the guard skips bin j)
@@ -109,7 +129,6 @@ inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
     auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align256(bytes); return p; };
     const size_t m = static_cast<size_t>(n) * static_cast<size_t>(nq);
     BrkWs w{};
-    w.lo    = reinterpret_cast<int*>(take(sizeof(int) * m));
     w.clo   = reinterpret_cast<double*>(take(sizeof(double) * m));
     w.chi   = reinterpret_cast<double*>(take(sizeof(double) * m));
     w.first = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(nq) * (static_cast<size_t>(n) + 2)));

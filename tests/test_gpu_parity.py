@@ -12,7 +12,7 @@ from gpu_util import (AGG_KERNELS, agg_params, assert_close, gpu_agg, gpu_brk, m
 pytestmark = pytest.mark.gpu
 
 MODES = [pg.MODE_GATHER, pg.MODE_SCATTER]
-GRIDS = ["geo_fine", "geo_ref", "geo_coarse", "generic", "linear"]
+GRIDS = ["geo_fine", "geo_ref", "geo_coarse", "generic", "generic_wide", "linear"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=["gather", "scatter"])

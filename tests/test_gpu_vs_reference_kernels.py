@@ -2,7 +2,10 @@
 sources into oracle/_ref/ and launched with its launch geometry by
 oracle/ref_runner.cpp), on the same device and inputs, up to the full
 single-instance workload n = 16384 (Brownian+shear, threshold breakage).
-Per-bin bound: |lib - ref| <= 1e-12 * scale (scale from the CPU oracle)."""
+Per-bin bound: |lib - ref| <= 1e-12 * scale + misplaced (+1e-280), with scale
+and misplaced from the CPU oracle run the reference's way: `misplaced` is what
+the reference's logarithm bracket moves near ties relative to the exact
+bracket the library uses (zero on generic grids and away from ties)."""
 import os
 
 import numpy as np
@@ -10,7 +13,8 @@ import pytest
 
 import pbe_gb300 as pg
 import pyoracle
-from gpu_util import AGG_KERNELS, agg_params, assert_close, make_N, make_grid, oracle_agg, t
+from gpu_util import (AGG_KERNELS, agg_params, assert_close, make_N, make_grid,
+                      oracle_agg_reference, t)
 
 pytestmark = pytest.mark.gpu
 
@@ -50,10 +54,10 @@ def test_aggregation_vs_reference_kernels(ref, kernel, b0, bbr, bsh, grid):
         N = make_N("random", x, rng)
         p = agg_params(n, kernel, b0, bbr, bsh, x, geometric=grid.startswith("geo"))
         r = _run_ref_agg(ref, N, x, p)
-        _, scale, _ = oracle_agg(N, x, p)
+        _, scale, mis = oracle_agg_reference(N, x, p)
         for mode in (pg.MODE_GATHER, pg.MODE_SCATTER):
             assert_close(_run_lib_agg(N, x, p, mode), r, scale,
-                         "k=%d %s n=%d mode=%d" % (kernel, grid, n, mode))
+                         "k=%d %s n=%d mode=%d" % (kernel, grid, n, mode), extra=mis)
 
 
 def test_full_size_workload_vs_reference_kernels(ref):
@@ -74,13 +78,12 @@ def test_full_size_workload_vs_reference_kernels(ref):
     torch.cuda.synchronize()
     r = r.cpu().numpy()
     # oracle scale (all host threads)
-    _, sa, _ = pyoracle.aggregation_rhs(N, x, 5, 0.0, c["beta_br"], c["beta_sh"], p.log_x0,
-                                        p.inv_log_r)
+    _, sa, mis = oracle_agg_reference(N, x, p)
     _, sb, _ = pyoracle.breakage_rhs(N, x, t_q, bw_q, 3, c["S0"], 1.0, 1.0, c["v_min"])
     for mode in (pg.MODE_GATHER, pg.MODE_SCATTER):
         out = torch.zeros(n, dtype=torch.float64, device="cuda")
         assert pg.aggregation_rhs(tN, tx, out, p, mode=mode) == 0
         assert pg.breakage_rhs(tN, tx, tt, tb, out, bp, mode=mode) == 0
         torch.cuda.synchronize()
-        worst = assert_close(out.cpu().numpy(), r, sa + sb, "n=16384 mode=%d" % mode)
+        worst = assert_close(out.cpu().numpy(), r, sa + sb, "n=16384 mode=%d" % mode, extra=mis)
         print("n=16384 mode %d: worst |lib-ref|/scale = %.3e" % (mode, worst))
