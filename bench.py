@@ -47,6 +47,14 @@ PAIRS = N_BINS * (N_BINS + 1) // 2
 FRAGMENTS = N_BINS * N_QUAD
 FLOPS_PER_PAIR = 22      # algorithmic FP64 flops per pair interaction
 FLOPS_PER_FRAGMENT = 8   # per breakage fragment
+# FP64 instructions the pair kernel executes per pair on this workload: 7 per
+# pair evaluation (3 DADD, 2 DFMA, 2 DMUL), 17/16 evaluations per pair (the
+# boundary slot of each 16-bin tile is evaluated twice). Confirmed by the
+# sass instruction counters in profiles/agg_main_kernel_n16384.md.
+FP64_INSTR_PER_PAIR = 7.0 * 17.0 / 16.0
+# dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
+# this workload, from the ncu capture in profiles/agg_main_kernel_n16384.md.
+MAIN_KERNEL_DRAM_BYTES = 1424896
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -311,6 +319,7 @@ def main():
         peak = fp64_peak_tflops(stream)
         mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
         achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
+        instr_rate = FP64_INSTR_PER_PAIR * PAIRS / mk if mk else None
         out["roofline"] = {
             "bound": "fp64",
             "kernel": "agg_main_kernel<5>",
@@ -318,11 +327,15 @@ def main():
             "peak": round(peak, 4) if peak else None,
             "unit": "TFLOP/s",
             "frac": round(achieved / peak, 4) if (achieved and peak) else None,
-            "traffic": None,
+            "traffic": MAIN_KERNEL_DRAM_BYTES,
             "kernel_ms": round(mk * 1e3, 5) if mk else None,
             "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
-            "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so); no FP64 entry in "
-                           "MEASURED_PEAKS.json",
+            "algorithmic_unit": "22 FP64 flops per pair interaction (reference formula, cube roots "
+                                "per bin); frac > 1 because the kernel executes ~7 FP64 "
+                                "instructions per pair",
+            "fp64_pipe_frac": round(instr_rate / (peak * 1e12 / 2.0), 4) if (instr_rate and peak) else None,
+            "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
+                           "FP64 entry in MEASURED_PEAKS.json",
         }
     if n_gpus == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(x, N, t_q, bw_q, ap, bp)
