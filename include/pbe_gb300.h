@@ -121,6 +121,24 @@ int pbe_breakage_rhs_ex(const double* N, const double* x, const double* t_q,
                         const pbe_brk_params_t* params, int mode,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Aggregation without any allocation (no counterpart in the reference, whose
+ * kernels need no scratch). For host codes that cannot let a library allocate
+ * device memory -- solvers that give the whole GPU to their own allocator,
+ * codes that forbid allocation once time stepping starts, plug-in interfaces
+ * with no way to pass a workspace -- this runs the same kernels as
+ * pbe_aggregation_rhs_ex with its scratch in a fixed device array compiled
+ * into the library (about 1.9 MiB, held by every GPU that loads the library).
+ *   Limit: params->n <= 32768; larger n returns cudaErrorInvalidValue.
+ *   The first call on a device looks up that array's address; make it before
+ *   any stream capture starts.
+ *   All calls on a device share the array: calls whose kernels overlap on the
+ *   GPU race; order them on one stream. Nothing needs clearing between calls.
+ * mode: PBE_MODE_*. Same argument checks and return codes as
+ * pbe_aggregation_rhs. */
+int pbe_aggregation_rhs_noalloc(const double* N, const double* x, double* rhs,
+                                const pbe_agg_params_t* params, int mode, void* stream);
+
 /* Human-readable name of a return code (cudaGetErrorString). */
 const char* pbe_error_string(int code);
 

@@ -158,6 +158,9 @@ cudaError_t brk_call(const double* N, const double* x, const double* t_q, const 
 }
 
 } // namespace
+
+bool mode_is_scatter(int mode) { return resolve_mode(mode) == PBE_MODE_SCATTER; }
+
 } // namespace pbe_gb300
 
 using namespace pbe_gb300;

@@ -85,10 +85,22 @@ struct AggWs {
     int*    counter;   // [8]  task counter(s)
 };
 
-inline int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
-inline int agg_clip_blocks(int n) { return (n + kClipWarps - 1) / kClipWarps; }
+constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
+constexpr int agg_clip_blocks(int n) { return (n + kClipWarps - 1) / kClipWarps; }
 
-inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Size of the aggregation scratch for n bins, equal to agg_ws_layout(n) below
+// (kept in step with it; usable in constant expressions).
+constexpr size_t agg_ws_bytes(int n)
+{
+    const size_t dn = align256(sizeof(double) * static_cast<size_t>(n));
+    return 7 * dn + align256(sizeof(int) * static_cast<size_t>(n))
+         + align256(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n)))
+         + align256(sizeof(double) * 8)
+         + align256(sizeof(double) * static_cast<size_t>(agg_clip_blocks(n)))
+         + align256(sizeof(int) * 8);
+}
 
 // Carves the aggregation scratch out of `base` (may be null to query the size).
 inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
@@ -153,6 +165,9 @@ struct BrkArgs {
     const double* N; const double* x; const double* t_q; const double* bw_q; double* rhs;
     int n; int n_quad; int selection; double S0, v_ref, alpha, v_min;
 };
+
+// true when `mode` (PBE_MODE_*) resolves to the scatter variant. Defined in api.cu.
+bool mode_is_scatter(int mode);
 
 // Launch the aggregation kernels with a scratch buffer `ws_base` of at least
 // agg_ws_layout(n) bytes. scatter selects the atomic-flush variant.
