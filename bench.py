@@ -47,14 +47,36 @@ PAIRS = N_BINS * (N_BINS + 1) // 2
 FRAGMENTS = N_BINS * N_QUAD
 FLOPS_PER_PAIR = 22      # algorithmic FP64 flops per pair interaction
 FLOPS_PER_FRAGMENT = 8   # per breakage fragment
-# FP64 instructions the pair kernel executes per pair on this workload: 7 per
-# pair evaluation (3 DADD, 2 DFMA, 2 DMUL), 17/16 evaluations per pair (the
-# boundary slot of each 16-bin tile is evaluated twice). Confirmed by the
-# sass instruction counters in profiles/agg_main_kernel_n16384.md.
-FP64_INSTR_PER_PAIR = 7.0 * 17.0 / 16.0
+# FP64 instructions of the Brownian+shear pair kernel per pair evaluation:
+# lags with lo > k: rate (DMUL, DFMA, DMUL) + R += rate (DADD) + TH (DFMA) = 5;
+# lags with lo = k: q (DMUL, DFMA) + R (DADD) + TH (DFMA) = 4. The weight
+# numerator runs on the integer pipe. fp64_instr_per_launch() counts the
+# evaluations of both kinds the kernel performs on a given grid (each 12-bin
+# tile also evaluates its left neighbour slot); profiles/ cross-checks the
+# count with the SASS instruction counters.
+FP64_PHASE1, FP64_PHASE2, TILE_W = 5, 4, 12
+
+
+def fp64_instr_per_launch(x) -> int:
+    n = len(x)
+    v = x[0] + x
+    L = np.searchsorted(x, v, side="right") - 1          # bracket of x_0 + x_d
+    L = np.where(v >= x[-1], 1 << 30, L)
+    e0 = np.flatnonzero(L == np.arange(n))
+    D0 = int(e0[0]) if len(e0) else n
+    total = 0
+    d_idx = np.arange(n)
+    for I in range(0, n, TILE_W):
+        smax = min(I + TILE_W - 1, n - 2)
+        thi = smax - I + 1
+        ok = L <= smax
+        tlo = np.maximum(0, L - I + 1)
+        cnt = np.where(ok, np.maximum(0, thi - tlo + 1), 0)
+        total += FP64_PHASE1 * int(cnt[d_idx < D0].sum()) + FP64_PHASE2 * int(cnt[d_idx >= D0].sum())
+    return total
 # dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
 # this workload, from the ncu capture in profiles/agg_main_kernel_n16384.md.
-MAIN_KERNEL_DRAM_BYTES = 1424896
+MAIN_KERNEL_DRAM_BYTES = 1343488
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -267,6 +289,31 @@ def main():
             e2e_evs[k][1].record(stream)
         torch.cuda.synchronize()
         e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs)
+
+        # ---- adjoint: aggregation + breakage VJP of the same step ----------
+        vjp_ms = None
+        if args.impl == "ours":
+            lam = torch.randn(N_BINS, dtype=torch.float64, device=dev,
+                              generator=torch.Generator(device=dev).manual_seed(7))
+            gN = torch.zeros(N_BINS, **f64)
+            ga = torch.zeros(3, **f64)
+            gb = torch.zeros(4, **f64)
+
+            def vjp_step():
+                gN.zero_()
+                pg.check(pg.aggregation_rhs_vjp(dN, dx, lam, gN, ga, ap, stream=stream), "agg vjp")
+                pg.check(pg.breakage_rhs_vjp(dN, dx, dt, db, lam, gN, gb, bp, stream=stream), "brk vjp")
+            for _ in range(3):
+                vjp_step()
+            v_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                     for _ in range(max(args.steps // 4, 5))]
+            for a_, b_ in v_evs:
+                flush.zero_()
+                a_.record(stream)
+                vjp_step()
+                b_.record(stream)
+            torch.cuda.synchronize()
+            vjp_ms = sum(a_.elapsed_time(b_) for a_, b_ in v_evs) / len(v_evs)
         time.sleep(0.2)
         clk = clocks.stop()
 
@@ -309,6 +356,11 @@ def main():
         "gpu_launches": launches_per_step * args.steps if args.impl == "ours" else 0,
         "clocks": clk,
     }
+    if vjp_ms is not None:
+        out["vjp"] = {"ms_per_eval": round(vjp_ms, 5),
+                      "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
+                      "what": "aggregation + breakage VJP (dL/dN and parameter gradients) of "
+                              "the same n=16384 step, device-resident, L2 flushed"}
     if args.impl == "reference":
         out["impl"] = "reference"
         out["reference_build"] = ("acuoci/pbe-fixed-pivot-cuda src/aggregation.cu + src/breakage.cu, "
@@ -319,7 +371,8 @@ def main():
         peak = fp64_peak_tflops(stream)
         mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
         achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
-        instr_rate = FP64_INSTR_PER_PAIR * PAIRS / mk if mk else None
+        instr = fp64_instr_per_launch(x)
+        instr_rate = instr / mk if mk else None
         out["roofline"] = {
             "bound": "fp64",
             "kernel": "agg_main_kernel<5>",
@@ -331,8 +384,9 @@ def main():
             "kernel_ms": round(mk * 1e3, 5) if mk else None,
             "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
             "algorithmic_unit": "22 FP64 flops per pair interaction (reference formula, cube roots "
-                                "per bin); frac > 1 because the kernel executes ~7 FP64 "
-                                "instructions per pair",
+                                "per bin); frac > 1 because the kernel executes %.2f FP64 "
+                                "instructions per pair" % (instr / PAIRS),
+            "fp64_instr_per_launch": instr,
             "fp64_pipe_frac": round(instr_rate / (peak * 1e12 / 2.0), 4) if (instr_rate and peak) else None,
             "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
                            "FP64 entry in MEASURED_PEAKS.json",

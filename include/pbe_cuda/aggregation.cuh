@@ -51,4 +51,15 @@ cudaError_t launch_aggregation_rhs(
     const AggregationParams& params,
     cudaStream_t             stream = 0);
 
+// Adjoint (no counterpart in the reference): with lambda = dL/drhs, adds
+// dL/dN into gN[n] and dL/d(beta0, beta_br, beta_sh) into gparams[3] (device).
+cudaError_t launch_aggregation_rhs_vjp(
+    const double*            N,
+    const double*            x,
+    const double*            lambda,
+    double*                  gN,
+    double*                  gparams,
+    const AggregationParams& params,
+    cudaStream_t             stream = 0);
+
 } // namespace pbe_cuda

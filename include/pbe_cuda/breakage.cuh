@@ -54,4 +54,17 @@ cudaError_t launch_breakage_rhs(
     const BreakageParams&  params,
     cudaStream_t           stream = 0);
 
+// Adjoint (no counterpart in the reference): with lambda = dL/drhs, adds
+// dL/dN into gN[n] and dL/d(S0, v_ref, alpha, v_min) into gparams[4] (device).
+cudaError_t launch_breakage_rhs_vjp(
+    const double*          N,
+    const double*          x,
+    const double*          t_q,
+    const double*          bw_q,
+    const double*          lambda,
+    double*                gN,
+    double*                gparams,
+    const BreakageParams&  params,
+    cudaStream_t           stream = 0);
+
 } // namespace pbe_cuda

@@ -139,6 +139,27 @@ int pbe_breakage_rhs_ex(const double* N, const double* x, const double* t_q,
 int pbe_aggregation_rhs_noalloc(const double* N, const double* x, double* rhs,
                                 const pbe_agg_params_t* params, int mode, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Vector-Jacobian products (no counterpart in the reference). Given
+ * lambda = dL/drhs (device, length n) they ADD dL/dN into gN (length n) and
+ * dL/d(parameters) into gparams (device):
+ *   aggregation: gparams[0..2] += dL/dbeta0, dL/dbeta_br, dL/dbeta_sh
+ *   breakage:    gparams[0..3] += dL/dS0, dL/dv_ref, dL/dalpha, dL/dv_min (= 0)
+ * The result is bitwise reproducible. workspace: NULL (pool) or a device
+ * buffer of pbe_vjp_workspace_bytes(n), 256-byte aligned. Same argument
+ * checks as the forward calls (lambda and gparams must be non-null).
+ * ------------------------------------------------------------------------- */
+size_t pbe_vjp_workspace_bytes(int n);
+
+int pbe_aggregation_rhs_vjp(const double* N, const double* x, const double* lambda,
+                            double* gN, double* gparams, const pbe_agg_params_t* params,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+int pbe_breakage_rhs_vjp(const double* N, const double* x, const double* t_q,
+                         const double* bw_q, const double* lambda, double* gN,
+                         double* gparams, const pbe_brk_params_t* params,
+                         void* workspace, size_t workspace_bytes, void* stream);
+
 /* Human-readable name of a return code (cudaGetErrorString). */
 const char* pbe_error_string(int code);
 

@@ -299,6 +299,125 @@ int oracle_rk4_step(double* N, const double* x, int n, double dt,
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Vector-Jacobian products (no counterpart in the reference): given
+// lambda = dL/drhs, accumulate gN += dL/dN and gp += dL/d(parameters) for the
+// aggregation RHS above, pair by pair. For pair p = (j <= k) with
+// rate_p = c_p beta N_j N_k (c_p = 1/2 on the diagonal), L = sum_p rate_p G_p,
+// G_p = P_p - lambda_j - lambda_k, P_p = (1-w) lambda_lo + w lambda_hi
+// (lambda_{n-1} / lambda_0 for the clipped pairs), so
+//   dL/dN_j += G_p c_p beta (1 + [j==k]) N_k ... (N_j for k), dL/dbeta_X += G_p c_p f_X N_j N_k.
+// gp[0..2] = dL/dbeta0, dL/dbeta_br, dL/dbeta_sh.
+// sN / sp (nullable) receive the same sums with |P| + |lambda_j| + |lambda_k|
+// in place of G: the per-entry scale for relative tolerances.
+int oracle_aggregation_rhs_vjp(const double* N, const double* x, const double* lam,
+                               double* gN, double* gp, double* sN, double* sp, int n,
+                               double log_x0, double inv_log_r, int kernel, double beta0,
+                               double beta_br, double beta_sh, int exact_bracket)
+{
+    if (n <= 0 || !N || !x || !lam || !gN || !gp || kernel < 0 || kernel > 5) return 1;
+    for (int j = 0; j < n; ++j) {
+        for (int k = j; k < n; ++k) {
+            const double xj = x[j], xk = x[k];
+            double f0 = 0.0, fbr = 0.0, fsh = 0.0;
+            if (kernel == 0) f0 = 1.0;
+            if (kernel == 1) f0 = xj + xk;
+            if (kernel == 2) f0 = xj * xk;
+            if (kernel == 3 || kernel == 5) {
+                const double a = std::cbrt(xj), b = std::cbrt(xk);
+                fbr = a / b + b / a + 2.0;
+            }
+            if (kernel == 4 || kernel == 5) {
+                const double s = std::cbrt(xj) + std::cbrt(xk);
+                fsh = s * s * s;
+            }
+            const double beta = beta0 * f0 + beta_br * fbr + beta_sh * fsh;
+            const double c = (j == k) ? 0.5 : 1.0;
+            const double v = xj + xk;
+            double P, Pa;
+            if (v >= x[n - 1]) { P = lam[n - 1]; Pa = std::fabs(P); }
+            else if (v <= x[0]) { P = lam[0]; Pa = std::fabs(P); }
+            else {
+                const int hi = bin_index_ref(x, n, v, log_x0, exact_bracket ? 0.0 : inv_log_r);
+                const int lo = hi - 1;
+                const double w = (v - x[lo]) / (x[hi] - x[lo]);
+                P = (1.0 - w) * lam[lo] + w * lam[hi];
+                Pa = std::fabs((1.0 - w) * lam[lo]) + std::fabs(w * lam[hi]);
+            }
+            const double G = P - lam[j] - lam[k];
+            const double Ga = Pa + std::fabs(lam[j]) + std::fabs(lam[k]);
+            if (j == k) {
+                gN[j] += G * beta * N[j];
+                if (sN) sN[j] += Ga * std::fabs(beta * N[j]);
+            } else {
+                gN[j] += G * beta * N[k];
+                gN[k] += G * beta * N[j];
+                if (sN) { sN[j] += Ga * std::fabs(beta * N[k]); sN[k] += Ga * std::fabs(beta * N[j]); }
+            }
+            const double GNN = G * c * N[j] * N[k];
+            gp[0] += GNN * f0;
+            gp[1] += GNN * fbr;
+            gp[2] += GNN * fsh;
+            if (sp) {
+                const double GaNN = Ga * std::fabs(c * N[j] * N[k]);
+                sp[0] += GaNN * std::fabs(f0);
+                sp[1] += GaNN * std::fabs(fbr);
+                sp[2] += GaNN * std::fabs(fsh);
+            }
+        }
+    }
+    return 0;
+}
+
+// Breakage VJP: rhs_i = -S_i N_i + sum_j S_j N_j sum_q bw_q eta_i(x_j t_q) over
+// the guarded parents (S != 0, N > 2.2e-308). With Q_j = -lambda_j +
+// sum_q bw_q P_jq: gN_j += S_j Q_j; gp[0] = dL/dS0, gp[1] = dL/dv_ref,
+// gp[2] = dL/dalpha, gp[3] = dL/dv_min (0: the threshold is a step).
+int oracle_breakage_rhs_vjp(const double* N, const double* x, const double* t_q,
+                            const double* bw_q, const double* lam, double* gN,
+                            double* gp, double* sN, double* sp, int n, int n_quad,
+                            int selection, double S0, double v_ref, double alpha,
+                            double v_min)
+{
+    if (n <= 0 || n_quad <= 0 || !N || !x || !t_q || !bw_q || !lam || !gN || !gp) return 1;
+    if (selection < 0 || selection > 3) return 1;
+    for (int j = 0; j < n; ++j) {
+        const double xj = x[j], Nj = N[j];
+        const double S = selection_ref(selection, xj, S0, v_ref, alpha, v_min);
+        if (!(S != 0.0 && Nj > 2.2e-308)) continue;
+        double Q = -lam[j], Qa = std::fabs(lam[j]);
+        for (int q = 0; q < n_quad; ++q) {
+            const double v = xj * t_q[q];
+            double P, Pa;
+            if (v <= x[0]) { P = lam[0]; Pa = std::fabs(P); }
+            else if (v >= x[n - 1]) { P = lam[n - 1]; Pa = std::fabs(P); }
+            else {
+                const int lo = bin_search_ref(x, n, v);
+                const double eta = (v - x[lo]) / (x[lo + 1] - x[lo]);
+                P = (1.0 - eta) * lam[lo] + eta * lam[lo + 1];
+                Pa = std::fabs((1.0 - eta) * lam[lo]) + std::fabs(eta * lam[lo + 1]);
+            }
+            Q += bw_q[q] * P;
+            Qa += std::fabs(bw_q[q]) * Pa;
+        }
+        gN[j] += S * Q;
+        if (sN) sN[j] += std::fabs(S) * Qa;
+        const double NQ = Nj * Q, NQa = std::fabs(Nj) * Qa;
+        gp[0] += (S / S0) * NQ;
+        if (sp) sp[0] += std::fabs(S / S0) * NQa;
+        if (selection == 1) { gp[1] += -(S / v_ref) * NQ; if (sp) sp[1] += std::fabs(S / v_ref) * NQa; }
+        if (selection == 2) {
+            gp[1] += -(alpha * S / v_ref) * NQ;
+            gp[2] += S * std::log(xj / v_ref) * NQ;
+            if (sp) {
+                sp[1] += std::fabs(alpha * S / v_ref) * NQa;
+                sp[2] += std::fabs(S * std::log(xj / v_ref)) * NQa;
+            }
+        }
+    }
+    return 0;
+}
+
 int oracle_version(void) { return 1; }
 
 } // extern "C"

@@ -43,6 +43,14 @@ def _lib():
         lib.oracle_breakage_rhs.argtypes = [_D, _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_double]
+        lib.oracle_aggregation_rhs_vjp.restype = ctypes.c_int
+        lib.oracle_aggregation_rhs_vjp.argtypes = [_D, _D, _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        lib.oracle_breakage_rhs_vjp.restype = ctypes.c_int
+        lib.oracle_breakage_rhs_vjp.argtypes = [_D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double, ctypes.c_double]
         lib.oracle_rk4_step.restype = ctypes.c_int
         lib.oracle_rk4_step.argtypes = [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -111,6 +119,39 @@ def breakage_rhs(N, x, t_q, bw_q, selection, S0=1.0, v_ref=1.0, alpha=1.0, v_min
                                       int(n), int(nq), int(selection), float(S0), float(v_ref),
                                       float(alpha), float(v_min))
     return out, scale, code
+
+
+def aggregation_rhs_vjp(N, x, lam, kernel, beta0=1.0, beta_br=0.0, beta_sh=0.0, log_x0=0.0,
+                        inv_log_r=0.0, exact_bracket=True, with_scale=False):
+    """(dL/dN, [dL/dbeta0, dL/dbeta_br, dL/dbeta_sh], code) for L = lam . rhs_agg(N);
+    with_scale adds the per-entry absolute scales: (gN, gp, sN, sp, code)."""
+    N, x, lam = _f64(N), _f64(x), _f64(lam)
+    gN, sN = np.zeros(len(x)), np.zeros(len(x))
+    gp, sp = np.zeros(3), np.zeros(3)
+    code = _lib().oracle_aggregation_rhs_vjp(_dp(N), _dp(x), _dp(lam), _dp(gN), _dp(gp), _dp(sN),
+                                             _dp(sp), len(x), float(log_x0), float(inv_log_r),
+                                             int(kernel), float(beta0), float(beta_br),
+                                             float(beta_sh), 1 if exact_bracket else 0)
+    if with_scale:
+        return gN, gp, sN, sp, code
+    return gN, gp, code
+
+
+def breakage_rhs_vjp(N, x, t_q, bw_q, lam, selection, S0=1.0, v_ref=1.0, alpha=1.0, v_min=0.0,
+                     with_scale=False):
+    """(dL/dN, [dL/dS0, dL/dv_ref, dL/dalpha, dL/dv_min], code) for L = lam . rhs_brk(N);
+    with_scale adds the per-entry absolute scales: (gN, gp, sN, sp, code)."""
+    N, x, lam = _f64(N), _f64(x), _f64(lam)
+    t_q, bw_q = _f64(t_q), _f64(bw_q)
+    gN, sN = np.zeros(len(x)), np.zeros(len(x))
+    gp, sp = np.zeros(4), np.zeros(4)
+    code = _lib().oracle_breakage_rhs_vjp(_dp(N), _dp(x), _dp(t_q), _dp(bw_q), _dp(lam), _dp(gN),
+                                          _dp(gp), _dp(sN), _dp(sp), len(x), len(t_q),
+                                          int(selection), float(S0), float(v_ref), float(alpha),
+                                          float(v_min))
+    if with_scale:
+        return gN, gp, sN, sp, code
+    return gN, gp, code
 
 
 def rk4_step(N, x, dt, agg=None, brk=None):

@@ -19,9 +19,11 @@
 //  * Geometric grids (verified on the device, see agg_prep_kernel): the
 //    bracket offset lo - j, the Brownian factor and the shear factor depend on
 //    the lag d = k - j only. They come from per-lag tables, so a pair costs
-//    2-5 FP64 operations plus the weight. The weight numerator is
-//    fl(x_j + x_k) - x_lo from the actual pivots, exactly as the reference
-//    forms it (in 2^s-scaled units, see AggWs).
+//    1-3 FP64 operations plus two accumulations. The weight numerator
+//    fl(x_j + x_k) - x_lo is formed from the actual pivots exactly as the
+//    reference forms it, but on the integer pipe (exact_weight.cuh). For lags
+//    whose pairs land on the larger member's own slot (lo = k, about half of
+//    the pairs at n = 16384) N_k is a per-slot constant and is factored out.
 //  * Generic grids: per-pair brackets by a monotone walk over k, beta from
 //    per-bin cube roots.
 //  * Pairs clipped at x[n-1] are summed by a separate kernel (per lag on a
@@ -35,6 +37,7 @@
 // chunk) and flush with FP64 atomicAdd.
 // =============================================================================
 #include "pbe_internal.cuh"
+#include "exact_weight.cuh"
 
 namespace pbe_gb300 {
 namespace {
@@ -57,6 +60,18 @@ __device__ __forceinline__ double rate_geo(double B, double S, double Nj, double
     else if constexpr (K == 2) return (B * hj) * hk;
     else if constexpr (K == 4) return (S * hj) * Nk;
     else return Nk * fma(S, hj, B * Nj);
+}
+
+// Lags whose pairs land on the larger member's own slot (lo = k): the rate is
+// F_k * q_slot(j) with the per-slot factor F_k = N_k (h_k for Product). Not
+// used for Sum, whose rate has two k-dependent terms.
+template <int K>
+__device__ __forceinline__ double q_slot(double B, double S, double Nj, double hj)
+{
+    if constexpr (K == 0 || K == 3) return B * Nj;
+    else if constexpr (K == 2) return B * hj;
+    else if constexpr (K == 4) return S * hj;
+    else return fma(S, hj, B * Nj);
 }
 
 // Pair rate on any grid from per-bin values (a = x^(1/3), ia = 1/a, h = x N):
@@ -101,32 +116,6 @@ __device__ __forceinline__ double death_factor(double xi, double ai, double iai,
     }
 }
 
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ double warp_max(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-// Fixed-order block sum (result valid in every thread). sh: >= blockDim/32 doubles.
-__device__ __forceinline__ double block_sum(double v, double* sh)
-{
-    const int nw = blockDim.x >> 5;
-    v = warp_sum(v);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double r = 0.0;
-    for (int w = 0; w < nw; ++w) r += sh[w];
-    return r;
-}
-
 // ---------------------------------------------------------------------------
 // prep: one thread per bin i. Per-bin values, the lag tables for d = i,
 // moment partials and the geometric-grid deviation.
@@ -143,21 +132,22 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
                 double b0, double bbr, double bsh)
 {
     __shared__ double sh[kPrepThreads / 32];
+    __shared__ int d0_s;
     const int i = blockIdx.x * kPrepThreads + threadIdx.x;
     double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     double dev = 0.0;
+    int d0 = n;      // this thread's lag if its pairs land on their larger member (Ld == d)
+    if (threadIdx.x == 0) d0_s = n;
+    __syncthreads();
     if (i < n) {
         const double xi = x[i], Ni = N[i];
         const double hi = xi * Ni;
         const double ai = cbrt(xi);
         const double iai = 1.0 / ai;
-        const int s = -ilogb(x[n - 1]);
-        const double xsi = scalbn(xi, s);
         ws.h[i] = hi;
         ws.a[i] = ai;
         ws.ia[i] = iai;
-        ws.xs[i] = xsi;
-        ws.inv_dx[i] = (i < n - 1) ? 1.0 / (scalbn(x[i + 1], s) - xsi) : 0.0;
+        ws.inv_dx[i] = (i < n - 1) ? 1.0 / (x[i + 1] - xi) : 0.0;
         m[0] = iai * Ni; m[1] = Ni; m[2] = ai * Ni; m[3] = (ai * ai) * Ni; m[4] = hi;
 
         const double x0 = x[0];
@@ -172,13 +162,16 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         ws.Bd[i] = B;
         ws.Sd[i] = S;
         const double v = x0 + xi;
-        ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        ws.Ld[i] = L;
+        if (L == i) d0 = i;
         if (n >= 2) {
             const double lr = log(x[n - 1] / x0) / static_cast<double>(n - 1);
             dev = fabs(log(xi / x0) - static_cast<double>(i) * lr);
             if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
         }
     }
+    atomicMin(&d0_s, d0);
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         const double s = block_sum(m[q], sh);
@@ -192,14 +185,23 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         double mx = 0.0;
         for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
         ws.mom_part[blockIdx.x * 8 + 5] = mx;
+        ws.mom_part[blockIdx.x * 8 + 6] = static_cast<double>(d0_s);
     }
 }
 
-// fin: one block. Moments (fixed-order sums), geometric flag, counter reset.
-__global__ void __launch_bounds__(256) agg_fin_kernel(int n, AggWs ws)
+// fin: one block. Moments (fixed-order sums), geometric flag, the first lag
+// whose pairs land on their larger member's own slot (Ld[d] == d), counter reset.
+__global__ void __launch_bounds__(256) agg_fin_kernel(const double* __restrict__ x, int n, AggWs ws)
 {
     __shared__ double sh[8];
+    __shared__ int d0_s;
     const int nb = (n + kPrepThreads - 1) / kPrepThreads;
+    if (threadIdx.x == 0) d0_s = n;
+    __syncthreads();
+    int d0 = n;      // smallest lag with Ld[d] == d over the prep blocks
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+        d0 = min(d0, static_cast<int>(ws.mom_part[b * 8 + 6]));
+    atomicMin(&d0_s, d0);
     for (int q = 0; q < 5; ++q) {
         double s = 0.0;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ws.mom_part[b * 8 + q];
@@ -214,9 +216,13 @@ __global__ void __launch_bounds__(256) agg_fin_kernel(int n, AggWs ws)
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 0; w < 8; ++w) mx = fmax(mx, sh[w]);
-        ws.mom[5] = (n >= 2 && mx <= kGeoTol) ? 1.0 : 0.0;
+        // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades
+        // of its bracket pivot (precondition of sum_minus_scaled)
+        const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
+        ws.mom[5] = (n >= 2 && mx <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
         ws.mom[6] = mx;
         ws.counter[0] = 0;
+        ws.counter[1] = d0_s;     // lags d >= counter[1] have lo(j, j+d) = j + d
     }
 }
 
@@ -248,12 +254,12 @@ agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, doub
             }
         } else {
             const int j = w;
-            const double xj = ws.xs[j];
-            const long long tb = dbits(ws.xs[n - 1]);
+            const double xj = x[j];
+            const long long tb = dbits(x[n - 1]);
             int lo = j, hi = n - 1;   // xj + x[n-1] >= x[n-1] always holds
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (dbits(xj + ws.xs[mid]) >= tb) hi = mid; else lo = mid + 1;
+                if (dbits(xj + x[mid]) >= tb) hi = mid; else lo = mid + 1;
             }
             const double Nj = N[j], hj = ws.h[j], aj = ws.a[j], iaj = ws.ia[j];
             for (int k = lo + lane; k < n; k += 32)
@@ -280,6 +286,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 {
     extern __shared__ double red[];               // [kRedRows][kMainThreads]
     __shared__ double xs[W + 2];                  // x[I-1 .. I+W]
+    __shared__ double fs[W + 2];                  // per-slot factor N (h for Product)
     __shared__ double part4[4][kRedRows];
     __shared__ double fin[kRedRows];
     __shared__ double shw[kMainThreads / 32];
@@ -309,12 +316,14 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 
         if (tid < W + 2) {
             const int s = I - 1 + tid;
-            xs[tid] = (s >= 0 && s < n) ? ws.xs[s] : 0.0;
+            const bool in = (s >= 0 && s < n);
+            xs[tid] = in ? x[s] : 0.0;
+            fs[tid] = in ? (K == 2 ? ws.h[s] : N[s]) : 0.0;
         }
         // Per-task exponent shift of the weight numerators: th ~ x_I (r-1) is
         // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
         // the reference's w*rate even on grids spanning hundreds of octaves.
-        const int St = -ilogb(ws.xs[I]);
+        const int St = -ilogb(x[I]);
         const int St20 = St << 20;
         __syncthreads();
 
@@ -323,9 +332,13 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 #pragma unroll
             for (int t = 0; t <= W; ++t) { R[t] = 0.0; TH[t] = 0.0; }
             const int thi = smax - (I - 1);   // slot index t <= thi
-            for (int d = d_begin + tid; d < d_end; d += kMainThreads) {
+            // lags d >= D0 put every pair on its larger member's own slot (lo = k)
+            const int D0 = (K == 1) ? n : ws.counter[1];
+            int d = d_begin + tid;
+            // phase 1, lags with lo > k: rate per pair, R += rate, TH += rate * th
+            for (; d < d_end && d < D0; d += kMainThreads) {
                 const int L = __ldg(ws.Ld + d);
-                if (L > smax) break;           // Ld is nondecreasing in d
+                if (L > smax) { d = d_end; break; }   // Ld is nondecreasing in d
                 const double B = __ldg(ws.Bd + d), S = __ldg(ws.Sd + d);
                 const int jb = I - 1 - L;      // j of slot t is jb + t, k = jb + d + t
                 const int tlo = max(0, -jb);
@@ -337,9 +350,9 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                         const double hj = NeedH<K>::j ? __ldg(ws.h + j) : 0.0;
                         const double hk = NeedH<K>::k ? __ldg(ws.h + k) : 0.0;
                         const double rate = rate_geo<K>(B, S, Nj, hj, Nk, hk);
-                        // fl(x_j + x_k) - x_lo, the reference's weight numerator
-                        const double th =
-                            scale_pow2((__ldg(ws.xs + j) + __ldg(ws.xs + k)) - xs[t], St20);
+                        // (fl(x_j + x_k) - x_lo) 2^St on the integer pipe, bit-identical
+                        // to the reference's two FP64 additions
+                        const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + j), xs[t], St);
                         if (t > 0) R[t] += rate;
                         TH[t] = fma(rate, th, TH[t]);
                     }
@@ -349,6 +362,38 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
             for (int t = 0; t <= W; ++t) {
                 red[t * kMainThreads + tid] = R[t];
                 red[(W + 1 + t) * kMainThreads + tid] = TH[t];
+                R[t] = 0.0;
+                TH[t] = 0.0;
+            }
+            // phase 2, lags with lo = k: k is the slot itself, so rate = F_slot * q(j)
+            // (F = N, or h for Product); sum q and q * th, multiply by F once
+            if constexpr (K != 1) {
+                for (; d < d_end; d += kMainThreads) {
+                    const int L = __ldg(ws.Ld + d);
+                    if (L > smax) break;
+                    const double B = __ldg(ws.Bd + d), S = __ldg(ws.Sd + d);
+                    const int jb = I - 1 - L;
+                    const int tlo = max(0, -jb);
+#pragma unroll
+                    for (int t = 0; t <= W; ++t) {
+                        if (t >= tlo && t <= thi) {
+                            const int j = jb + t;
+                            const double Nj = __ldg(N + j);
+                            const double hj = NeedH<K>::j ? __ldg(ws.h + j) : 0.0;
+                            const double q = q_slot<K>(B, S, Nj, hj);
+                            const double th = sum_minus_scaled(xs[t], __ldg(x + j), xs[t], St);
+                            if (t > 0) R[t] += q;
+                            TH[t] = fma(q, th, TH[t]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t <= W; ++t) {
+                    double* r0 = red + t * kMainThreads + tid;
+                    double* r1 = red + (W + 1 + t) * kMainThreads + tid;
+                    *r0 = fma(fs[t], R[t], *r0);
+                    *r1 = fma(fs[t], TH[t], *r1);
+                }
             }
         } else {
 #pragma unroll
@@ -359,8 +404,8 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const int t_last = smax - (I - 1);
                 const long long blo = dbits(xs[t_first]);
                 const long long bhi = dbits(xs[t_last + 1]);
-                const double* __restrict__ xsc = ws.xs;      // scaled pivots (bracket
-                const double xlast = xsc[n - 1];            // decisions are unchanged)
+                const double* __restrict__ xsc = x;
+                const double xlast = xsc[n - 1];
                 for (int j = tid; j <= smax; j += kMainThreads) {
                     const double xj = xsc[j];
                     if (dbits(xj + xj) >= bhi) break;          // v >= 2 x_j grows with j
@@ -465,7 +510,7 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
-    agg_fin_kernel<<<1, 256, 0, s>>>(n, ws);
+    agg_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
     agg_clip_kernel<K, SC><<<nbc, kClipWarps * 32, 0, s>>>(a.N, a.x, a.rhs, n, ws, a.beta0,
                                                           a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;

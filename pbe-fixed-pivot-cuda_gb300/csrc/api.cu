@@ -157,6 +157,41 @@ cudaError_t brk_call(const double* N, const double* x, const double* t_q, const 
     });
 }
 
+cudaError_t agg_vjp_call(const double* N, const double* x, const double* lam, double* gN,
+                         double* gp, const pbe_agg_params_t* p, void* ws, size_t ws_bytes,
+                         cudaStream_t s)
+{
+    cudaError_t e = check_agg(N, x, gN, p);
+    if (e != cudaSuccess) return e;
+    if (!lam || !gp) return cudaErrorInvalidDevicePointer;
+    DeviceState* st = nullptr;
+    e = device_state(&st);
+    if (e != cudaSuccess) return e;
+    AggVjpArgs a{N, x, lam, gN, gp, p->n, p->kernel_type, p->beta0, p->beta_br, p->beta_sh};
+    const size_t need = vjp_ws_layout(p->n, nullptr, nullptr);
+    return with_scratch(need, ws, ws_bytes, s, st, [&](void* w) {
+        return agg_vjp_launch(a, w, st->num_sms, s);
+    });
+}
+
+cudaError_t brk_vjp_call(const double* N, const double* x, const double* t_q, const double* bw_q,
+                         const double* lam, double* gN, double* gp, const pbe_brk_params_t* p,
+                         void* ws, size_t ws_bytes, cudaStream_t s)
+{
+    cudaError_t e = check_brk(N, x, t_q, bw_q, gN, p);
+    if (e != cudaSuccess) return e;
+    if (!lam || !gp) return cudaErrorInvalidDevicePointer;
+    DeviceState* st = nullptr;
+    e = device_state(&st);
+    if (e != cudaSuccess) return e;
+    BrkVjpArgs a{N, x, t_q, bw_q, lam, gN, gp, p->n, p->n_quad, p->selection, p->S0, p->v_ref,
+                 p->alpha, p->v_min};
+    const size_t need = vjp_ws_layout(p->n, nullptr, nullptr);
+    return with_scratch(need, ws, ws_bytes, s, st, [&](void* w) {
+        return brk_vjp_launch(a, w, s);
+    });
+}
+
 } // namespace
 
 bool mode_is_scatter(int mode) { return resolve_mode(mode) == PBE_MODE_SCATTER; }
@@ -221,6 +256,29 @@ const char* pbe_error_string(int code)
 
 int pbe_version(void) { return 100; }
 
+size_t pbe_vjp_workspace_bytes(int n)
+{
+    if (n <= 0) return 0;
+    return vjp_ws_layout(n, nullptr, nullptr);
+}
+
+int pbe_aggregation_rhs_vjp(const double* N, const double* x, const double* lambda, double* gN,
+                            double* gparams, const pbe_agg_params_t* params, void* workspace,
+                            size_t workspace_bytes, void* stream)
+{
+    return static_cast<int>(agg_vjp_call(N, x, lambda, gN, gparams, params, workspace,
+                                         workspace_bytes, static_cast<cudaStream_t>(stream)));
+}
+
+int pbe_breakage_rhs_vjp(const double* N, const double* x, const double* t_q, const double* bw_q,
+                         const double* lambda, double* gN, double* gparams,
+                         const pbe_brk_params_t* params, void* workspace, size_t workspace_bytes,
+                         void* stream)
+{
+    return static_cast<int>(brk_vjp_call(N, x, t_q, bw_q, lambda, gN, gparams, params, workspace,
+                                         workspace_bytes, static_cast<cudaStream_t>(stream)));
+}
+
 int pbe_set_profile_events(void* start, void* stop)
 {
     g_prof_start = static_cast<cudaEvent_t>(start);
@@ -260,6 +318,29 @@ cudaError_t launch_breakage_rhs(const double* N, const double* x, const double* 
     c.S0 = p.S0; c.v_ref = p.v_ref; c.alpha = p.alpha; c.v_min = p.v_min;
     c.block_size = p.block_size;
     return brk_call(N, x, t_q, bw_q, rhs, &c, PBE_MODE_DEFAULT, nullptr, 0, stream);
+}
+
+cudaError_t launch_aggregation_rhs_vjp(const double* N, const double* x, const double* lambda,
+                                       double* gN, double* gparams, const AggregationParams& p,
+                                       cudaStream_t stream)
+{
+    pbe_agg_params_t c;
+    c.n = p.n; c.log_x0 = p.log_x0; c.inv_log_r = p.inv_log_r;
+    c.kernel_type = static_cast<int>(p.kernel_type);
+    c.beta0 = p.beta0; c.beta_br = p.beta_br; c.beta_sh = p.beta_sh;
+    c.block_size = p.block_size;
+    return agg_vjp_call(N, x, lambda, gN, gparams, &c, nullptr, 0, stream);
+}
+
+cudaError_t launch_breakage_rhs_vjp(const double* N, const double* x, const double* t_q,
+                                    const double* bw_q, const double* lambda, double* gN,
+                                    double* gparams, const BreakageParams& p, cudaStream_t stream)
+{
+    pbe_brk_params_t c;
+    c.n = p.n; c.n_quad = p.n_quad; c.selection = static_cast<int>(p.selection);
+    c.S0 = p.S0; c.v_ref = p.v_ref; c.alpha = p.alpha; c.v_min = p.v_min;
+    c.block_size = p.block_size;
+    return brk_vjp_call(N, x, t_q, bw_q, lambda, gN, gparams, &c, nullptr, 0, stream);
 }
 
 } // namespace pbe_cuda

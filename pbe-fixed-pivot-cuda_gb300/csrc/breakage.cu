@@ -23,25 +23,6 @@
 namespace pbe_gb300 {
 namespace {
 
-template <int F>
-__device__ __forceinline__ double selection(double v, double S0, double v_ref, double alpha,
-                                            double v_min)
-{
-    if constexpr (F == 0) return S0;
-    else if constexpr (F == 1) return S0 * v / v_ref;
-    else if constexpr (F == 2) return S0 * pow(v / v_ref, alpha);
-    else return (v > v_min) ? S0 : 0.0;
-}
-
-// Bracket of a fragment volume: -1 when clipped to bin 0 (v <= x[0]), n-1 when
-// clipped to bin n-1 (v >= x[n-1]), else lo with x[lo] <= v < x[lo+1].
-__device__ __forceinline__ int frag_bracket(const double* __restrict__ x, int n, double v)
-{
-    if (dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
-    if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
-    return bracket_lo(x, n, v);
-}
-
 // Shares of one fragment: (to lo, to lo+1). Clipped fragments put everything
 // into the first share.
 __device__ __forceinline__ void frag_shares(const double* __restrict__ x, int n, int lo, double v,

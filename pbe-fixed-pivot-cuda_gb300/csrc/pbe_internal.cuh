@@ -19,7 +19,7 @@
 namespace pbe_gb300 {
 
 // ---- launch geometry --------------------------------------------------------
-constexpr int kTileW        = 16;    // output bins owned by one task
+constexpr int kTileW        = 12;    // output bins owned by one task (125 regs, no spill)
 constexpr int kMainThreads  = 256;   // threads per aggregation task CTA
 constexpr int kPrepThreads  = 256;
 constexpr int kClipWarps    = 8;     // warps per block of the clip kernel
@@ -49,6 +49,32 @@ __device__ __forceinline__ double scale_pow2(double v, int s20)
     return __hiloint2double(hi, lo);
 }
 
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Fixed-order block sum (result valid in every thread). sh: >= blockDim/32 doubles.
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+    const int nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < nw; ++w) r += sh[w];
+    return r;
+}
+
 // Left bracket lo in [0, n-2] with x[lo] <= v < x[lo+1], for x[0] < v < x[n-1]
 // (same result as the reference's binary searches, src/breakage_kernels.cuh:95-105
 // and src/aggregation_kernels.cuh:125-132), comparing bit patterns.
@@ -63,26 +89,44 @@ __device__ __forceinline__ int bracket_lo(const double* __restrict__ x, int n, d
     return lo;
 }
 
+// Selection function S(v) (reference src/breakage_kernels.cuh:51-65).
+template <int F>
+__device__ __forceinline__ double selection(double v, double S0, double v_ref, double alpha,
+                                            double v_min)
+{
+    if constexpr (F == 0) return S0;
+    else if constexpr (F == 1) return S0 * v / v_ref;
+    else if constexpr (F == 2) return S0 * pow(v / v_ref, alpha);
+    else return (v > v_min) ? S0 : 0.0;
+}
+
+// Bracket of a fragment volume: -1 when clipped to bin 0 (v <= x[0]), n-1 when
+// clipped to bin n-1 (v >= x[n-1]), else lo with x[lo] <= v < x[lo+1].
+__device__ __forceinline__ int frag_bracket(const double* __restrict__ x, int n, double v)
+{
+    if (dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
+    if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
+    return bracket_lo(x, n, v);
+}
+
 // ---- aggregation scratch ----------------------------------------------------
-// Pivot volumes enter the weights only through differences v - x_lo. They are
-// carried in units scaled by 2^s, s = -ilogb(x[n-1]) (exact: a power of two
-// commutes with rounding), and each task shifts its numerators v - x_lo once
-// more by the exponent of its own tile (scale_pow2), so sum rate*(v - x_lo)
-// neither overflows nor underflows earlier than the reference's (1-w)*rate and
-// w*rate would, whatever range the grid spans.
+// Pivot volumes enter the weights only through differences v - x_lo. Each task
+// carries them shifted by the exponent of its own tile (times 2^St, exact), so
+// sum rate*(v - x_lo) neither overflows nor underflows earlier than the
+// reference's (1-w)*rate and w*rate would, whatever range the grid spans.
+// Pivots must be positive normal doubles.
 struct AggWs {
     double* h;         // [n]  x_i N_i
     double* a;         // [n]  x_i^(1/3)
     double* ia;        // [n]  1 / x_i^(1/3)
-    double* xs;        // [n]  x_i 2^s
-    double* inv_dx;    // [n]  1 / (xs_{i+1} - xs_i)   (entry n-1 unused)
+    double* inv_dx;    // [n]  1 / (x_{i+1} - x_i)   (entry n-1 unused)
     double* Bd;        // [n]  per-lag factor (see agg_prep_kernel)
     double* Sd;        // [n]  per-lag factor multiplying x_j
     int*    Ld;        // [n]  bracket offset of lag d: lo(j, j+d) = j + Ld[d]
     double* mom_part;  // [nb_prep * 8] per-block moment partials
     double* mom;       // [8]  M_{-1/3}, M_0, M_{1/3}, M_{2/3}, M_1, geo flag, max dev
     double* clip_part; // [nb_clip] per-block sums of clipped pair rates
-    int*    counter;   // [8]  task counter(s)
+    int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
@@ -95,7 +139,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t agg_ws_bytes(int n)
 {
     const size_t dn = align256(sizeof(double) * static_cast<size_t>(n));
-    return 7 * dn + align256(sizeof(int) * static_cast<size_t>(n))
+    return 6 * dn + align256(sizeof(int) * static_cast<size_t>(n))
          + align256(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n)))
          + align256(sizeof(double) * 8)
          + align256(sizeof(double) * static_cast<size_t>(agg_clip_blocks(n)))
@@ -112,7 +156,6 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.h         = reinterpret_cast<double*>(take(dn));
     w.a         = reinterpret_cast<double*>(take(dn));
     w.ia        = reinterpret_cast<double*>(take(dn));
-    w.xs        = reinterpret_cast<double*>(take(dn));
     w.inv_dx    = reinterpret_cast<double*>(take(dn));
     w.Bd        = reinterpret_cast<double*>(take(dn));
     w.Sd        = reinterpret_cast<double*>(take(dn));
@@ -148,6 +191,56 @@ inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
     if (ws) *ws = w;
     return off;
 }
+
+// ---- VJP scratch ---------------------------------------------------------------
+struct VjpWs {
+    double* h;         // [n]  x_i N_i
+    double* a;         // [n]  x_i^(1/3)
+    double* ia;        // [n]  1 / x_i^(1/3)
+    double* D;         // [n]  (lambda_{i+1} - lambda_i) / (x_{i+1} - x_i)
+    double* Bf;        // [n]  Brownian factor of lag d (rho + 1/rho + 2), no beta, no 1/2
+    double* Sf;        // [n]  shear factor of lag d (1 + rho)^3 (times x of the smaller member)
+    int*    Ld;        // [n]  bracket offset of lag d (as AggWs)
+    double* mom_part;  // [nb_prep * 16] moments of N and lambda*N, max deviation
+    double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
+    double* gpart;     // [max(ntile, nb_brk) * 4] per-task parameter partials
+    int*    counter;   // [8]
+};
+
+inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align256(bytes); return p; };
+    const size_t dn = sizeof(double) * static_cast<size_t>(n);
+    const int ntile = (n + kTileW - 1) / kTileW;
+    const int nbb = (n + 255) / 256;
+    VjpWs w{};
+    w.h        = reinterpret_cast<double*>(take(dn));
+    w.a        = reinterpret_cast<double*>(take(dn));
+    w.ia       = reinterpret_cast<double*>(take(dn));
+    w.D        = reinterpret_cast<double*>(take(dn));
+    w.Bf       = reinterpret_cast<double*>(take(dn));
+    w.Sf       = reinterpret_cast<double*>(take(dn));
+    w.Ld       = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(n)));
+    w.mom_part = reinterpret_cast<double*>(take(sizeof(double) * 16 * static_cast<size_t>(agg_prep_blocks(n))));
+    w.mom      = reinterpret_cast<double*>(take(sizeof(double) * 16));
+    w.gpart    = reinterpret_cast<double*>(take(sizeof(double) * 4 * static_cast<size_t>(ntile > nbb ? ntile : nbb)));
+    w.counter  = reinterpret_cast<int*>(take(sizeof(int) * 8));
+    if (ws) *ws = w;
+    return off;
+}
+
+struct AggVjpArgs {
+    const double* N; const double* x; const double* lam; double* gN; double* gp;
+    int n; int kernel; double beta0, beta_br, beta_sh;
+};
+struct BrkVjpArgs {
+    const double* N; const double* x; const double* t_q; const double* bw_q; const double* lam;
+    double* gN; double* gp;
+    int n; int n_quad; int selection; double S0, v_ref, alpha, v_min;
+};
+cudaError_t agg_vjp_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s);
+cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s);
 
 // ---- profiling hook ----------------------------------------------------------
 // When both are non-null the aggregation launcher records g_prof_start right

@@ -1,0 +1,467 @@
+// =============================================================================
+// vjp.cu -- vector-Jacobian products (adjoints) of the aggregation and
+// breakage RHS, FP64, sm_103a. No counterpart in the reference.
+//
+// Given lambda = dL/drhs, the calls ADD dL/dN into gN and dL/d(parameters)
+// into a small device array, like the forward calls add into rhs.
+//
+// Aggregation. For pair p = (j <= k): rate_p = c_p beta_jk N_j N_k (c = 1/2 on
+// the diagonal), L = sum_p rate_p G_p with G_p = P_p - lambda_j - lambda_k,
+// P_p = lambda_lo + w (lambda_hi - lambda_lo) (lambda_{n-1} for pairs clipped
+// at x[n-1]). Then
+//   dL/dN_m  = sum_k G(m,k) beta(m,k) N_k           (all partners k, k = m once)
+//   dL/dbeta_X = 1/2 sum_m N_m A_X[m],  A_X[m] = sum_k G(m,k) f_X(m,k) N_k
+// where beta = sum_X beta_X f_X. The -lambda_m - lambda_k part of G reduces to
+// moments of N and of lambda*N (as the forward death term); the P part is a
+// row gather: row m meets each partner k once as the smaller member
+// ("upper", lo = m + Ld[k-m]) and once as the larger ("lower",
+// lo = k + Ld[m-k]). P uses the reference's weight numerator fl(x_j + x_k) -
+// x_lo (integer pipe) times (lambda_{lo+1} - lambda_lo)/(x_{lo+1} - x_lo).
+// One CTA owns each row tile and reduces it in a fixed order -> deterministic.
+//
+// Breakage. rhs_i = -S_i N_i + sum_j S_j N_j sum_q bw_q eta_i(x_j t_q) over
+// the guarded parents. With Q_j = -lambda_j + sum_q bw_q P_jq:
+//   dL/dN_j = S_j Q_j, dL/dS0 = sum_j (S_j/S0) N_j Q_j, dL/dv_ref, dL/dalpha
+// (PowerLaw: dS/dalpha = S ln(x/v_ref)), dL/dv_min = 0 (threshold step).
+// =============================================================================
+#include "pbe_internal.cuh"
+#include "exact_weight.cuh"
+
+namespace pbe_gb300 {
+namespace {
+
+constexpr int VW = kTileW;              // rows per task
+constexpr int kVRows = 3 * VW;          // three accumulators per row
+
+// dL/dN needs, per kernel type K, up to three row sums (see vjp_main_kernel):
+//   K=0: R0 = sum P N_k                       f = 1
+//   K=1: R0 = sum P N_k, R1 = sum P h_k       f N_k = x_m N_k + h_k
+//   K=2: R0 = sum P h_k                       f N_k = x_m h_k
+//   K=3: R0 = sum P N_k Bf                    Brownian factor per lag
+//   K=4: R1 = sum_upper P N_k Sf, R2 = sum_lower P h_k Sf   (shear f = x_min Sf)
+//   K=5: R0, R1, R2 as K=3 and K=4
+// The generic (non-geometric) path accumulates sum P N_k f directly: R0 for
+// K=0..3 (f = f_0 or Bf), R1 for the shear part.
+
+// -------------------------------------------------------------------------
+// prep: per-bin values, lag factors (no beta, no diagonal 1/2), moments of N
+// and lambda*N, geometric deviation. Moment slots per block (stride 16):
+// 0..4 sum N{1/a, 1, a, a^2, x}, 5..9 the same of lambda*N, 10 max dev.
+// -------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPrepThreads)
+vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                const double* __restrict__ lam, int n, VjpWs ws)
+{
+    __shared__ double sh[kPrepThreads / 32];
+    const int i = blockIdx.x * kPrepThreads + threadIdx.x;
+    double m[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) m[q] = 0.0;
+    double dev = 0.0;
+    if (i < n) {
+        const double xi = x[i], Ni = N[i], li = lam[i];
+        const double ai = cbrt(xi), iai = 1.0 / ai;
+        ws.h[i] = xi * Ni;
+        ws.a[i] = ai;
+        ws.ia[i] = iai;
+        ws.D[i] = (i < n - 1) ? (lam[i + 1] - li) / (x[i + 1] - xi) : 0.0;
+        const double w[5] = {iai, 1.0, ai, ai * ai, xi};
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            m[q] = w[q] * Ni;
+            m[5 + q] = w[q] * (li * Ni);
+        }
+        const double x0 = x[0];
+        const double rho = ai / cbrt(x0);
+        ws.Bf[i] = rho + 1.0 / rho + 2.0;
+        const double s = 1.0 + rho;
+        ws.Sf[i] = (s * s) * s;
+        const double v = x0 + xi;
+        ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        if (n >= 2) {
+            const double lr = log(x[n - 1] / x0) / static_cast<double>(n - 1);
+            dev = fabs(log(xi / x0) - static_cast<double>(i) * lr);
+            if (!(dev == dev)) dev = 1.0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) {
+        const double s = block_sum(m[q], sh);
+        if (threadIdx.x == 0) ws.mom_part[blockIdx.x * 16 + q] = s;
+    }
+    dev = warp_max(dev);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0.0;
+        for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
+        ws.mom_part[blockIdx.x * 16 + 10] = mx;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
+{
+    __shared__ double sh[8];
+    const int nb = (n + kPrepThreads - 1) / kPrepThreads;
+    for (int q = 0; q < 10; ++q) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ws.mom_part[b * 16 + q];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) ws.mom[q] = s;
+    }
+    double mx = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) mx = fmax(mx, ws.mom_part[b * 16 + 10]);
+    mx = warp_max(mx);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < 8; ++w) mx = fmax(mx, sh[w]);
+        const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
+        ws.mom[10] = (n >= 2 && mx <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
+        ws.counter[0] = 0;
+    }
+}
+
+// sum_k f(m,k) N_k (or lambda_k N_k) from the moments mo[0..4].
+template <int K, int X>   // X: 0 = beta0 / Brownian part, 1 = shear part
+__device__ __forceinline__ double moment_factor(double xm, double am, double iam, const double* mo)
+{
+    if constexpr (K == 0) return mo[1];
+    else if constexpr (K == 1) return fma(xm, mo[1], mo[4]);
+    else if constexpr (K == 2) return xm * mo[4];
+    else if constexpr (X == 0) return fma(am, mo[0], iam * mo[2]) + 2.0 * mo[1];
+    else return fma(xm, mo[1], (3.0 * am) * fma(am, mo[2], mo[3])) + mo[4];
+}
+
+template <int K>
+__global__ void __launch_bounds__(kMainThreads, 2)
+vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
+                int ntile, double b0, double bbr, double bsh)
+{
+    extern __shared__ double red[];               // [kVRows][kMainThreads]
+    __shared__ double part4[4][kVRows];
+    __shared__ double fin[kVRows];
+    __shared__ double gsh[VW][2];
+    __shared__ int s_task;
+
+    const int tid = threadIdx.x;
+    const bool geo = ws.mom[10] != 0.0;
+    const double lamlast = lam[n - 1];
+
+    for (;;) {
+        if (tid == 0) s_task = atomicAdd(ws.counter, 1);
+        __syncthreads();
+        const int task = s_task;
+        __syncthreads();
+        if (task >= ntile) break;
+        const int I = task * VW;
+        const int tmax = min(VW, n - I);          // rows I .. I+tmax-1
+
+        double R0[VW], R1[VW], R2[VW];
+#pragma unroll
+        for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; R2[t] = 0.0; }
+
+        if (geo) {
+            for (int d = tid; d < n; d += kMainThreads) {
+                const int L = __ldg(ws.Ld + d);
+                const double Bf = __ldg(ws.Bf + d), Sf = __ldg(ws.Sf + d);
+                // upper visits: partner k = m + d
+#pragma unroll
+                for (int t = 0; t < VW; ++t) {
+                    const int m = I + t, k = m + d;
+                    if (t < tmax && k < n) {
+                        const double Nk = __ldg(N + k);
+                        const int lo = (L >= kLagClipAll) ? n : m + L;
+                        double P;
+                        if (lo >= n - 1) {
+                            P = lamlast;
+                        } else {
+                            const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + m),
+                                                               __ldg(x + lo), 0);
+                            P = fma(th, __ldg(ws.D + lo), __ldg(lam + lo));
+                        }
+                        if constexpr (K == 2) {
+                            R0[t] = fma(P, __ldg(ws.h + k), R0[t]);
+                        } else {
+                            const double t1 = P * Nk;
+                            if constexpr (K == 0) R0[t] += t1;
+                            if constexpr (K == 1) { R0[t] += t1; R1[t] = fma(P, __ldg(ws.h + k), R1[t]); }
+                            if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
+                            if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sf, R1[t]);
+                        }
+                    }
+                }
+                // lower visits: partner k = m - d (d >= 1)
+                if (d >= 1 && L < kLagClipAll) {
+                    const int e = L - d;
+#pragma unroll
+                    for (int t = 0; t < VW; ++t) {
+                        const int m = I + t, k = m - d;
+                        if (t < tmax && k >= 0) {
+                            const int lo = m + e;
+                            double P;
+                            if (lo >= n - 1) {
+                                P = lamlast;
+                            } else {
+                                const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
+                                                                   __ldg(x + lo), 0);
+                                P = fma(th, __ldg(ws.D + lo), __ldg(lam + lo));
+                            }
+                            if constexpr (K == 2) {
+                                R0[t] = fma(P, __ldg(ws.h + k), R0[t]);
+                            } else {
+                                const double Nk = __ldg(N + k);
+                                if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
+                                if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(ws.h + k), R1[t]); }
+                                if constexpr (K == 3 || K == 5) R0[t] = fma(P * Nk, Bf, R0[t]);
+                                if constexpr (K == 4 || K == 5) R2[t] = fma(P * __ldg(ws.h + k), Sf, R2[t]);
+                            }
+                        }
+                    }
+                } else if (d >= 1) {
+                    // every pair of this lag is clipped: P = lambda_{n-1}
+#pragma unroll
+                    for (int t = 0; t < VW; ++t) {
+                        const int m = I + t, k = m - d;
+                        if (t < tmax && k >= 0) {
+                            if constexpr (K == 2) {
+                                R0[t] = fma(lamlast, __ldg(ws.h + k), R0[t]);
+                            } else {
+                                const double Nk = __ldg(N + k);
+                                if constexpr (K == 0) R0[t] = fma(lamlast, Nk, R0[t]);
+                                if constexpr (K == 1) { R0[t] = fma(lamlast, Nk, R0[t]); R1[t] = fma(lamlast, __ldg(ws.h + k), R1[t]); }
+                                if constexpr (K == 3 || K == 5) R0[t] = fma(lamlast * Nk, Bf, R0[t]);
+                                if constexpr (K == 4 || K == 5) R2[t] = fma(lamlast * __ldg(ws.h + k), Sf, R2[t]);
+                            }
+                        }
+                    }
+                }
+            }
+        } else {
+            // generic grid: thread tid owns the partner chunk [k0, k1), walks the
+            // bracket of x_m + x_k upward along it for every row of the tile
+            const int chunk = (n + kMainThreads - 1) / kMainThreads;
+            const int k0 = min(n, tid * chunk), k1 = min(n, k0 + chunk);
+            const long long blast = dbits(x[n - 1]);
+#pragma unroll 1
+            for (int t = 0; t < tmax; ++t) {
+                const int m = I + t;
+                const double xm = x[m], am = ws.a[m], iam = ws.ia[m];
+                int lo = -1;
+                double r0 = 0.0, r1 = 0.0;
+                for (int k = k0; k < k1; ++k) {
+                    const double xk = x[k];
+                    const double v = xm + xk;
+                    double P;
+                    if (dbits(v) >= blast) {
+                        P = lamlast;
+                    } else {
+                        if (lo < 0) lo = bracket_lo(x, n, v);
+                        while (dbits(x[lo + 1]) <= dbits(v)) ++lo;
+                        P = fma(v - x[lo], ws.D[lo], lam[lo]);
+                    }
+                    const double PN = P * N[k];
+                    if constexpr (K == 0) r0 += PN;
+                    if constexpr (K == 1) r0 = fma(PN, xm + xk, r0);
+                    if constexpr (K == 2) r0 = fma(PN, xm * xk, r0);
+                    if constexpr (K == 3 || K == 5) r0 = fma(PN, fma(am, ws.ia[k], ws.a[k] * iam) + 2.0, r0);
+                    if constexpr (K == 4 || K == 5) { const double s = am + ws.a[k]; r1 = fma(PN, (s * s) * s, r1); }
+                }
+#pragma unroll
+                for (int u = 0; u < VW; ++u)
+                    if (u == t) { R0[u] = r0; R1[u] = r1; }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < VW; ++t) {
+            red[t * kMainThreads + tid] = R0[t];
+            red[(VW + t) * kMainThreads + tid] = R1[t];
+            red[(2 * VW + t) * kMainThreads + tid] = R2[t];
+        }
+        __syncthreads();
+        if (tid < kVRows * 4) {
+            const int r = tid >> 2, c = tid & 3;
+            const double* p = red + r * kMainThreads + c * 64;
+            double s = 0.0;
+#pragma unroll 8
+            for (int q = 0; q < 64; ++q) s += p[q];
+            part4[c][r] = s;
+        }
+        __syncthreads();
+        if (tid < kVRows) fin[tid] = (part4[0][tid] + part4[1][tid]) + (part4[2][tid] + part4[3][tid]);
+        __syncthreads();
+        if (tid < VW) {
+            const int t = tid, m = I + t;
+            double gB = 0.0, gS = 0.0;
+            if (t < tmax) {
+                const double xm = x[m], am = ws.a[m], iam = ws.ia[m], lm = lam[m], Nm = N[m];
+                const double* M = ws.mom;        // moments of N
+                const double* Lm = ws.mom + 5;   // moments of lambda*N
+                double AX0 = 0.0, AX1 = 0.0;     // A for beta0 / Brownian, and for shear
+                if constexpr (K <= 2) {
+                    double T = fin[t];
+                    if (geo) {
+                        if constexpr (K == 1) T = fma(xm, fin[t], fin[VW + t]);
+                        if constexpr (K == 2) T = xm * fin[t];
+                    }
+                    AX0 = T - fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
+                }
+                if constexpr (K == 3 || K == 5)
+                    AX0 = fin[t] - fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
+                if constexpr (K == 4 || K == 5) {
+                    const double T = geo ? fma(xm, fin[VW + t], fin[2 * VW + t]) : fin[VW + t];
+                    AX1 = T - fma(lm, moment_factor<K, 1>(xm, am, iam, M), moment_factor<K, 1>(xm, am, iam, Lm));
+                }
+                double g;
+                if constexpr (K <= 2) g = b0 * AX0;
+                else if constexpr (K == 3) g = bbr * AX0;
+                else if constexpr (K == 4) g = bsh * AX1;
+                else g = fma(bbr, AX0, bsh * AX1);
+                gN[m] += g;
+                gB = 0.5 * Nm * AX0;
+                gS = 0.5 * Nm * AX1;
+            }
+            gsh[t][0] = gB;
+            gsh[t][1] = gS;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double s0 = 0.0, s1 = 0.0;
+            for (int t = 0; t < VW; ++t) { s0 += gsh[t][0]; s1 += gsh[t][1]; }
+            // slots: 0 beta0, 1 beta_br, 2 beta_sh
+            ws.gpart[task * 4 + 0] = (K <= 2) ? s0 : 0.0;
+            ws.gpart[task * 4 + 1] = (K == 3 || K == 5) ? s0 : 0.0;
+            ws.gpart[task * 4 + 2] = (K == 4 || K == 5) ? s1 : 0.0;
+        }
+        __syncthreads();
+    }
+}
+
+// gp[0..2] += fixed-order sums of the per-tile partials
+__global__ void __launch_bounds__(256) vjp_gfin_kernel(int ntile, VjpWs ws, double* gp, int nslots)
+{
+    __shared__ double sh[8];
+    for (int q = 0; q < nslots; ++q) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < ntile; b += blockDim.x) s += ws.gpart[b * 4 + q];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) gp[q] += s;
+    }
+}
+
+// -------------------------------------------------------------------------
+// breakage VJP: one thread per parent j; block partials of the parameter sums
+// -------------------------------------------------------------------------
+template <int F>
+__global__ void __launch_bounds__(256)
+brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
+               const double* __restrict__ t_q, const double* __restrict__ bw_q,
+               const double* __restrict__ lam, double* __restrict__ gN, double* part, int n,
+               int nq, double S0, double v_ref, double alpha, double v_min)
+{
+    __shared__ double sh[8];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (j < n) {
+        const double xj = x[j], Nj = N[j];
+        const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
+        if ((S != 0.0) && (Nj > kBreakageNMin)) {
+            double Q = -lam[j];
+            for (int q = 0; q < nq; ++q) {
+                const double v = xj * t_q[q];
+                const int lo = frag_bracket(x, n, v);
+                double P;
+                if (lo < 0) P = lam[0];
+                else if (lo >= n - 1) P = lam[n - 1];
+                else {
+                    const double xl = x[lo], xh = x[lo + 1];
+                    const double eta = (v - xl) / (xh - xl);
+                    P = fma(1.0 - eta, lam[lo], eta * lam[lo + 1]);
+                }
+                Q = fma(bw_q[q], P, Q);
+            }
+            gN[j] += S * Q;
+            const double NQ = Nj * Q;
+            p0 = (S / S0) * NQ;
+            if constexpr (F == 1) p1 = -(S / v_ref) * NQ;
+            if constexpr (F == 2) {
+                p1 = -(alpha * S / v_ref) * NQ;
+                p2 = S * log(xj / v_ref) * NQ;
+            }
+        }
+    }
+    const double s0 = block_sum(p0, sh);
+    const double s1 = block_sum(p1, sh);
+    const double s2 = block_sum(p2, sh);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x * 4 + 0] = s0;
+        part[blockIdx.x * 4 + 1] = s1;
+        part[blockIdx.x * 4 + 2] = s2;
+        part[blockIdx.x * 4 + 3] = 0.0;
+    }
+}
+
+template <int K>
+cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStream_t s)
+{
+    const int n = a.n;
+    const int nb = (n + kPrepThreads - 1) / kPrepThreads;
+    const int ntile = (n + VW - 1) / VW;
+    const int grid = ntile < 2 * num_sms ? ntile : 2 * num_sms;
+    const size_t smem = sizeof(double) * kVRows * kMainThreads;
+    cudaError_t e = cudaFuncSetAttribute(vjp_main_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    vjp_prep_kernel<<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
+    vjp_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
+    vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, a.beta0,
+                                                         a.beta_br, a.beta_sh);
+    vjp_gfin_kernel<<<1, 256, 0, s>>>(ntile, ws, a.gp, 3);
+    return cudaGetLastError();
+}
+
+template <int F>
+cudaError_t brk_vjp_f(const BrkVjpArgs& a, const VjpWs& ws, cudaStream_t s)
+{
+    const int nb = (a.n + 255) / 256;
+    brk_vjp_kernel<F><<<nb, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.lam, a.gN, ws.gpart, a.n,
+                                         a.n_quad, a.S0, a.v_ref, a.alpha, a.v_min);
+    vjp_gfin_kernel<<<1, 256, 0, s>>>(nb, ws, a.gp, 4);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t agg_vjp_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+{
+    VjpWs ws;
+    vjp_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
+    switch (a.kernel) {
+    case 0: return agg_vjp_k<0>(a, ws, num_sms, s);
+    case 1: return agg_vjp_k<1>(a, ws, num_sms, s);
+    case 2: return agg_vjp_k<2>(a, ws, num_sms, s);
+    case 3: return agg_vjp_k<3>(a, ws, num_sms, s);
+    case 4: return agg_vjp_k<4>(a, ws, num_sms, s);
+    case 5: return agg_vjp_k<5>(a, ws, num_sms, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s)
+{
+    VjpWs ws;
+    vjp_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
+    switch (a.selection) {
+    case 0: return brk_vjp_f<0>(a, ws, s);
+    case 1: return brk_vjp_f<1>(a, ws, s);
+    case 2: return brk_vjp_f<2>(a, ws, s);
+    case 3: return brk_vjp_f<3>(a, ws, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace pbe_gb300

@@ -31,8 +31,10 @@ from ._lib import (  # noqa: F401
 )
 from .rhs import (  # noqa: F401
     aggregation_rhs,
+    aggregation_rhs_vjp,
     aggregation_workspace_bytes,
     breakage_rhs,
+    breakage_rhs_vjp,
     breakage_workspace_bytes,
 )
 from . import grids, quadrature  # noqa: F401

@@ -10,7 +10,9 @@ import ctypes
 import os
 
 _PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(_PKG_DIR, "lib", "libpbe_gb300.so")
+# PBE_GB300_LIB selects another build of the library (e.g. one compiled with
+# different tuning macros); default: the in-tree build.
+LIB_PATH = os.environ.get("PBE_GB300_LIB") or os.path.join(_PKG_DIR, "lib", "libpbe_gb300.so")
 
 # cudaError_t values used by the API
 SUCCESS = 0
@@ -82,6 +84,11 @@ _SIGNATURES = {
     "pbe_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "pbe_version": (ctypes.c_int, []),
     "pbe_set_profile_events": (ctypes.c_int, [_P, _P]),
+    "pbe_vjp_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int]),
+    "pbe_aggregation_rhs_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(AggregationParams),
+                                               _P, ctypes.c_size_t, _P]),
+    "pbe_breakage_rhs_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(BreakageParams),
+                                            _P, ctypes.c_size_t, _P]),
 }
 
 _lib = None

@@ -96,3 +96,20 @@ def aggregation_workspace_bytes(n: int, mode: int = MODE_DEFAULT) -> int:
 
 def breakage_workspace_bytes(n: int, n_quad: int, mode: int = MODE_DEFAULT) -> int:
     return int(_lib.load().pbe_breakage_workspace_bytes(int(n), int(n_quad), int(mode)))
+
+
+def aggregation_rhs_vjp(N: Array, x: Array, lam: Array, gN: Array, gparams: Array,
+                        params: AggregationParams, stream=None) -> int:
+    """gN += dL/dN, gparams[0:3] += dL/d(beta0, beta_br, beta_sh) for L = lam . rhs_agg."""
+    return _lib.load().pbe_aggregation_rhs_vjp(_ptr(N, "N"), _ptr(x, "x"), _ptr(lam, "lambda"),
+                                               _ptr(gN, "gN"), _ptr(gparams, "gparams"), params,
+                                               None, 0, _stream(stream))
+
+
+def breakage_rhs_vjp(N: Array, x: Array, t_q: Array, bw_q: Array, lam: Array, gN: Array,
+                     gparams: Array, params: BreakageParams, stream=None) -> int:
+    """gN += dL/dN, gparams[0:4] += dL/d(S0, v_ref, alpha, v_min) for L = lam . rhs_brk."""
+    return _lib.load().pbe_breakage_rhs_vjp(_ptr(N, "N"), _ptr(x, "x"), _ptr(t_q, "t_q"),
+                                            _ptr(bw_q, "bw_q"), _ptr(lam, "lambda"), _ptr(gN, "gN"),
+                                            _ptr(gparams, "gparams"), params, None, 0,
+                                            _stream(stream))

@@ -105,7 +105,7 @@ def make_grid(kind, n, rng):
     if kind == "geo_ref":         # the reference tests' grid, by repeated multiplication
         return pg.grids.geometric_by_product(n, 1e-18, 1.122018)
     if kind == "geo_coarse":      # ratio 2: x_j + x_k lands exactly on pivots often
-        return pg.grids.geometric_pow2(n, 1e-150, 1.0)   # finite up to n ~ 1500
+        return np.ldexp(1e-150, np.arange(n))             # exact, finite up to n ~ 1500
     if kind == "generic":         # non-geometric, strictly increasing, spans ~e^40
         steps = rng.uniform(0.2, 1.8, size=n) * (40.0 / max(n, 1))
         return 1e-20 * np.exp(np.cumsum(steps))

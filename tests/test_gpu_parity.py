@@ -21,6 +21,8 @@ GRIDS = ["geo_fine", "geo_ref", "geo_coarse", "generic", "generic_wide", "linear
 def test_aggregation_matches_oracle(kernel, b0, bbr, bsh, grid, mode):
     rng = np.random.default_rng(1000 * kernel + len(grid))
     for n in (1, 2, 3, 17, 64, 300, 1111):
+        if grid == "geo_coarse" and n > 700:
+            continue   # x_n ~ 2^n: beta0 x_j x_k would overflow in the reference formula
         x = make_grid(grid, n, rng)
         for ic in ("lognormal", "random"):
             N = make_N(ic, x, rng)
