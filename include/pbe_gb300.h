@@ -160,6 +160,120 @@ int pbe_breakage_rhs_vjp(const double* N, const double* x, const double* t_q,
                          double* gparams, const pbe_brk_params_t* params,
                          void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched cells (no counterpart in the reference, whose callers loop over
+ * cells and launch per cell and per RK4 stage, with host round trips between
+ * stages: examples/common/pbe_examples_utils.hpp:409-456, driven per time
+ * step as in examples/flocculation_two_stage/main.cpp:311-355).
+ *
+ * A plan describes n_cells independent PBE instances ("cells"). Cell c has
+ * cell_n[c] sections on the first cell_n[c] pivots of grid cell_grid[c]. The
+ * n_grids grids are given packed, grid after grid, in grid_x (grid g has
+ * grid_n[g] strictly increasing positive pivots). Cells that share a grid
+ * share its tables, which are built once per plan. All cells use one
+ * aggregation kernel type (PBE_AGG_*, or -1 for none) and one breakage
+ * selection (PBE_SEL_*, or -1 for none) with one daughter table (n_quad
+ * points, 0 < t_q <= 1); each cell has its own coefficients, read from a
+ * device array of pbe_batch_cell_params_t at every call.
+ *
+ * Packed cell state: cell c owns entries [off_c, off_c + cell_n[c]) of N and
+ * rhs, off = exclusive prefix sum of cell_n in cell order (pbe_batch_offsets).
+ *
+ * Results are those of the single-instance functions on each cell (same
+ * formulas, same clip rules) up to the order of FP64 summation; for one plan
+ * they are bitwise reproducible run to run (no atomics on the data path).
+ *
+ * The plan owns device memory for its tables, its task schedule and its stage
+ * arrays (about 7 doubles per packed bin) and caches one CUDA graph. Use a
+ * plan from one stream at a time. The plan-creation arrays are HOST arrays;
+ * the call arrays (N, rhs, params) are DEVICE arrays.
+ * ------------------------------------------------------------------------- */
+typedef struct pbe_batch_plan* pbe_batch_t;
+
+typedef struct pbe_batch_cell_params {
+    double beta0, beta_br, beta_sh;    /* aggregation coefficients (pbe_agg_params_t)   */
+    double S0, v_ref, alpha, v_min;    /* selection parameters (pbe_brk_params_t)       */
+    double reserved;                   /* set to 0                                      */
+} pbe_batch_cell_params_t;
+
+/* flags of pbe_batch_create */
+enum {
+    PBE_BATCH_TUNE   = 1,  /* pick the tile group size per section-count class by timing
+                              candidates on the device (results cached per process, and
+                              in the file named by PBE_GB300_TUNE_CACHE when set)        */
+    PBE_BATCH_RETUNE = 2   /* like TUNE, ignoring cached results                          */
+};
+
+/* Builds a plan. Returns 1 (InvalidValue) for inconsistent sizes, a cell with
+ * more sections than its grid, non-increasing or non-positive pivots, or t_q
+ * outside (0, 1]; 2 (MemoryAllocation) when device memory runs out. */
+int pbe_batch_create(pbe_batch_t* plan, int n_grids, const int* grid_n, const double* grid_x,
+                     int n_cells, const int* cell_n, const int* cell_grid, int kernel_type,
+                     int selection, int n_quad, const double* t_q, const double* bw_q,
+                     int flags, void* stream);
+
+/* Frees the plan and its device memory (cudaFree waits for device work in
+ * flight). NULL is accepted. */
+int pbe_batch_destroy(pbe_batch_t plan);
+
+/* offsets (host, n_cells + 1 entries) receives the packed offsets; the last
+ * entry is the packed length. */
+int pbe_batch_offsets(pbe_batch_t plan, long long* offsets);
+
+/* rhs += RHS(N) for every cell (aggregation + breakage). */
+int pbe_batch_rhs(pbe_batch_t plan, const double* N, double* rhs,
+                  const pbe_batch_cell_params_t* params, void* stream);
+
+/* n_steps classical RK4 steps of size dt on every cell, in place on N, as one
+ * CUDA graph launch (captured on the first call and reused while N, params,
+ * dt and n_steps stay the same). The stage arithmetic is that of the
+ * reference examples' rk4_step (pbe_examples_utils.hpp:416-456). */
+int pbe_batch_rk4(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                  double dt, int n_steps, void* stream);
+
+/* The same integration as a per-cell launch loop: for every step, cell and
+ * stage, the single-instance aggregation and breakage calls plus a stage
+ * update kernel (no graph, no batching). Baseline and cross-check. */
+int pbe_batch_rk4_percell(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                          double dt, int n_steps, void* stream);
+
+/* Schedule in use: group_size[c] (16 entries) = threads per tile task for
+ * cells with floor(log2(n)) == c (0 where no cell falls), *n_bundles = the
+ * number of bundles in the persistent launch. Either pointer may be NULL. */
+int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles);
+
+/* ---------------------------------------------------------------------------
+ * Checkpointed RK4 adjoint of one instance (no counterpart in the reference,
+ * which has no derivatives). A tape runs n_steps classical RK4 steps of size
+ * dt -- the stage arithmetic of the reference examples' rk4_step
+ * (examples/common/pbe_examples_utils.hpp:416-456) -- saving N every
+ * checkpoint_every steps; the backward pass recomputes one segment at a time
+ * from its checkpoint and reverses every step with the VJP kernels, so memory
+ * is (n_steps / checkpoint_every + 4 checkpoint_every + 16) n doubles.
+ * Step s uses parameter set step_set[s] (step_set NULL: set 0) of agg_sets /
+ * brk_sets (host arrays of n_sets structs; either may be NULL for a run
+ * without that term; all sets share n, kernel_type, selection and n_quad).
+ * ------------------------------------------------------------------------- */
+typedef struct pbe_rk4_tape* pbe_rk4_tape_t;
+
+int pbe_rk4_tape_create(pbe_rk4_tape_t* tape, int n_steps, double dt, int checkpoint_every,
+                        int n_sets, const pbe_agg_params_t* agg_sets,
+                        const pbe_brk_params_t* brk_sets, const int* step_set);
+
+int pbe_rk4_tape_destroy(pbe_rk4_tape_t tape);
+
+/* N (device, n): N(0) in, N(T) out. x, t_q, bw_q (device) are used again by
+ * the backward pass and must stay valid until it is enqueued. */
+int pbe_rk4_tape_forward(pbe_rk4_tape_t tape, double* N, const double* x, const double* t_q,
+                         const double* bw_q, void* stream);
+
+/* Given lambda_T = dL/dN(T) (device, n), writes gN0 = dL/dN(0) (device, n),
+ * g_agg[3 m + j] = dL/d(beta0, beta_br, beta_sh)[j] of set m and
+ * g_brk[4 m + j] = dL/d(S0, v_ref, alpha, v_min)[j] of set m (device; may be
+ * NULL for an absent term). Returns cudaErrorInvalidValue before a forward. */
+int pbe_rk4_tape_backward(pbe_rk4_tape_t tape, const double* lambda_T, double* gN0,
+                          double* g_agg, double* g_brk, void* stream);
+
 /* Human-readable name of a return code (cudaGetErrorString). */
 const char* pbe_error_string(int code);
 

@@ -418,6 +418,95 @@ int oracle_breakage_rhs_vjp(const double* N, const double* x, const double* t_q,
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Discrete adjoint of n_steps classical RK4 steps (no counterpart in the
+// reference; its forward step is examples/common/pbe_examples_utils.hpp:416-456,
+// restated by oracle_rk4_step above). Step s uses parameter set step_set[s]
+// (NULL: set 0). agg_sets[m] = {kernel (< 0: none), beta0, beta_br, beta_sh},
+// brk_sets[m] = {selection (< 0: none), S0, v_ref, alpha, v_min}. Every stage
+// state of every step is kept (no checkpointing: this is the checker).
+// Given lamT = dL/dN(T): NT = N(T), gN0 = dL/dN(0),
+// g_agg[m][0..2] = dL/d(beta0, beta_br, beta_sh) of set m,
+// g_brk[m][0..3] = dL/d(S0, v_ref, alpha, v_min) of set m.
+// Per step, with h = dt/2, c = dt/6 and J_s the RHS Jacobian at stage s:
+//   a4 = c lam', mu4 = J4^T a4, a3 = 2c lam' + dt mu4, mu3 = J3^T a3,
+//   a2 = 2c lam' + h mu3, mu2 = J2^T a2, a1 = c lam' + h mu2, mu1 = J1^T a1,
+//   lam = lam' + mu1 + mu2 + mu3 + mu4, dL/dtheta += sum_s (df/dtheta)^T a_s.
+int oracle_rk4_adjoint(const double* N0, const double* x, int n, double dt, int n_steps,
+                       const int* step_set, int n_sets, const double* agg_sets,
+                       const double* brk_sets, const double* t_q, const double* bw_q,
+                       int n_quad, const double* lamT, double* NT, double* gN0,
+                       double* g_agg, double* g_brk)
+{
+    if (n <= 0 || n_steps < 0 || n_sets <= 0 || !N0 || !x || !lamT || !NT || !gN0) return 1;
+    const size_t un = static_cast<size_t>(n);
+    std::vector<double> Y(static_cast<size_t>(n_steps) * 4 * un);
+    std::vector<double> N(N0, N0 + n), k(un), acc(un), st(un);
+    auto set_of = [&](int s) { return step_set ? step_set[s] : 0; };
+    auto R = [&](int m, const double* Nin, double* out) {
+        std::fill(out, out + n, 0.0);
+        const double* A = agg_sets ? agg_sets + 4 * m : nullptr;
+        const double* B = brk_sets ? brk_sets + 5 * m : nullptr;
+        if (A && A[0] >= 0)
+            oracle_aggregation_rhs(Nin, x, out, nullptr, nullptr, n, 0.0, 0.0,
+                                   static_cast<int>(A[0]), A[1], A[2], A[3], 1);
+        if (B && B[0] >= 0 && n_quad > 0)
+            oracle_breakage_rhs(Nin, x, t_q, bw_q, out, nullptr, n, n_quad,
+                                static_cast<int>(B[0]), B[1], B[2], B[3], B[4]);
+    };
+    const double h = 0.5 * dt, c6 = dt / 6.0;
+    const double cs[3] = {h, h, dt};
+    for (int s = 0; s < n_steps; ++s) {
+        const int m = set_of(s);
+        double* Ys = Y.data() + static_cast<size_t>(s) * 4 * un;
+        std::copy(N.begin(), N.end(), Ys);
+        for (int q = 0; q < 4; ++q) {
+            R(m, Ys + q * un, k.data());
+            for (int i = 0; i < n; ++i) {
+                acc[i] = (q == 0) ? k[i] : acc[i] + ((q == 3) ? k[i] : 2.0 * k[i]);
+                if (q < 3) Ys[(q + 1) * un + i] = N[i] + cs[q] * k[i];
+            }
+        }
+        for (int i = 0; i < n; ++i) N[i] += c6 * acc[i];
+    }
+    std::copy(N.begin(), N.end(), NT);
+    std::vector<double> lam(lamT, lamT + n), lp(un), a(un), mu(un), lsum(un);
+    if (g_agg) std::fill(g_agg, g_agg + 3 * n_sets, 0.0);
+    if (g_brk) std::fill(g_brk, g_brk + 4 * n_sets, 0.0);
+    std::vector<double> ga(3), gb(4);
+    for (int s = n_steps - 1; s >= 0; --s) {
+        const int m = set_of(s);
+        const double* A = agg_sets ? agg_sets + 4 * m : nullptr;
+        const double* B = brk_sets ? brk_sets + 5 * m : nullptr;
+        const double* Ys = Y.data() + static_cast<size_t>(s) * 4 * un;
+        lp = lam;
+        lsum = lam;
+        std::fill(mu.begin(), mu.end(), 0.0);
+        for (int q = 3; q >= 0; --q) {
+            // a_q = w_q c lam' + (coefficient of stage q+1 on k_q) mu_{q+1}
+            const double w = (q == 0 || q == 3) ? c6 : 2.0 * c6;
+            for (int i = 0; i < n; ++i) a[i] = (q == 3) ? w * lp[i] : w * lp[i] + cs[q] * mu[i];
+            std::fill(mu.begin(), mu.end(), 0.0);
+            const double* Yq = Ys + q * un;
+            std::fill(ga.begin(), ga.end(), 0.0);
+            std::fill(gb.begin(), gb.end(), 0.0);
+            if (A && A[0] >= 0)
+                oracle_aggregation_rhs_vjp(Yq, x, a.data(), mu.data(), ga.data(), nullptr, nullptr,
+                                           n, 0.0, 0.0, static_cast<int>(A[0]), A[1], A[2], A[3], 1);
+            if (B && B[0] >= 0 && n_quad > 0)
+                oracle_breakage_rhs_vjp(Yq, x, t_q, bw_q, a.data(), mu.data(), gb.data(), nullptr,
+                                        nullptr, n, n_quad, static_cast<int>(B[0]), B[1], B[2],
+                                        B[3], B[4]);
+            if (g_agg) for (int j = 0; j < 3; ++j) g_agg[3 * m + j] += ga[j];
+            if (g_brk) for (int j = 0; j < 4; ++j) g_brk[4 * m + j] += gb[j];
+            for (int i = 0; i < n; ++i) lsum[i] += mu[i];
+        }
+        lam = lsum;
+    }
+    std::copy(lam.begin(), lam.end(), gN0);
+    return 0;
+}
+
 int oracle_version(void) { return 1; }
 
 } // extern "C"

@@ -51,6 +51,10 @@ def _lib():
         lib.oracle_breakage_rhs_vjp.argtypes = [_D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        lib.oracle_rk4_adjoint.restype = ctypes.c_int
+        lib.oracle_rk4_adjoint.argtypes = [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int), ctypes.c_int, _D, _D, _D,
+                                           _D, ctypes.c_int, _D, _D, _D, _D, _D]
         lib.oracle_rk4_step.restype = ctypes.c_int
         lib.oracle_rk4_step.argtypes = [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -172,6 +176,35 @@ def rk4_step(N, x, dt, agg=None, brk=None):
     if code:
         raise RuntimeError("oracle_rk4_step failed")
     return N
+
+
+def rk4_adjoint(N0, x, dt, n_steps, lamT, agg_sets=None, brk_sets=None, step_set=None,
+                t_q=None, bw_q=None):
+    """Serial discrete adjoint of n_steps RK4 steps. agg_sets: rows
+    (kernel, beta0, beta_br, beta_sh); brk_sets: rows (selection, S0, v_ref,
+    alpha, v_min); step_set: parameter-set index per step (default all 0).
+    Returns (N_T, dL/dN0, g_agg [sets, 3], g_brk [sets, 4]) for L with
+    dL/dN(T) = lamT."""
+    N0, x, lamT = _f64(N0), _f64(x), _f64(lamT)
+    n = len(x)
+    A = None if agg_sets is None else _f64(np.atleast_2d(agg_sets))
+    B = None if brk_sets is None else _f64(np.atleast_2d(brk_sets))
+    n_sets = (A if A is not None else B).shape[0]
+    ss = None
+    if step_set is not None:
+        ss = np.ascontiguousarray(step_set, dtype=np.int32)
+    tq = None if t_q is None else _f64(t_q)
+    bw = None if bw_q is None else _f64(bw_q)
+    NT, gN0 = np.zeros(n), np.zeros(n)
+    ga, gb = np.zeros((n_sets, 3)), np.zeros((n_sets, 4))
+    code = _lib().oracle_rk4_adjoint(
+        _dp(N0), _dp(x), n, float(dt), int(n_steps),
+        None if ss is None else ss.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n_sets,
+        _dp(A), _dp(B), _dp(tq), _dp(bw), 0 if tq is None else len(tq), _dp(lamT), _dp(NT),
+        _dp(gN0), _dp(ga), _dp(gb))
+    if code:
+        raise RuntimeError("oracle_rk4_adjoint failed")
+    return NT, gN0, ga, gb
 
 
 class RefRunner:

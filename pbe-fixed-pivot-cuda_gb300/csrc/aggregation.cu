@@ -37,84 +37,12 @@
 // chunk) and flush with FP64 atomicAdd.
 // =============================================================================
 #include "pbe_internal.cuh"
-#include "exact_weight.cuh"
+#include "agg_tile.cuh"
 
 namespace pbe_gb300 {
 namespace {
 
 constexpr int W = kTileW;
-
-template <int K> struct NeedH {
-    static constexpr bool j = (K == 1 || K == 2 || K == 4 || K == 5);
-    static constexpr bool k = (K == 1 || K == 2);
-};
-
-// Pair rate on a verified geometric grid, lag tables B = c_d * Bfactor(d),
-// S = c_d * Sfactor(d) with c_d = 1/2 for d = 0 (see agg_prep_kernel).
-template <int K>
-__device__ __forceinline__ double rate_geo(double B, double S, double Nj, double hj,
-                                           double Nk, double hk)
-{
-    if constexpr (K == 0 || K == 3) return (B * Nj) * Nk;
-    else if constexpr (K == 1) return B * fma(hj, Nk, Nj * hk);
-    else if constexpr (K == 2) return (B * hj) * hk;
-    else if constexpr (K == 4) return (S * hj) * Nk;
-    else return Nk * fma(S, hj, B * Nj);
-}
-
-// Lags whose pairs land on the larger member's own slot (lo = k): the rate is
-// F_k * q_slot(j) with the per-slot factor F_k = N_k (h_k for Product). Not
-// used for Sum, whose rate has two k-dependent terms.
-template <int K>
-__device__ __forceinline__ double q_slot(double B, double S, double Nj, double hj)
-{
-    if constexpr (K == 0 || K == 3) return B * Nj;
-    else if constexpr (K == 2) return B * hj;
-    else if constexpr (K == 4) return S * hj;
-    else return fma(S, hj, B * Nj);
-}
-
-// Pair rate on any grid from per-bin values (a = x^(1/3), ia = 1/a, h = x N):
-// beta of src/aggregation_kernels.cuh:56-89 with the divisions replaced by
-// products with the reciprocal cube roots.
-template <int K>
-__device__ __forceinline__ double rate_gen(bool diag, double b0, double bbr, double bsh,
-                                           double Nj, double hj, double aj, double iaj,
-                                           double Nk, double hk, double ak, double iak)
-{
-    double r;
-    if constexpr (K == 0) r = (b0 * Nj) * Nk;
-    else if constexpr (K == 1) r = b0 * fma(hj, Nk, Nj * hk);
-    else if constexpr (K == 2) r = (b0 * hj) * hk;
-    else {
-        double beta = 0.0;
-        if constexpr (K == 3 || K == 5) beta = bbr * (fma(aj, iak, ak * iaj) + 2.0);
-        if constexpr (K == 4 || K == 5) { const double s = aj + ak; beta = fma(bsh * s, s * s, beta); }
-        r = (beta * Nj) * Nk;
-    }
-    return diag ? 0.5 * r : r;
-}
-
-// sum_k beta(x_i, x_k) N_k from the moments
-// M[0] = sum N/a, M[1] = sum N, M[2] = sum a N, M[3] = sum a^2 N, M[4] = sum x N.
-template <int K>
-__device__ __forceinline__ double death_factor(double xi, double ai, double iai,
-                                               const double* M, double b0, double bbr,
-                                               double bsh)
-{
-    if constexpr (K == 0) return b0 * M[1];
-    else if constexpr (K == 1) return b0 * fma(xi, M[1], M[4]);
-    else if constexpr (K == 2) return (b0 * xi) * M[4];
-    else {
-        double f = 0.0;
-        // beta_br (a_i/a_k + a_k/a_i + 2)
-        if constexpr (K == 3 || K == 5) f = bbr * (fma(ai, M[0], iai * M[2]) + 2.0 * M[1]);
-        // beta_sh (a_i + a_k)^3 = beta_sh (x_i + 3 a_i^2 a_k + 3 a_i a_k^2 + x_k)
-        if constexpr (K == 4 || K == 5)
-            f = fma(bsh, fma(xi, M[1], (3.0 * ai) * fma(ai, M[2], M[3])) + M[4], f);
-        return f;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // prep: one thread per bin i. Per-bin values, the lag tables for d = i,
@@ -166,8 +94,7 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         ws.Ld[i] = L;
         if (L == i) d0 = i;
         if (n >= 2) {
-            const double lr = log(x[n - 1] / x0) / static_cast<double>(n - 1);
-            dev = fabs(log(xi / x0) - static_cast<double>(i) * lr);
+            dev = geo_dev(geo_fit(x0, x[n - 1], n), xi, i);
             if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
         }
     }
@@ -273,10 +200,12 @@ agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, doub
     }
 }
 
+
 // ---------------------------------------------------------------------------
 // main: persistent CTAs; each task owns the W bins [I, I+W) of one tile and
 // accumulates the slots s = I-1 .. I+W-1 (slot I-1 only feeds the w-part of
-// bin I). Thread-private partial sums are reduced in a fixed order.
+// bin I) with the whole CTA as one group (agg_tile.cuh). Thread-private
+// partial sums are reduced in a fixed order.
 // ---------------------------------------------------------------------------
 template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
@@ -285,16 +214,22 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 int ntasks, double b0, double bbr, double bsh)
 {
     extern __shared__ double red[];               // [kRedRows][kMainThreads]
-    __shared__ double xs[W + 2];                  // x[I-1 .. I+W]
-    __shared__ double fs[W + 2];                  // per-slot factor N (h for Product)
-    __shared__ double part4[4][kRedRows];
-    __shared__ double fin[kRedRows];
-    __shared__ double shw[kMainThreads / 32];
+    __shared__ TileShared sm;
     __shared__ int s_task;
 
     const int tid = threadIdx.x;
-    const bool geo = ws.mom[5] != 0.0;
-    const double M[5] = {ws.mom[0], ws.mom[1], ws.mom[2], ws.mom[3], ws.mom[4]};
+    AggCellView v;
+    v.x = x; v.Nk = N; v.Hk = ws.h; v.Nj = N; v.Hj = ws.h;
+    v.Fs = (K == 2) ? ws.h : N;
+    v.a = ws.a; v.ia = ws.ia; v.inv_dx = ws.inv_dx;
+    v.Bd = ws.Bd; v.Sd = ws.Sd; v.Ld = ws.Ld;
+    v.n = n;
+    v.D0 = ws.counter[1];
+    v.geo = ws.mom[5] != 0.0;
+    v.b0 = b0; v.bbr = bbr; v.bsh = bsh;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) v.M[q] = ws.mom[q];
+    const TileGroup G{0, tid, kMainThreads};
 
     for (;;) {
         if (tid == 0) s_task = atomicAdd(ws.counter, 1);
@@ -304,159 +239,21 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         if (task >= ntasks) break;
 
         int tile, chunk = 0;
-        if (SCATTER && geo) { tile = ntile - 1 - task / nchunk; chunk = task % nchunk; }
+        if (SCATTER && v.geo) { tile = ntile - 1 - task / nchunk; chunk = task % nchunk; }
         else { if (task >= ntile) continue; tile = ntile - 1 - task; }
 
         const int I = tile * W;
-        const int smax = min(I + W - 1, n - 2);     // highest non-clipped slot
-        const int d_begin = (SCATTER && geo) ? chunk * kScatterChunk : 0;
-        const int d_end = (SCATTER && geo) ? min(n, d_begin + kScatterChunk) : n;
+        const int smax = min(I + W - 1, n - 2);
+        const int d_begin = (SCATTER && v.geo) ? chunk * kScatterChunk : 0;
+        const int d_end = (SCATTER && v.geo) ? min(n, d_begin + kScatterChunk) : n;
         // skip empty lag chunks (uniform: every thread reads the same entry)
-        if (SCATTER && geo && chunk > 0 && (d_begin >= n || ws.Ld[d_begin] > smax)) continue;
+        if (SCATTER && v.geo && chunk > 0 && (d_begin >= n || ws.Ld[d_begin] > smax)) continue;
 
-        if (tid < W + 2) {
-            const int s = I - 1 + tid;
-            const bool in = (s >= 0 && s < n);
-            xs[tid] = in ? x[s] : 0.0;
-            fs[tid] = in ? (K == 2 ? ws.h[s] : N[s]) : 0.0;
-        }
         // Per-task exponent shift of the weight numerators: th ~ x_I (r-1) is
         // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
         // the reference's w*rate even on grids spanning hundreds of octaves.
         const int St = -ilogb(x[I]);
-        const int St20 = St << 20;
-        __syncthreads();
-
-        if (geo) {
-            double R[W + 1], TH[W + 1];
-#pragma unroll
-            for (int t = 0; t <= W; ++t) { R[t] = 0.0; TH[t] = 0.0; }
-            const int thi = smax - (I - 1);   // slot index t <= thi
-            // lags d >= D0 put every pair on its larger member's own slot (lo = k)
-            const int D0 = (K == 1) ? n : ws.counter[1];
-            int d = d_begin + tid;
-            // phase 1, lags with lo > k: rate per pair, R += rate, TH += rate * th
-            for (; d < d_end && d < D0; d += kMainThreads) {
-                const int L = __ldg(ws.Ld + d);
-                if (L > smax) { d = d_end; break; }   // Ld is nondecreasing in d
-                const double B = __ldg(ws.Bd + d), S = __ldg(ws.Sd + d);
-                const int jb = I - 1 - L;      // j of slot t is jb + t, k = jb + d + t
-                const int tlo = max(0, -jb);
-#pragma unroll
-                for (int t = 0; t <= W; ++t) {
-                    if (t >= tlo && t <= thi) {
-                        const int j = jb + t, k = j + d;
-                        const double Nj = __ldg(N + j), Nk = __ldg(N + k);
-                        const double hj = NeedH<K>::j ? __ldg(ws.h + j) : 0.0;
-                        const double hk = NeedH<K>::k ? __ldg(ws.h + k) : 0.0;
-                        const double rate = rate_geo<K>(B, S, Nj, hj, Nk, hk);
-                        // (fl(x_j + x_k) - x_lo) 2^St on the integer pipe, bit-identical
-                        // to the reference's two FP64 additions
-                        const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + j), xs[t], St);
-                        if (t > 0) R[t] += rate;
-                        TH[t] = fma(rate, th, TH[t]);
-                    }
-                }
-            }
-#pragma unroll
-            for (int t = 0; t <= W; ++t) {
-                red[t * kMainThreads + tid] = R[t];
-                red[(W + 1 + t) * kMainThreads + tid] = TH[t];
-                R[t] = 0.0;
-                TH[t] = 0.0;
-            }
-            // phase 2, lags with lo = k: k is the slot itself, so rate = F_slot * q(j)
-            // (F = N, or h for Product); sum q and q * th, multiply by F once
-            if constexpr (K != 1) {
-                for (; d < d_end; d += kMainThreads) {
-                    const int L = __ldg(ws.Ld + d);
-                    if (L > smax) break;
-                    const double B = __ldg(ws.Bd + d), S = __ldg(ws.Sd + d);
-                    const int jb = I - 1 - L;
-                    const int tlo = max(0, -jb);
-#pragma unroll
-                    for (int t = 0; t <= W; ++t) {
-                        if (t >= tlo && t <= thi) {
-                            const int j = jb + t;
-                            const double Nj = __ldg(N + j);
-                            const double hj = NeedH<K>::j ? __ldg(ws.h + j) : 0.0;
-                            const double q = q_slot<K>(B, S, Nj, hj);
-                            const double th = sum_minus_scaled(xs[t], __ldg(x + j), xs[t], St);
-                            if (t > 0) R[t] += q;
-                            TH[t] = fma(q, th, TH[t]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int t = 0; t <= W; ++t) {
-                    double* r0 = red + t * kMainThreads + tid;
-                    double* r1 = red + (W + 1 + t) * kMainThreads + tid;
-                    *r0 = fma(fs[t], R[t], *r0);
-                    *r1 = fma(fs[t], TH[t], *r1);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < kRedRows; ++r) red[r * kMainThreads + tid] = 0.0;
-            const int s_first = max(I - 1, 0);
-            if (smax >= s_first) {
-                const int t_first = s_first - (I - 1);
-                const int t_last = smax - (I - 1);
-                const long long blo = dbits(xs[t_first]);
-                const long long bhi = dbits(xs[t_last + 1]);
-                const double* __restrict__ xsc = x;
-                const double xlast = xsc[n - 1];
-                for (int j = tid; j <= smax; j += kMainThreads) {
-                    const double xj = xsc[j];
-                    if (dbits(xj + xj) >= bhi) break;          // v >= 2 x_j grows with j
-                    if (dbits(xj + xlast) < blo) continue;     // this row never reaches the tile
-                    int lo = j, hi = n - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (dbits(xj + xsc[mid]) >= blo) hi = mid; else lo = mid + 1;
-                    }
-                    const int ka = lo;
-                    hi = n;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (dbits(xj + xsc[mid]) >= bhi) hi = mid; else lo = mid + 1;
-                    }
-                    const int kb = lo;
-                    if (ka >= kb) continue;
-                    const double Nj = N[j], hj = ws.h[j], aj = ws.a[j], iaj = ws.ia[j];
-                    int t = t_first;
-                    double Rc = 0.0, THc = 0.0;
-                    for (int k = ka; k < kb; ++k) {
-                        const double v = xj + xsc[k];
-                        const long long vb = dbits(v);
-                        while (t < t_last && dbits(xs[t + 1]) <= vb) {
-                            red[t * kMainThreads + tid] += Rc;
-                            red[(W + 1 + t) * kMainThreads + tid] += THc;
-                            Rc = 0.0; THc = 0.0; ++t;
-                        }
-                        const double rate = rate_gen<K>(j == k, b0, bbr, bsh, Nj, hj, aj, iaj,
-                                                        N[k], ws.h[k], ws.a[k], ws.ia[k]);
-                        Rc += rate;
-                        THc = fma(rate, scale_pow2(v - xs[t], St20), THc);
-                    }
-                    red[t * kMainThreads + tid] += Rc;
-                    red[(W + 1 + t) * kMainThreads + tid] += THc;
-                }
-            }
-        }
-        __syncthreads();
-
-        // fixed-order reduction: 4 chunks of 64 columns per row, then the chunks
-        if (tid < kRedRows * 4) {
-            const int r = tid >> 2, c = tid & 3;
-            const double* p = red + r * kMainThreads + c * 64;
-            double s = 0.0;
-#pragma unroll 8
-            for (int q = 0; q < 64; ++q) s += p[q];
-            part4[c][r] = s;
-        }
-        __syncthreads();
-        if (tid < kRedRows) fin[tid] = (part4[0][tid] + part4[1][tid]) + (part4[2][tid] + part4[3][tid]);
+        agg_tile_accumulate<K>(v, I, d_begin, d_end, St, red, sm, G);
 
         // clipped pairs of bin n-1 (gather: sum of the clip kernel's partials)
         double clip = 0.0;
@@ -464,21 +261,15 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
             const int nbc = (n + kClipWarps - 1) / kClipWarps;
             double s = 0.0;
             for (int b = tid; b < nbc; b += kMainThreads) s += ws.clip_part[b];
-            clip = block_sum(s, shw);
+            clip = group_sum(s, sm, G);
         }
-        __syncthreads();
 
         if (tid < W) {
             const int i = I + tid;
             if (i < n) {
-                double birth = 0.0;
-                // TH is carried times 2^St: undo it on the (per-bin) inverse widths
-                if (i <= n - 2)
-                    birth = fma(-fin[W + 1 + tid + 1], scalbn(ws.inv_dx[i], -St), fin[tid + 1]);
-                if (i >= 1) birth = fma(fin[W + 1 + tid], scalbn(ws.inv_dx[i - 1], -St), birth);
-                const bool first = !(SCATTER && geo) || chunk == 0;
-                const double death = first ? N[i] * death_factor<K>(x[i], ws.a[i], ws.ia[i], M, b0, bbr, bsh)
-                                           : 0.0;
+                double birth = agg_tile_birth(v, I, tid, St, sm.fin[0]);
+                const bool first = !(SCATTER && v.geo) || chunk == 0;
+                const double death = first ? agg_death<K>(v, i) : 0.0;
                 if constexpr (SCATTER) {
                     const double val = birth - death;
                     if (val != 0.0) atomicAdd(rhs + i, val);

@@ -1,0 +1,626 @@
+// =============================================================================
+// batch.cu -- host side of the batched-cell path: plans, the task scheduler,
+// the tile-group autotuner, RK4 as one CUDA graph, the per-cell launch loop,
+// and the pbe_batch_* C ABI (include/pbe_gb300.h).
+//
+// Schedule. Every cell is cut into tiles of kTileW bins; a tile task costs
+// about min(I + W, n) lags. Cells are classed by floor(log2 n). Each class has a group
+// size T (threads per task): a bundle packs 256/T tasks of one class, so a
+// CTA of the persistent kernel runs up to eight small tiles at once. Bundles
+// are sorted by work (largest first) and pulled from an atomic counter.
+//
+// Autotuner. With PBE_BATCH_TUNE, each class present in the plan times the
+// persistent kernel on its own tasks for T = 32, 64, 128, 256 (synthetic
+// state; the work of a tile does not depend on the values) and keeps the
+// fastest. Results are cached per process and device (key: SM count, kernel
+// type, breakage on/off, class) and, when PBE_GB300_TUNE_CACHE names a file,
+// in that file (one "sms kernel brk class T" line per entry).
+//
+// RK4. A step is four (prep, main) launch pairs; the prep of a stage applies
+// the previous stage's update in place (batch_internal.cuh, BatchStage).
+// pbe_batch_rk4 captures n_steps steps plus the closing update into one CUDA
+// graph on a private stream and launches it on the caller's stream.
+// =============================================================================
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "batch_internal.cuh"
+
+struct pbe_batch_plan {
+    int device = 0;
+    int num_sms = 0;
+    int n_grids = 0, n_cells = 0, kernel = -1, selection = -1, nq = 0;
+    long long total = 0;
+    int max_n = 0;
+    std::vector<int> grid_n, grid_off, cell_n, cell_grid;
+    std::vector<long long> offsets;
+    pbe_gb300::BatchDev d{};
+    std::vector<void*> allocs;
+    int group_size[16] = {0};
+    int4* d_bundles = nullptr;
+    int2* d_tasks = nullptr;
+    std::vector<double> t_q, bw_q;
+    double* d_tq = nullptr;
+    double* d_bw = nullptr;
+    // per-cell launch loop scratch (allocated on first use)
+    void* cell_agg_ws = nullptr;
+    void* cell_brk_ws = nullptr;
+    // graph cache
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void* g_N = nullptr;
+    const void* g_params = nullptr;
+    double g_dt = 0.0;
+    int g_steps = 0;
+};
+
+namespace pbe_gb300 {
+namespace {
+
+constexpr int W = kTileW;
+constexpr int kClasses = 16;
+
+int n_class(int n)
+{
+    int c = 0;
+    while ((2 << c) <= n && c < kClasses - 1) ++c;
+    return c;
+}
+
+int rule_group_size(int cls)
+{
+    if (cls <= 7) return 32;      // n < 256
+    if (cls == 8) return 64;      // n < 512
+    if (cls == 9) return 128;     // n < 1024
+    return 256;
+}
+
+// ---- tune cache ----------------------------------------------------------------
+using TuneKey = std::tuple<int, int, int, int>;   // sms, kernel, brk, class
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+bool g_tune_file_read = false;
+
+const char* tune_file() { return std::getenv("PBE_GB300_TUNE_CACHE"); }
+
+void tune_cache_load_locked()
+{
+    if (g_tune_file_read) return;
+    g_tune_file_read = true;
+    const char* path = tune_file();
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    int a, b, c, e, t;
+    while (std::fscanf(f, "%d %d %d %d %d", &a, &b, &c, &e, &t) == 5)
+        if (t == 32 || t == 64 || t == 128 || t == 256) g_tune[TuneKey(a, b, c, e)] = t;
+    std::fclose(f);
+}
+
+void tune_cache_store_locked(const TuneKey& k, int t)
+{
+    g_tune[k] = t;
+    const char* path = tune_file();
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%d %d %d %d %d\n", std::get<0>(k), std::get<1>(k), std::get<2>(k),
+                 std::get<3>(k), t);
+    std::fclose(f);
+}
+
+// ---- schedule ------------------------------------------------------------------
+struct HostTask { int cell, I; long long cost; };
+
+long long task_cost(int n, int I, int T)
+{
+    const long long lags = std::min(I + W, n);
+    const long long it = (lags + T - 1) / T;
+    return it * T + 4LL * T;                          // + reduction / epilogue
+}
+
+// Bundles for the cells of the classes selected by `want` (all when null),
+// each class with its group size gs[class]; sorted by work, largest first.
+void build_schedule(const pbe_batch_plan& p, const int* gs, const bool* want,
+                    std::vector<int4>& bundles, std::vector<int2>& tasks)
+{
+    std::vector<std::vector<HostTask>> per(kClasses);
+    for (int c = 0; c < p.n_cells; ++c) {
+        const int n = p.cell_n[c];
+        const int cls = n_class(n);
+        if (want && !want[cls]) continue;
+        for (int I = 0; I < n; I += W) per[cls].push_back({c, I, task_cost(n, I, gs[cls])});
+    }
+    struct B { long long cost; int cls; int first; int cnt; };
+    std::vector<B> bl;
+    std::vector<std::vector<HostTask>> sorted(kClasses);
+    for (int cls = 0; cls < kClasses; ++cls) {
+        auto& v = per[cls];
+        if (v.empty()) continue;
+        std::stable_sort(v.begin(), v.end(),
+                         [](const HostTask& a, const HostTask& b) { return a.cost > b.cost; });
+        const int per_b = kMainThreads / gs[cls];
+        for (size_t i = 0; i < v.size(); i += per_b) {
+            const int cnt = static_cast<int>(std::min<size_t>(per_b, v.size() - i));
+            long long cost = 0;
+            for (int k = 0; k < cnt; ++k) cost += v[i + k].cost;
+            bl.push_back({cost, cls, static_cast<int>(i), cnt});
+        }
+        sorted[cls] = v;
+    }
+    std::stable_sort(bl.begin(), bl.end(), [](const B& a, const B& b) { return a.cost > b.cost; });
+    bundles.clear();
+    tasks.clear();
+    for (const B& b : bl) {
+        bundles.push_back(make_int4(static_cast<int>(tasks.size()), b.cnt, gs[b.cls], 0));
+        for (int k = 0; k < b.cnt; ++k) {
+            const HostTask& t = sorted[b.cls][b.first + k];
+            tasks.push_back(make_int2(t.cell, t.I));
+        }
+    }
+}
+
+template <class T>
+cudaError_t plan_alloc(pbe_batch_plan* p, T** out, size_t count)
+{
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    p->allocs.push_back(q);
+    *out = static_cast<T*>(q);
+    return cudaSuccess;
+}
+
+cudaError_t upload_schedule(pbe_batch_plan* p, const std::vector<int4>& b,
+                            const std::vector<int2>& t, int4** db, int2** dt, cudaStream_t s)
+{
+    cudaError_t e = plan_alloc(p, db, b.size());
+    if (e == cudaSuccess) e = plan_alloc(p, dt, t.size());
+    if (e == cudaSuccess && !b.empty())
+        e = cudaMemcpyAsync(*db, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !t.empty())
+        e = cudaMemcpyAsync(*dt, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
+void free_last(pbe_batch_plan* p, int count)
+{
+    for (int i = 0; i < count && !p->allocs.empty(); ++i) {
+        cudaFree(p->allocs.back());
+        p->allocs.pop_back();
+    }
+}
+
+// Times the persistent kernel on the tasks of one class for each group size.
+cudaError_t tune_class(pbe_batch_plan* p, int cls, const pbe_batch_cell_params_t* dparams,
+                       double* dN, double* dout, cudaStream_t s, int* best_T)
+{
+    static const int cand[4] = {32, 64, 128, 256};
+    bool want[kClasses] = {false};
+    want[cls] = true;
+    float best = 0.0f;
+    *best_T = rule_group_size(cls);
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) { cudaEventDestroy(e0); return e; }
+    for (int ci = 0; ci < 4 && e == cudaSuccess; ++ci) {
+        int gs[kClasses];
+        for (int c = 0; c < kClasses; ++c) gs[c] = cand[ci];
+        std::vector<int4> b;
+        std::vector<int2> t;
+        build_schedule(*p, gs, want, b, t);
+        int4* db = nullptr;
+        int2* dt = nullptr;
+        e = upload_schedule(p, b, t, &db, &dt, s);
+        if (e != cudaSuccess) break;
+        const int nb = static_cast<int>(b.size());
+        e = batch_main_bundles(p->d, dN, dparams, dout, false, db, dt, nb, s);   // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+            e = batch_main_bundles(p->d, dN, dparams, dout, false, db, dt, nb, s);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        free_last(p, 2);
+        if (e == cudaSuccess && (ci == 0 || ms < best)) { best = ms; *best_T = cand[ci]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return e;
+}
+
+cudaError_t autotune(pbe_batch_plan* p, bool retune, cudaStream_t s)
+{
+    bool present[kClasses] = {false};
+    for (int c = 0; c < p->n_cells; ++c) present[n_class(p->cell_n[c])] = true;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_cache_load_locked();
+    // synthetic state and coefficients (any finite values: the work is value-independent)
+    double* dN = nullptr;
+    double* dout = nullptr;
+    pbe_batch_cell_params_t* dparams = nullptr;
+    const size_t np = static_cast<size_t>(p->total);
+    cudaError_t e = plan_alloc(p, &dN, np);
+    if (e == cudaSuccess) e = plan_alloc(p, &dout, np);
+    if (e == cudaSuccess) e = plan_alloc(p, &dparams, static_cast<size_t>(p->n_cells));
+    if (e != cudaSuccess) return e;
+    {
+        std::vector<double> ones(np, 1.0);
+        std::vector<pbe_batch_cell_params_t> prm(static_cast<size_t>(p->n_cells));
+        for (auto& q : prm) q = pbe_batch_cell_params_t{1e-15, 1e-17, 1.0, 1e-3, 1.0, 1.0, 0.0, 0.0};
+        e = cudaMemcpyAsync(dN, ones.data(), np * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dparams, prm.data(), prm.size() * sizeof(pbe_batch_cell_params_t),
+                                cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = batch_prep(p->d, dN, dparams, kStageRhs, 0.0, 0.0, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
+        if (!present[cls]) continue;
+        const TuneKey key(p->num_sms, p->kernel, p->nq > 0 ? 1 : 0, cls);
+        auto it = g_tune.find(key);
+        if (!retune && it != g_tune.end()) { p->group_size[cls] = it->second; continue; }
+        int T = rule_group_size(cls);
+        e = tune_class(p, cls, dparams, dN, dout, s, &T);
+        if (e == cudaSuccess) {
+            p->group_size[cls] = T;
+            tune_cache_store_locked(key, T);
+        }
+    }
+    free_last(p, 3);
+    return e;
+}
+
+cudaError_t validate(int n_grids, const int* grid_n, const double* grid_x, int n_cells,
+                     const int* cell_n, const int* cell_grid, int kernel, int selection,
+                     int n_quad, const double* t_q, const double* bw_q)
+{
+    if (n_grids <= 0 || n_cells <= 0 || !grid_n || !grid_x || !cell_n || !cell_grid)
+        return cudaErrorInvalidValue;
+    if (kernel < -1 || kernel > 5 || selection < -1 || selection > 3) return cudaErrorInvalidValue;
+    if (kernel < 0 && selection < 0) return cudaErrorInvalidValue;
+    if (selection >= 0 && (n_quad <= 0 || !t_q || !bw_q)) return cudaErrorInvalidValue;
+    if (selection < 0 && n_quad != 0) return cudaErrorInvalidValue;
+    long long gtot = 0;
+    for (int g = 0; g < n_grids; ++g) {
+        if (grid_n[g] <= 0) return cudaErrorInvalidValue;
+        const double* x = grid_x + gtot;
+        for (int i = 0; i < grid_n[g]; ++i) {
+            if (!(x[i] > 0.0) || !std::isfinite(x[i]) || !std::isnormal(x[i]))
+                return cudaErrorInvalidValue;
+            if (i > 0 && !(x[i] > x[i - 1])) return cudaErrorInvalidValue;
+        }
+        gtot += grid_n[g];
+        // packed grid tables (n_quad (n + 2) run starts per grid) are int-indexed
+        if ((gtot + 2LL * (g + 1)) * std::max(n_quad, 1) > 0x7fffffffLL) return cudaErrorInvalidValue;
+    }
+    long long ctot = 0;
+    for (int c = 0; c < n_cells; ++c) {
+        if (cell_grid[c] < 0 || cell_grid[c] >= n_grids) return cudaErrorInvalidValue;
+        if (cell_n[c] <= 0 || cell_n[c] > grid_n[cell_grid[c]]) return cudaErrorInvalidValue;
+        ctot += cell_n[c];
+    }
+    if (ctot > 0x7fffffffLL) return cudaErrorInvalidValue;
+    for (int q = 0; q < n_quad; ++q)
+        if (!(t_q[q] > 0.0 && t_q[q] <= 1.0) || !std::isfinite(bw_q[q])) return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
+cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const double* grid_x,
+                   int n_cells, const int* cell_n, const int* cell_grid, int kernel,
+                   int selection, int n_quad, const double* t_q, const double* bw_q, int flags,
+                   cudaStream_t s)
+{
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+    if (e != cudaSuccess) return e;
+    p->n_grids = n_grids; p->n_cells = n_cells; p->kernel = kernel; p->selection = selection;
+    p->nq = selection >= 0 ? n_quad : 0;
+    p->grid_n.assign(grid_n, grid_n + n_grids);
+    p->cell_n.assign(cell_n, cell_n + n_cells);
+    p->cell_grid.assign(cell_grid, cell_grid + n_cells);
+    std::vector<BatchGridDev> hg(static_cast<size_t>(n_grids));
+    int goff = 0, foff = 0, woff = 0;
+    p->grid_off.resize(static_cast<size_t>(n_grids));
+    for (int g = 0; g < n_grids; ++g) {
+        hg[g] = BatchGridDev{goff, grid_n[g], 0, 0, foff, woff, 0, 0};
+        p->grid_off[g] = goff;
+        goff += grid_n[g];
+        foff += p->nq * (grid_n[g] + 2);
+        woff += p->nq * grid_n[g];
+    }
+    std::vector<BatchCellDev> hc(static_cast<size_t>(n_cells));
+    p->offsets.resize(static_cast<size_t>(n_cells) + 1);
+    long long off = 0;
+    for (int c = 0; c < n_cells; ++c) {
+        hc[c] = BatchCellDev{static_cast<int>(off), cell_n[c], cell_grid[c], 0};
+        p->offsets[c] = off;
+        off += cell_n[c];
+        p->max_n = std::max(p->max_n, cell_n[c]);
+    }
+    p->offsets[n_cells] = off;
+    p->total = off;
+
+    BatchDev& d = p->d;
+    d.n_grids = n_grids; d.n_cells = n_cells; d.kernel = kernel; d.selection = selection;
+    d.nq = p->nq; d.num_sms = p->num_sms;
+    const size_t G = static_cast<size_t>(goff), C = static_cast<size_t>(off);
+    BatchCellDev* dcells = nullptr;
+    e = plan_alloc(p, &d.grids, static_cast<size_t>(n_grids));
+    if (e == cudaSuccess) e = plan_alloc(p, &dcells, static_cast<size_t>(n_cells));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gx, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.ga, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gia, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.ginv_dx, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gBd, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gSd, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gLd, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.bfirst, static_cast<size_t>(foff));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.bwlo, static_cast<size_t>(woff));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.bwhi, static_cast<size_t>(woff));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.Y, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.Nj, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.Hj, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.Hk, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.SN, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.Bk, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.k, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.kacc, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.mom, static_cast<size_t>(n_cells) * 8);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.counter, 8);
+    if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_tq, static_cast<size_t>(p->nq));
+    if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_bw, static_cast<size_t>(p->nq));
+    if (e != cudaSuccess) return e;
+    d.cells = dcells;
+    // zero the stage arrays once: entries a kernel type never writes stay
+    // finite for the loads that the tile body issues unconditionally
+    for (double* a : {d.Y, d.Nj, d.Hj, d.Hk, d.SN, d.Bk, d.k, d.kacc})
+        if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, C * sizeof(double), s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d.grids, hg.data(), hg.size() * sizeof(BatchGridDev),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dcells, hc.data(), hc.size() * sizeof(BatchCellDev),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d.gx, grid_x, G * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (p->nq > 0) {
+        p->t_q.assign(t_q, t_q + p->nq);
+        p->bw_q.assign(bw_q, bw_q + p->nq);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->d_tq, t_q, p->nq * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->d_bw, bw_q, p->nq * sizeof(double), cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = batch_kernel_setup(kernel);
+    if (e == cudaSuccess) e = batch_grid_tables(d, p->d_tq, p->d_bw, 0, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+
+    for (int cls = 0; cls < kClasses; ++cls) p->group_size[cls] = rule_group_size(cls);
+    if (flags & (PBE_BATCH_TUNE | PBE_BATCH_RETUNE)) {
+        e = autotune(p, (flags & PBE_BATCH_RETUNE) != 0, s);
+        if (e != cudaSuccess) return e;
+    }
+    std::vector<int4> b;
+    std::vector<int2> t;
+    build_schedule(*p, p->group_size, nullptr, b, t);
+    e = upload_schedule(p, b, t, &p->d_bundles, &p->d_tasks, s);
+    if (e != cudaSuccess) return e;
+    d.bundles = p->d_bundles;
+    d.tasks = p->d_tasks;
+    d.n_bundles = static_cast<int>(b.size());
+    return cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+}
+
+void destroy(pbe_batch_plan* p)
+{
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    for (void* q : p->allocs) cudaFree(q);
+    delete p;
+}
+
+cudaError_t check_plan(pbe_batch_plan* p)
+{
+    if (!p) return cudaErrorInvalidValue;
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    return dev == p->device ? cudaSuccess : cudaErrorInvalidDevice;
+}
+
+// One RK4 step sequence (or a plain RHS) enqueued on s.
+cudaError_t enqueue_rk4(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
+                        double dt, int n_steps, cudaStream_t s)
+{
+    const BatchDev& d = p->d;
+    const double h = 0.5 * dt, dt6 = dt / 6.0;
+    cudaError_t e = cudaSuccess;
+    for (int step = 0; step < n_steps && e == cudaSuccess; ++step) {
+        e = batch_prep(d, N, prm, step == 0 ? kStageRhs : kStageNext, 0.0, dt6, s);
+        if (e == cudaSuccess) e = batch_main(d, N, prm, d.k, false, s);
+        if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageTwo, h, dt6, s);
+        if (e == cudaSuccess) e = batch_main(d, d.Y, prm, d.k, false, s);
+        if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageThree, h, dt6, s);
+        if (e == cudaSuccess) e = batch_main(d, d.Y, prm, d.k, false, s);
+        if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageThree, dt, dt6, s);
+        if (e == cudaSuccess) e = batch_main(d, d.Y, prm, d.k, false, s);
+    }
+    if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageFinish, 0.0, dt6, s);
+    return e;
+}
+
+cudaError_t rk4_graph(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
+                      int n_steps, cudaStream_t s)
+{
+    if (!p->exec || p->g_N != N || p->g_params != prm || p->g_dt != dt || p->g_steps != n_steps) {
+        if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t le = enqueue_rk4(p, N, prm, dt, n_steps, p->cap);
+        e = cudaStreamEndCapture(p->cap, &graph);
+        if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return le; }
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&p->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { p->exec = nullptr; return e; }
+        p->g_N = N; p->g_params = prm; p->g_dt = dt; p->g_steps = n_steps;
+    }
+    cudaError_t e = cudaGraphLaunch(p->exec, s);
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t rk4_percell(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
+                        double dt, int n_steps, cudaStream_t s)
+{
+    const BatchDev& d = p->d;
+    if (!p->cell_agg_ws && p->kernel >= 0) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, agg_ws_layout(p->max_n, nullptr, nullptr));
+        if (e != cudaSuccess) return e;
+        p->allocs.push_back(q);
+        p->cell_agg_ws = q;
+    }
+    if (!p->cell_brk_ws && p->nq > 0) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, brk_ws_layout(p->max_n, p->nq, nullptr, nullptr));
+        if (e != cudaSuccess) return e;
+        p->allocs.push_back(q);
+        p->cell_brk_ws = q;
+    }
+    // the single-instance calls take their coefficients by value
+    std::vector<pbe_batch_cell_params_t> hp(static_cast<size_t>(p->n_cells));
+    cudaError_t e = cudaMemcpyAsync(hp.data(), prm, hp.size() * sizeof(pbe_batch_cell_params_t),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const double h = 0.5 * dt, dt6 = dt / 6.0;
+    static const int kStages[4] = {kStageTwo, kStageThree, kStageThree, kStageFinish};
+    const double cs[4] = {h, h, dt, 0.0};
+    for (int step = 0; step < n_steps && e == cudaSuccess; ++step) {
+        for (int c = 0; c < p->n_cells && e == cudaSuccess; ++c) {
+            const int n = p->cell_n[c];
+            const long long off = p->offsets[c];
+            const double* x = d.gx + p->grid_off[p->cell_grid[c]];
+            double* Nc = N + off;
+            double* kc = d.k + off;
+            double* ac = d.kacc + off;
+            double* Yc = d.Y + off;
+            const pbe_batch_cell_params_t& P = hp[c];
+            for (int st = 0; st < 4 && e == cudaSuccess; ++st) {
+                const double* in = (st == 0) ? Nc : Yc;
+                e = cudaMemsetAsync(kc, 0, static_cast<size_t>(n) * sizeof(double), s);
+                if (e == cudaSuccess && p->kernel >= 0) {
+                    AggArgs a{in, x, kc, n, p->kernel, P.beta0, P.beta_br, P.beta_sh};
+                    e = agg_launch(a, false, p->cell_agg_ws, p->num_sms, s);
+                }
+                if (e == cudaSuccess && p->nq > 0) {
+                    BrkArgs b{in, x, p->d_tq, p->d_bw, kc, n, p->nq, p->selection,
+                              P.S0, P.v_ref, P.alpha, P.v_min};
+                    e = brk_launch(b, false, p->cell_brk_ws, s);
+                }
+                if (e == cudaSuccess) e = cell_stage(Nc, kc, ac, Yc, n, kStages[st], cs[st], dt6, s);
+            }
+        }
+    }
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+} // namespace
+} // namespace pbe_gb300
+
+using namespace pbe_gb300;
+
+extern "C" {
+
+int pbe_batch_create(pbe_batch_t* plan, int n_grids, const int* grid_n, const double* grid_x,
+                     int n_cells, const int* cell_n, const int* cell_grid, int kernel_type,
+                     int selection, int n_quad, const double* t_q, const double* bw_q,
+                     int flags, void* stream)
+{
+    if (!plan) return cudaErrorInvalidValue;
+    *plan = nullptr;
+    cudaError_t e = validate(n_grids, grid_n, grid_x, n_cells, cell_n, cell_grid, kernel_type,
+                             selection, n_quad, t_q, bw_q);
+    if (e != cudaSuccess) return e;
+    pbe_batch_plan* p = new (std::nothrow) pbe_batch_plan();
+    if (!p) return cudaErrorMemoryAllocation;
+    e = create(p, n_grids, grid_n, grid_x, n_cells, cell_n, cell_grid, kernel_type, selection,
+               n_quad, t_q, bw_q, flags, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) { destroy(p); return e; }
+    *plan = p;
+    return cudaSuccess;
+}
+
+int pbe_batch_destroy(pbe_batch_t plan)
+{
+    if (plan) destroy(plan);
+    return cudaSuccess;
+}
+
+int pbe_batch_offsets(pbe_batch_t plan, long long* offsets)
+{
+    if (!plan || !offsets) return cudaErrorInvalidValue;
+    std::memcpy(offsets, plan->offsets.data(), plan->offsets.size() * sizeof(long long));
+    return cudaSuccess;
+}
+
+int pbe_batch_rhs(pbe_batch_t plan, const double* N, double* rhs,
+                  const pbe_batch_cell_params_t* params, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !rhs || !params) return cudaErrorInvalidDevicePointer;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    e = batch_prep(plan->d, const_cast<double*>(N), params, kStageRhs, 0.0, 0.0, s);
+    if (e == cudaSuccess) e = batch_main(plan->d, N, params, rhs, true, s);
+    return e;
+}
+
+int pbe_batch_rk4(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,
+                  int n_steps, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (n_steps < 0 || !std::isfinite(dt)) return cudaErrorInvalidValue;
+    if (n_steps == 0) return cudaSuccess;
+    return rk4_graph(plan, N, params, dt, n_steps, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_rk4_percell(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                          double dt, int n_steps, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (n_steps < 0 || !std::isfinite(dt)) return cudaErrorInvalidValue;
+    return rk4_percell(plan, N, params, dt, n_steps, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)
+{
+    if (!plan) return cudaErrorInvalidValue;
+    if (group_size) {
+        bool present[16] = {false};
+        for (int c = 0; c < plan->n_cells; ++c) present[n_class(plan->cell_n[c])] = true;
+        for (int c = 0; c < 16; ++c) group_size[c] = present[c] ? plan->group_size[c] : 0;
+    }
+    if (n_bundles) *n_bundles = plan->d.n_bundles;
+    return cudaSuccess;
+}
+
+} // extern "C"

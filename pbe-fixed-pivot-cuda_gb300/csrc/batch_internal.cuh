@@ -1,0 +1,101 @@
+// =============================================================================
+// batch_internal.cuh -- device layouts and launchers of the batched-cell path
+// (many independent PBE cells with uneven section counts in one launch).
+//
+// Cells reference grids. Every cell c uses the first n_c pivots of its grid
+// g(c) (n_c <= n_g), so cells that share a grid also share the grid's per-bin
+// values, per-lag tables and breakage fragment tables, which are built once
+// per plan. Cell state is packed: cell c owns [off_c, off_c + n_c) of every
+// per-bin array (N, rhs and the stage arrays), off = prefix sum of n in cell
+// order.
+// =============================================================================
+#pragma once
+
+#include "pbe_internal.cuh"
+#include "pbe_gb300.h"
+
+namespace pbe_gb300 {
+
+struct BatchGridDev {
+    int off;     // first bin in the packed grid arrays
+    int n;       // pivots
+    int D0;      // first lag with Ld[d] == d (written by the grid kernel)
+    int geo;     // 1 when verified geometric (written by the grid kernel)
+    int foff;    // first entry of the grid's run-start table (nq * (n + 2) ints)
+    int woff;    // first entry of the grid's fragment weights (nq * n doubles)
+    int pad0, pad1;
+};
+
+struct BatchCellDev {
+    int off;     // first bin in the packed cell arrays
+    int n;       // sections of the cell (<= its grid's n)
+    int grid;
+    int pad;
+};
+
+// Device pointers of a plan: grid tables (static) and per-stage cell arrays.
+struct BatchDev {
+    BatchGridDev* grids;
+    const BatchCellDev* cells;
+    int n_grids, n_cells;
+    int kernel;        // aggregation kernel type, -1 = no aggregation
+    int selection;     // breakage selection, -1 = no breakage
+    int nq;            // quadrature points (0 = no breakage)
+    // per grid bin (packed by BatchGridDev::off)
+    double* gx; double* ga; double* gia; double* ginv_dx; double* gBd; double* gSd; int* gLd;
+    // breakage fragment tables: bfirst[foff + q (n+2) + m + 1] = first j with
+    // lo(q, j) >= m; bwlo / bwhi[woff + q n + j] = bw_q times the shares of the
+    // fragment x_j t_q at lo and lo + 1 (all of bw_q at lo when clipped)
+    int* bfirst; double* bwlo; double* bwhi;
+    // per cell bin (packed by BatchCellDev::off), rewritten every stage
+    double* Y;      // stage state (the RHS argument)
+    double* Nj;     // j-side N factor: beta N (beta0, beta_br)
+    double* Hj;     // j-side x N factor: beta x N (beta0, beta_sh)
+    double* Hk;     // x N (Sum, Product)
+    double* SN;     // S(x) N, 0 where the breakage guard skips the bin
+    double* Bk;     // breakage term of the stage (gathered by the prep kernel)
+    double* k;      // stage derivative (RK4)
+    double* kacc;   // k1 + 2 k2 + 2 k3 (+ k4)
+    double* mom;    // [n_cells * 8] moments of the stage state (death term), [5] clip sum
+    int* counter;   // [8] task counter of the persistent kernel
+    // schedule
+    const int4* bundles;   // {first task, tasks, group size, 0}
+    const int2* tasks;     // {cell, first bin}
+    int n_bundles;
+    int num_sms;
+};
+
+// Stage modes of the per-cell prep kernel (RK4 as the reference examples
+// write it, examples/common/pbe_examples_utils.hpp:409-456):
+enum BatchStage : int {
+    kStageRhs     = 0,  // Y = N as given (RHS evaluation, RK4 stage 1 of the first step)
+    kStageNext    = 1,  // kacc += k4; N += dt/6 kacc; Y = N (stage 1 of a later step)
+    kStageTwo     = 2,  // kacc = k1; Y = N + c k1
+    kStageThree   = 3,  // kacc += 2 k; Y = N + c k (stages 3 and 4)
+    kStageFinish  = 4,  // kacc += k4; N += dt/6 kacc (no RHS follows)
+};
+
+// Launchers (batch_kernels.cu). All are asynchronous on `s`.
+// Once per plan, before any launch (and outside stream capture): the
+// persistent kernel's shared-memory attribute for `kernel`.
+cudaError_t batch_kernel_setup(int kernel);
+cudaError_t batch_grid_tables(const BatchDev& d, const double* t_q, const double* bw_q,
+                              int max_grid_n, cudaStream_t s);
+// Prep of a stage: state update per `stage`, stage arrays, moments, counter reset.
+// N: state (read, and written by kStageNext / kStageFinish); Yrhs: the state
+// the RHS is evaluated at (N itself for kStageRhs / kStageNext).
+cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
+                       int stage, double c, double dt6, cudaStream_t s);
+// Persistent RHS kernel over the plan's bundles: out (+)= RHS(Y) for every cell.
+cudaError_t batch_main(const BatchDev& d, const double* Y, const pbe_batch_cell_params_t* params,
+                       double* out, bool accumulate, cudaStream_t s);
+// Same over an explicit bundle list (the autotuner's candidate schedules).
+cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
+                               const pbe_batch_cell_params_t* params, double* out,
+                               bool accumulate, const int4* bundles, const int2* tasks,
+                               int n_bundles, cudaStream_t s);
+// Per-cell RK4 stage update for the per-cell launch loop (one cell, n bins).
+cudaError_t cell_stage(double* N, const double* k, double* kacc, double* Y, int n, int stage,
+                       double c, double dt6, cudaStream_t s);
+
+} // namespace pbe_gb300

@@ -38,6 +38,48 @@ constexpr double kBreakageNMin = 2.2e-308;
 
 __device__ __forceinline__ long long dbits(double v) { return __double_as_longlong(v); }
 
+// Geometric-progression fit through x_0 and x_{n-1}, for the deviation test
+// |ln(x_i/x_0) - i ln r| <= kGeoTol. Computed in log2 with the binary
+// exponents split off exactly (x = 2^E m, m in [1, 2)) and the step
+// log2(x_{n-1}/x_0)/(n-1) carried as a double-double, so the test resolves
+// ~1e-15 whatever the grid spans (a plain log(x_i/x_0) - i*lr already rounds
+// by more than kGeoTol once ln(x_i/x_0) passes ~450).
+struct GeoFit {
+    int E0;          // exponent of x_0
+    double f0;       // log2 of the mantissa of x_0
+    double s_hi;     // step, high part
+    double s_lo;     // step, low part
+};
+
+__device__ __forceinline__ GeoFit geo_fit(double x0, double xl, int n)
+{
+    GeoFit g;
+    g.E0 = ilogb(x0);
+    g.f0 = log2(scalbn(x0, -g.E0));
+    const int El = ilogb(xl);
+    const double fl = log2(scalbn(xl, -El));
+    const double m = static_cast<double>(n > 1 ? n - 1 : 1);
+    const double L_hi = static_cast<double>(El) - static_cast<double>(g.E0);   // exact
+    const double L_lo = fl - g.f0;
+    g.s_hi = L_hi / m;
+    const double r = fma(-g.s_hi, m, L_hi);                // exact remainder
+    g.s_lo = (r + L_lo) / m;
+    return g;
+}
+
+// |ln(x_i / x_0) - i ln r| for the fitted r (natural-log units).
+__device__ __forceinline__ double geo_dev(const GeoFit& g, double xi, int i)
+{
+    const int Ei = ilogb(xi);
+    const double fi = log2(scalbn(xi, -Ei));
+    const double di = static_cast<double>(i);
+    const double p_hi = di * g.s_hi;
+    const double p_lo = fma(di, g.s_hi, -p_hi) + di * g.s_lo;
+    const double dev2 = ((static_cast<double>(Ei) - static_cast<double>(g.E0)) - p_hi)
+                      + ((fi - g.f0) - p_lo);
+    return fabs(dev2) * 0.6931471805599453;
+}
+
 // v * 2^s for a normal (or zero) double, by adding s to the exponent field:
 // three integer instructions instead of an FP64 multiply. s20 = s << 20.
 // Zero stays zero; callers keep |v| 2^s inside the normal range.

@@ -79,8 +79,7 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
         const double v = x0 + xi;
         ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
         if (n >= 2) {
-            const double lr = log(x[n - 1] / x0) / static_cast<double>(n - 1);
-            dev = fabs(log(xi / x0) - static_cast<double>(i) * lr);
+            dev = geo_dev(geo_fit(x0, x[n - 1], n), xi, i);
             if (!(dev == dev)) dev = 1.0;
         }
     }

@@ -22,7 +22,10 @@ from ._lib import (  # noqa: F401
     SEL_LINEAR,
     SEL_POWERLAW,
     SEL_THRESHOLD,
+    BATCH_RETUNE,
+    BATCH_TUNE,
     AggregationParams,
+    BatchCellParams,
     BreakageParams,
     PbeError,
     check,
@@ -37,6 +40,8 @@ from .rhs import (  # noqa: F401
     breakage_rhs_vjp,
     breakage_workspace_bytes,
 )
+from .adjoint import Rk4Tape  # noqa: F401
+from .batch import BatchPlan  # noqa: F401
 from . import grids, quadrature  # noqa: F401
 
 __version__ = "0.1.0"

@@ -71,7 +71,17 @@ class BreakageParams(ctypes.Structure):
         super().__init__(**defaults)
 
 
+class BatchCellParams(ctypes.Structure):
+    """Layout of pbe_batch_cell_params_t (one per cell of a batch plan)."""
+
+    _fields_ = [(name, ctypes.c_double) for name in
+                ("beta0", "beta_br", "beta_sh", "S0", "v_ref", "alpha", "v_min", "reserved")]
+
+
+BATCH_TUNE, BATCH_RETUNE = 1, 2
+
 _P = ctypes.c_void_p
+_I = ctypes.c_int
 _SIGNATURES = {
     "pbe_aggregation_rhs": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(AggregationParams), _P]),
     "pbe_breakage_rhs": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(BreakageParams), _P]),
@@ -89,6 +99,17 @@ _SIGNATURES = {
                                                _P, ctypes.c_size_t, _P]),
     "pbe_breakage_rhs_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(BreakageParams),
                                             _P, ctypes.c_size_t, _P]),
+    "pbe_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _P, _I, _P, _P, _I, _I, _I, _P, _P, _I, _P]),
+    "pbe_batch_destroy": (_I, [_P]),
+    "pbe_batch_offsets": (_I, [_P, _P]),
+    "pbe_batch_rhs": (_I, [_P, _P, _P, _P, _P]),
+    "pbe_batch_rk4": (_I, [_P, _P, _P, ctypes.c_double, _I, _P]),
+    "pbe_batch_rk4_percell": (_I, [_P, _P, _P, ctypes.c_double, _I, _P]),
+    "pbe_batch_schedule": (_I, [_P, _P, _P]),
+    "pbe_rk4_tape_create": (_I, [ctypes.POINTER(_P), _I, ctypes.c_double, _I, _I, _P, _P, _P]),
+    "pbe_rk4_tape_destroy": (_I, [_P]),
+    "pbe_rk4_tape_forward": (_I, [_P, _P, _P, _P, _P, _P]),
+    "pbe_rk4_tape_backward": (_I, [_P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -1,0 +1,122 @@
+"""Batched cells: many independent PBE instances with uneven section counts,
+evaluated by one persistent launch per RHS and integrated with RK4 steps
+captured in one CUDA graph (C ABI pbe_batch_*, include/pbe_gb300.h).
+
+The reference has no batched interface: its callers loop over cells and call
+launch_aggregation_rhs / launch_breakage_rhs per cell and per RK4 stage, with
+host round trips between stages (examples/common/pbe_examples_utils.hpp:409-456).
+`BatchPlan.rk4_percell` runs that per-cell launch loop (without the host round
+trips) on the single-instance kernels, as a baseline and a cross-check.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import BATCH_RETUNE, BATCH_TUNE, PbeError
+from .rhs import _ptr, _stream
+
+PARAM_FIELDS = ("beta0", "beta_br", "beta_sh", "S0", "v_ref", "alpha", "v_min", "reserved")
+
+
+def cell_params(n_cells: int, **values) -> np.ndarray:
+    """Host array [n_cells, 8] of pbe_batch_cell_params_t rows. Each keyword
+    (beta0, beta_br, beta_sh, S0, v_ref, alpha, v_min) is a scalar or an array
+    of n_cells; unspecified fields take the reference's struct defaults
+    (beta0 = S0 = v_ref = alpha = 1, the others 0)."""
+    defaults = dict(beta0=1.0, beta_br=0.0, beta_sh=0.0, S0=1.0, v_ref=1.0, alpha=1.0, v_min=0.0)
+    unknown = set(values) - set(defaults)
+    if unknown:
+        raise TypeError("unknown cell parameters: %s" % sorted(unknown))
+    defaults.update(values)
+    out = np.zeros((n_cells, 8))
+    for i, name in enumerate(PARAM_FIELDS[:7]):
+        out[:, i] = np.broadcast_to(np.asarray(defaults[name], dtype=np.float64), (n_cells,))
+    return out
+
+
+class BatchPlan:
+    """A plan over `cell_n` cells; cell c uses the first cell_n[c] pivots of
+    grids[cell_grid[c]]. kernel: AGG_* or -1 (no aggregation); selection:
+    SEL_* or -1 (no breakage) with the daughter table (t_q, bw_q)."""
+
+    def __init__(self, grids: Sequence[np.ndarray], cell_n: Sequence[int],
+                 cell_grid: Sequence[int], kernel: int, selection: int = -1,
+                 t_q: Optional[np.ndarray] = None, bw_q: Optional[np.ndarray] = None,
+                 tune: bool = False, retune: bool = False, stream=None):
+        lib = _lib.load()
+        grid_n = np.ascontiguousarray([len(g) for g in grids], dtype=np.int32)
+        grid_x = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float64) for g in grids]))
+        cn = np.ascontiguousarray(cell_n, dtype=np.int32)
+        cg = np.ascontiguousarray(cell_grid, dtype=np.int32)
+        nq = 0
+        tq = bw = None
+        if selection >= 0:
+            tq = np.ascontiguousarray(t_q, dtype=np.float64)
+            bw = np.ascontiguousarray(bw_q, dtype=np.float64)
+            nq = len(tq)
+        flags = (BATCH_TUNE if tune else 0) | (BATCH_RETUNE if retune else 0)
+        h = ctypes.c_void_p()
+        code = lib.pbe_batch_create(
+            ctypes.byref(h), len(grid_n), grid_n.ctypes.data, grid_x.ctypes.data, len(cn),
+            cn.ctypes.data, cg.ctypes.data, int(kernel), int(selection), nq,
+            None if tq is None else tq.ctypes.data, None if bw is None else bw.ctypes.data,
+            flags, _stream(stream))
+        if code:
+            raise PbeError(code, "pbe_batch_create")
+        self._h = h
+        self.n_cells = len(cn)
+        self.cell_n = cn.copy()
+        self.offsets = np.zeros(self.n_cells + 1, dtype=np.int64)
+        _lib.check(lib.pbe_batch_offsets(h, self.offsets.ctypes.data), "pbe_batch_offsets")
+        self.total = int(self.offsets[-1])
+
+    # -- calls ------------------------------------------------------------------
+    def rhs(self, N, rhs, params, stream=None) -> int:
+        """rhs += RHS(N) for every cell. N, rhs: packed float64 device arrays;
+        params: device array [n_cells, 8] (cell_params layout)."""
+        return _lib.load().pbe_batch_rhs(self._h, _ptr(N, "N"), _ptr(rhs, "rhs"),
+                                         _ptr(params, "params"), _stream(stream))
+
+    def rk4(self, N, params, dt: float, n_steps: int, stream=None) -> int:
+        """n_steps RK4 steps in place on N, as one CUDA graph launch."""
+        return _lib.load().pbe_batch_rk4(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                         float(dt), int(n_steps), _stream(stream))
+
+    def rk4_percell(self, N, params, dt: float, n_steps: int, stream=None) -> int:
+        """The same integration as a per-cell launch loop (baseline)."""
+        return _lib.load().pbe_batch_rk4_percell(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                                 float(dt), int(n_steps), _stream(stream))
+
+    def schedule(self):
+        """({class: group size} for the section-count classes present, bundles)."""
+        gs = np.zeros(16, dtype=np.int32)
+        nb = ctypes.c_int()
+        _lib.check(_lib.load().pbe_batch_schedule(self._h, gs.ctypes.data, ctypes.byref(nb)),
+                   "pbe_batch_schedule")
+        return {c: int(t) for c, t in enumerate(gs) if t}, nb.value
+
+    def split(self, packed: np.ndarray):
+        """Per-cell views of a packed host array."""
+        return [packed[self.offsets[c]:self.offsets[c + 1]] for c in range(self.n_cells)]
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().pbe_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

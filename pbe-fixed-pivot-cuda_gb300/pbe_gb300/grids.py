@@ -58,3 +58,76 @@ def config_n16384():
     N = lognormal_ic(x, 2048, 1.0, 1e14)
     return dict(n=n, x=x, N=N, beta_br=6.73e-18, beta_sh=4.0 * 50.0 / 3.0, S0=1e-3,
                 v_min=float(x[8192]))
+
+
+BATCH_SEED = 2026
+
+
+def config_batched_cells(n_cells: int = 4096, seed: int = BATCH_SEED, n_max: int = 3840,
+                         total: float = 1e13):
+    """Batched-cell workload: `n_cells` independent cells, seeded
+    (numpy.random.default_rng(seed)).
+      sections n ~ U{64, 128, ..., n_max}; q ~ U{4, 8, 16, 32};
+      grid x_i = 1e-21 * 2**(i/q) m^3 (one shared grid per q, n_max pivots;
+      a cell uses its first n);
+      Brownian + shear aggregation, beta_br = 6.73e-18 m^3/s,
+      beta_sh = 4 G / 3 with G log-uniform in [10, 200] 1/s per cell;
+      power-law selection S = S0 (x / x_ref)^a, S0 = 1e-3 1/s,
+      a ~ U[0.5, 1.5], x_ref = the cell's middle pivot x[n // 2];
+      uniform daughter on Gauss-Legendre 8 points;
+      lognormal N (sigma_ln = 1, total `total` m^-3) with median at
+      1e-18 m^3, or at bin n // 4 when the cell's grid ends below that.
+    Returns dict(grids, q_values, cell_n, cell_grid, params [n_cells, 8],
+    N (packed), t_q, bw_q, seed)."""
+    from .batch import cell_params
+    from .quadrature import uniform
+
+    rng = np.random.default_rng(seed)
+    cell_n = 64 * rng.integers(1, n_max // 64 + 1, size=n_cells)
+    q_values = np.array([4, 8, 16, 32])
+    qi = rng.integers(0, 4, size=n_cells)
+    G = np.exp(rng.uniform(math.log(10.0), math.log(200.0), size=n_cells))
+    a = rng.uniform(0.5, 1.5, size=n_cells)
+    grids = [geometric_pow2(n_max, 1e-21, float(q)) for q in q_values]
+    x_ref = np.array([grids[g][n // 2] for g, n in zip(qi, cell_n)])
+    params = cell_params(n_cells, beta0=0.0, beta_br=6.73e-18, beta_sh=4.0 * G / 3.0, S0=1e-3,
+                         v_ref=x_ref, alpha=a)
+    parts = []
+    for g, n in zip(qi, cell_n):
+        x = grids[g][:n]
+        m = min(int(round(q_values[g] * math.log2(1e-18 / 1e-21))), n // 4)
+        parts.append(lognormal_ic(x, m, 1.0, total))
+    t_q, bw_q = uniform(8)
+    return dict(grids=grids, q_values=q_values, cell_n=cell_n.astype(np.int32),
+                cell_grid=qi.astype(np.int32), params=params, N=np.concatenate(parts),
+                t_q=t_q, bw_q=bw_q, seed=seed)
+
+
+def config_flocculation_adjoint(n: int = 3840, n_steps: int = 200, switch_step: int = 100):
+    """Two-stage flocculation adjoint workload: x_i = 1e-21 * 2**(i/128) m^3,
+    Brownian + shear aggregation (beta_br = 6.73e-18 m^3/s, beta_sh = 4 G / 3
+    with G = 100 1/s for steps < switch_step and 20 1/s after), power-law
+    selection S0 = 5e-4 1/s, a = 1, v_ref = 1e-18 m^3, power-law daughter
+    b(v|v') = 4 v^2 / v'^3 (exponent 2; 2 x 4 Gauss-Legendre points split at
+    t = 1/2), dt = 0.5 s. Initial N: lognormal in ln x with median 3.2e-20 m^3
+    (bin 640), sigma_ln = 1, total 1e12 m^-3, set to exactly 0 beyond 5 sigma
+    (the upper bins have shear death rates far above 1/dt, so they start
+    empty). Loss L = sum_i x_i^(2/3) N_i(T), so dL/dN(T) = x^(2/3).
+    Returns dict(x, N0, t_q, bw_q, agg_sets (2), brk_sets (2), step_set, dt,
+    n_steps, lam_T)."""
+    from ._lib import AggregationParams, BreakageParams
+    from .quadrature import power_law
+
+    x = geometric_pow2(n, 1e-21, 128.0)
+    m = min(640, n // 4)
+    z = (np.log(x) - math.log(x[m])) / 1.0
+    N0 = np.where(np.abs(z) <= 5.0, np.exp(-0.5 * z * z), 0.0)
+    N0 *= 1e12 / N0.sum()
+    t_q, bw_q = power_law(2.0, 4)
+    agg = [AggregationParams(n=n, kernel_type=5, beta0=0.0, beta_br=6.73e-18,
+                             beta_sh=4.0 * G / 3.0) for G in (100.0, 20.0)]
+    brk = [BreakageParams(n=n, n_quad=len(t_q), selection=2, S0=5e-4, v_ref=1e-18, alpha=1.0,
+                          v_min=0.0) for _ in range(2)]
+    step_set = np.array([0 if s < switch_step else 1 for s in range(n_steps)], dtype=np.int32)
+    return dict(x=x, N0=N0, t_q=t_q, bw_q=bw_q, agg_sets=agg, brk_sets=brk, step_set=step_set,
+                dt=0.5, n_steps=n_steps, lam_T=x ** (2.0 / 3.0))

@@ -1,0 +1,199 @@
+"""Checkpointed RK4 adjoint (pbe_rk4_tape_*) on the GPU.
+
+Checked three ways: against the oracle's serial discrete adjoint (itself
+pinned to finite differences in test_oracle_rk4_adjoint.py), against central
+finite differences of the GPU forward (h = 1e-6 relative), and for
+independence of the checkpoint interval (bitwise). The two-stage flocculation
+workload (shear rate switching mid-run, power-law selection and daughter,
+L = sum x^(2/3) N(T)) is run at full size. A torch.autograd.Function wraps the
+tape here, in the test harness only."""
+import numpy as np
+import pytest
+
+import pbe_gb300 as pg
+import pyoracle
+from gpu_util import t
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def small_case(n=200, steps=12, switch=6):
+    x = pg.grids.geometric_pow2(n, 1e-21, 16.0)
+    N0 = pg.grids.lognormal_ic(x, n // 4, 1.0, 1e13)
+    t_q, bw_q = pg.quadrature.power_law(2.0, 4)
+    v_ref = float(x[n // 2])
+    agg = [pg.AggregationParams(n=n, kernel_type=5, beta0=0.0, beta_br=6.73e-18, beta_sh=4 * G / 3)
+           for G in (100.0, 20.0)]
+    brk = [pg.BreakageParams(n=n, n_quad=len(t_q), selection=2, S0=5e-4 * f, v_ref=v_ref,
+                             alpha=1.0 + 0.1 * f) for f in (1.0, 2.0)]
+    step_set = np.array([0 if s < switch else 1 for s in range(steps)], dtype=np.int32)
+    return x, N0, t_q, bw_q, agg, brk, step_set
+
+
+def run_tape(x, N0, t_q, bw_q, agg, brk, step_set, dt, every, lam):
+    torch = _torch()
+    n, m = len(x), len(agg if agg is not None else brk)
+    with pg.Rk4Tape(len(step_set), dt, every, agg, brk, step_set) as tape:
+        N = t(N0)
+        dx, dtq, dbw = t(x), t(t_q), t(bw_q)
+        assert tape.forward(N, dx, dtq, dbw) == 0
+        gN0 = t(np.zeros(n))
+        ga, gb = t(np.zeros(3 * m)), t(np.zeros(4 * m))
+        assert tape.backward(t(lam), gN0, ga, gb) == 0
+        torch.cuda.synchronize()
+        return (N.cpu().numpy(), gN0.cpu().numpy(), ga.cpu().numpy().reshape(m, 3),
+                gb.cpu().numpy().reshape(m, 4))
+
+
+def oracle_sets(agg, brk):
+    A = np.array([[a.kernel_type, a.beta0, a.beta_br, a.beta_sh] for a in agg])
+    B = np.array([[b.selection, b.S0, b.v_ref, b.alpha, b.v_min] for b in brk])
+    return A, B
+
+
+def test_tape_matches_oracle_adjoint():
+    x, N0, t_q, bw_q, agg, brk, step_set = small_case()
+    dt = 0.5
+    lam = x ** (2.0 / 3.0)
+    NT, gN0, ga, gb = run_tape(x, N0, t_q, bw_q, agg, brk, step_set, dt, 5, lam)
+    A, B = oracle_sets(agg, brk)
+    rNT, rgN0, rga, rgb = pyoracle.rk4_adjoint(N0, x, dt, len(step_set), lam, A, B, step_set,
+                                               t_q, bw_q)
+    np.testing.assert_allclose(NT, rNT, rtol=1e-11, atol=1e-11 * np.abs(N0).max())
+    np.testing.assert_allclose(gN0, rgN0, rtol=1e-10, atol=1e-10 * np.abs(rgN0).max())
+    np.testing.assert_allclose(ga[:, 1:], rga[:, 1:], rtol=1e-9)
+    np.testing.assert_allclose(gb[:, [0, 2]], rgb[:, [0, 2]], rtol=1e-9)
+    np.testing.assert_allclose(gb[:, 1], rgb[:, 1], rtol=1e-9, atol=1e-9 * np.abs(rgb[:, 1]).max())
+
+
+def test_checkpoint_interval_does_not_change_the_result():
+    x, N0, t_q, bw_q, agg, brk, step_set = small_case(n=120, steps=9, switch=4)
+    lam = np.random.default_rng(3).normal(size=len(x))
+    outs = [run_tape(x, N0, t_q, bw_q, agg, brk, step_set, 0.5, every, lam)
+            for every in (1, 4, 9, 50)]
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
+def test_tape_matches_finite_differences_of_gpu_forward():
+    torch = _torch()
+    x, N0, t_q, bw_q, agg, brk, step_set = small_case(n=160, steps=8, switch=4)
+    dt = 0.5
+    w = x ** (2.0 / 3.0)
+    _, gN0, ga, gb = run_tape(x, N0, t_q, bw_q, agg, brk, step_set, dt, 3, w)
+    dx, dtq, dbw = t(x), t(t_q), t(bw_q)
+
+    def L(N0_=N0, agg_=agg, brk_=brk):
+        with pg.Rk4Tape(len(step_set), dt, 4, agg_, brk_, step_set) as tape:
+            N = t(N0_)
+            assert tape.forward(N, dx, dtq, dbw) == 0
+            torch.cuda.synchronize()
+            return float(w @ N.cpu().numpy())
+
+    L0 = abs(L())
+    for m in (10, 40, 41, 80, 120):
+        h = 1e-6 * N0[m]
+        Np, Nm = N0.copy(), N0.copy()
+        Np[m] += h
+        Nm[m] -= h
+        fd = (L(Np) - L(Nm)) / (2 * h)
+        assert abs(fd - gN0[m]) <= 1e-6 * abs(gN0[m]) + 1e-12 * L0 / h, (m, fd, gN0[m])
+
+    def perturbed(sets, k, name, h):
+        out = []
+        for i, s in enumerate(sets):
+            c = type(s).from_buffer_copy(s)
+            if i == k:
+                setattr(c, name, getattr(c, name) + h)
+            out.append(c)
+        return out
+
+    for k in range(2):
+        for name, g in (("beta_br", ga[k, 1]), ("beta_sh", ga[k, 2])):
+            h = 1e-6 * getattr(agg[k], name)
+            fd = (L(agg_=perturbed(agg, k, name, h)) - L(agg_=perturbed(agg, k, name, -h))) / (2 * h)
+            assert abs(fd - g) <= 2e-6 * abs(g) + 1e-12 * L0 / h, (k, name, fd, g)
+        for name, g in (("S0", gb[k, 0]), ("alpha", gb[k, 2])):
+            h = 1e-6 * getattr(brk[k], name)
+            fd = (L(brk_=perturbed(brk, k, name, h)) - L(brk_=perturbed(brk, k, name, -h))) / (2 * h)
+            assert abs(fd - g) <= 2e-6 * abs(g) + 1e-12 * L0 / h, (k, name, fd, g)
+
+
+def test_autograd_function_wrapper():
+    """The tape behind torch.autograd (harness-only wrapper): gradient of
+    L = sum w N(T) with respect to N(0) equals the tape's dL/dN(0)."""
+    torch = _torch()
+    x, N0, t_q, bw_q, agg, brk, step_set = small_case(n=96, steps=6, switch=3)
+    dt = 0.5
+    dx, dtq, dbw = t(x), t(t_q), t(bw_q)
+
+    class RK4Run(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, N0_):
+            tape = pg.Rk4Tape(len(step_set), dt, 2, agg, brk, step_set)
+            N = N0_.detach().clone().contiguous()
+            assert tape.forward(N, dx, dtq, dbw) == 0
+            ctx.tape = tape
+            return N
+
+        @staticmethod
+        def backward(ctx, g):
+            gN0 = torch.zeros_like(g)
+            ga = torch.zeros(6, dtype=torch.float64, device=g.device)
+            gb = torch.zeros(8, dtype=torch.float64, device=g.device)
+            assert ctx.tape.backward(g.contiguous(), gN0, ga, gb) == 0
+            ctx.tape.close()
+            return gN0
+
+    N0t = t(N0).requires_grad_(True)
+    w = t(x ** (2.0 / 3.0))
+    L = (w * RK4Run.apply(N0t)).sum()
+    (g,) = torch.autograd.grad(L, N0t)
+    _, gN0, _, _ = run_tape(x, N0, t_q, bw_q, agg, brk, step_set, dt, 2, x ** (2.0 / 3.0))
+    assert np.array_equal(g.cpu().numpy(), gN0)
+
+
+def test_flocculation_two_stage_adjoint_full_size():
+    """n = 3840, 200 RK4 steps, checkpoints every 20, shear switching at step
+    100: finite result, mass-like moment sane, gradient checked against central
+    differences for a few initial bins and for the coefficients."""
+    torch = _torch()
+    cfg = pg.grids.config_flocculation_adjoint()
+    x, N0 = cfg["x"], cfg["N0"]
+    agg, brk, ss = cfg["agg_sets"], cfg["brk_sets"], cfg["step_set"]
+    NT, gN0, ga, gb = run_tape(x, N0, cfg["t_q"], cfg["bw_q"], agg, brk, ss, cfg["dt"], 20,
+                               cfg["lam_T"])
+    assert np.all(np.isfinite(NT)) and np.all(np.isfinite(gN0))
+    assert np.all(np.isfinite(ga)) and np.all(np.isfinite(gb))
+    dx, dtq, dbw = t(x), t(cfg["t_q"]), t(cfg["bw_q"])
+
+    def L(N0_=N0, agg_=agg, brk_=brk):
+        with pg.Rk4Tape(len(ss), cfg["dt"], 50, agg_, brk_, ss) as tape:
+            N = t(N0_)
+            assert tape.forward(N, dx, dtq, dbw) == 0
+            torch.cuda.synchronize()
+            return float(cfg["lam_T"] @ N.cpu().numpy())
+
+    L0 = abs(L())
+    for m in (400, 640, 900):
+        h = 1e-6 * N0[m]
+        Np, Nm = N0.copy(), N0.copy()
+        Np[m] += h
+        Nm[m] -= h
+        fd = (L(Np) - L(Nm)) / (2 * h)
+        assert abs(fd - gN0[m]) <= 1e-5 * abs(gN0[m]) + 1e-11 * L0 / h, (m, fd, gN0[m])
+    for k in range(2):
+        h = 1e-6 * agg[k].beta_sh
+        ap = [type(a).from_buffer_copy(a) for a in agg]
+        am = [type(a).from_buffer_copy(a) for a in agg]
+        ap[k].beta_sh += h
+        am[k].beta_sh -= h
+        fd = (L(agg_=ap) - L(agg_=am)) / (2 * h)
+        assert abs(fd - ga[k, 2]) <= 1e-5 * abs(ga[k, 2]) + 1e-11 * L0 / h, (k, fd, ga[k, 2])
