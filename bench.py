@@ -186,6 +186,277 @@ def cpu_baseline(x, N, t_q, bw_q, ap, bp, seconds=3.0):
                       "aggregation rows, breakage serial)" % (evals, el)}
 
 
+def fp64_instr_tiles(x, n_cell=None) -> int:
+    """FP64 instructions of the tile kernel for a cell with the first n_cell
+    pivots of x (same counting as fp64_instr_per_launch)."""
+    x = x[:n_cell] if n_cell else x
+    return fp64_instr_per_launch(x)
+
+
+def batched_section(dev, stream):
+    """Batched cells: 4096 cells with n in {64..3840}, q in {4,8,16,32}
+    (pbe_gb300.grids.config_batched_cells, seed 2026), Brownian+shear with a
+    per-cell shear rate, power-law selection, uniform daughter (GL 8); 100 RK4
+    steps of dt = 0.5 s as one CUDA graph, against the per-cell launch loop
+    (single-instance calls per cell and stage) over one step."""
+    import torch
+
+    import pbe_gb300 as pg
+
+    cfg = pg.grids.config_batched_cells()
+    t0 = time.perf_counter()
+    plan = pg.BatchPlan(cfg["grids"], cfg["cell_n"], cfg["cell_grid"], pg.AGG_BROWNIAN_SHEAR,
+                        pg.SEL_POWERLAW, cfg["t_q"], cfg["bw_q"], tune=True, stream=stream)
+    plan_s = time.perf_counter() - t0
+    f64 = dict(dtype=torch.float64, device=dev)
+    dN = torch.tensor(cfg["N"], **f64)
+    P = torch.tensor(cfg["params"], **f64)
+    out = torch.zeros(plan.total, **f64)
+    n_cells = len(cfg["cell_n"])
+    cn = cfg["cell_n"].astype(np.float64)
+    pairs = float((cn * (cn + 1) / 2).sum())
+    frags = float(cn.sum() * len(cfg["t_q"]))
+    steps, dt = 100, 0.5
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            pg.check(plan.rhs(dN, out, P, stream=stream), "batch rhs")
+        reps = 5
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            pg.check(plan.rhs(dN, out, P, stream=stream), "batch rhs")
+        b.record(stream)
+        torch.cuda.synchronize()
+        rhs_ms = a.elapsed_time(b) / reps
+        # 100 steps in one graph (captured and uploaded before the timing)
+        Y = dN.clone()
+        pg.check(plan.rk4_prepare(Y, P, dt, steps), "rk4 prepare")
+        torch.cuda.synchronize()
+        a.record(stream)
+        pg.check(plan.rk4(Y, P, dt, steps, stream=stream), "rk4")
+        b.record(stream)
+        torch.cuda.synchronize()
+        graph_ms = a.elapsed_time(b)
+        fin = torch.isfinite(Y).cpu().numpy()
+        off = np.r_[0, np.cumsum(cfg["cell_n"])]
+        bad_cells = int(sum(not fin[off[c]:off[c + 1]].all() for c in range(n_cells)))
+        finite = bad_cells == 0
+        # per-cell launch loop, one step
+        Z = dN.clone()
+        pg.check(plan.rk4_percell(Z, P, dt, 1, stream=stream), "percell warm-up")
+        Z = dN.clone()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        a.record(stream)
+        pg.check(plan.rk4_percell(Z, P, dt, 1, stream=stream), "percell")
+        b.record(stream)
+        torch.cuda.synchronize()
+        loop_ms = a.elapsed_time(b)
+        loop_wall = time.perf_counter() - w0
+        Y1 = dN.clone()
+        pg.check(plan.rk4(Y1, P, dt, 1, stream=stream), "rk4 one step")
+        torch.cuda.synchronize()
+        agree = float((Y1 - Z).abs().max() / dN.abs().max())
+    gs, nb = plan.schedule()
+    plan.close()
+    # FP64 instructions of one batched RHS (tile evaluations, per cell)
+    instr = 0
+    memo = {}
+    for g, n in zip(cfg["cell_grid"], cfg["cell_n"]):
+        key = (int(g), int(n))
+        if key not in memo:
+            memo[key] = fp64_instr_tiles(cfg["grids"][g], int(n))
+        instr += memo[key]
+    peak = fp64_peak_tflops(stream)
+    cell_steps = n_cells * steps / (graph_ms / 1e3)
+    loop_cell_steps = n_cells / (loop_ms / 1e3)
+    achieved = (FLOPS_PER_PAIR * pairs + FLOPS_PER_FRAGMENT * frags) / (rhs_ms / 1e3) / 1e12
+    return {
+        "workload": "4096 cells, n ~ U{64..3840}, x_i = 1e-21*2^(i/q), q ~ U{4,8,16,32}, "
+                    "Brownian+shear (per-cell G log-uniform [10,200]) + power-law selection "
+                    "(S0=1e-3, a ~ U[0.5,1.5], x_ref = middle pivot) + uniform daughter GL8, "
+                    "lognormal N; seed 2026; 100 RK4 steps dt=0.5 s in one CUDA graph",
+        "cell_steps_per_s": round(cell_steps, 1),
+        "graph_ms": round(graph_ms, 2),
+        "steps": steps,
+        "percell_loop_cell_steps_per_s": round(loop_cell_steps, 1),
+        "percell_loop_ms_per_step": round(loop_ms, 2),
+        "percell_loop_wall_s": round(loop_wall, 3),
+        "speedup_vs_percell_loop": round(cell_steps / loop_cell_steps, 3),
+        "graph_vs_loop_max_rel_diff_1step": agree,
+        "finite_after_100_steps": finite,
+        "cells_not_finite": bad_cells,
+        "rhs_ms": round(rhs_ms, 3),
+        "pair_interactions_per_s": round(pairs / (rhs_ms / 1e3), 1),
+        "pairs_per_rhs": pairs,
+        "roofline": {"bound": "fp64", "kernel": "batch_main_kernel<5> + batch_prep_kernel<5>",
+                     "achieved": round(achieved, 4), "peak": round(peak, 4) if peak else None,
+                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                     "fp64_instr_per_rhs": instr,
+                     "fp64_pipe_frac": round(instr / (rhs_ms / 1e3) / (peak * 1e12 / 2.0), 4)
+                     if peak else None},
+        "schedule": {"group_size_by_log2n": gs, "bundles": nb, "tuned": True,
+                     "plan_create_s": round(plan_s, 3)},
+        "l2": "not flushed: one RHS touches > 300 MB of stage arrays (L2 126 MiB)",
+    }
+
+
+def adjoint_section(dev, stream):
+    """Two-stage flocculation adjoint (pbe_gb300.grids.config_flocculation_adjoint):
+    n = 3840, 200 RK4 steps dt = 0.5 s, G 100 -> 20 at step 100, checkpoints
+    every 20 steps; gradient of L = sum x^(2/3) N(T) w.r.t. N(0) and the
+    coefficients of both stages."""
+    import torch
+
+    import pbe_gb300 as pg
+
+    cfg = pg.grids.config_flocculation_adjoint()
+    f64 = dict(dtype=torch.float64, device=dev)
+    n = len(cfg["x"])
+    dx, dtq, dbw = (torch.tensor(cfg[k], **f64) for k in ("x", "t_q", "bw_q"))
+    lam = torch.tensor(cfg["lam_T"], **f64)
+    gN0 = torch.zeros(n, **f64)
+    ga, gb = torch.zeros(6, **f64), torch.zeros(8, **f64)
+    tape = pg.Rk4Tape(cfg["n_steps"], cfg["dt"], 20, cfg["agg_sets"], cfg["brk_sets"],
+                      cfg["step_set"])
+    a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            N = torch.tensor(cfg["N0"], **f64)
+            pg.check(tape.forward(N, dx, dtq, dbw, stream=stream), "tape forward")
+            pg.check(tape.backward(lam, gN0, ga, gb, stream=stream), "tape backward")
+        N = torch.tensor(cfg["N0"], **f64)
+        torch.cuda.synchronize()
+        a.record(stream)
+        pg.check(tape.forward(N, dx, dtq, dbw, stream=stream), "tape forward")
+        b.record(stream)
+        pg.check(tape.backward(lam, gN0, ga, gb, stream=stream), "tape backward")
+        c.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms, bwd_ms = a.elapsed_time(b), b.elapsed_time(c)
+        # one RHS and one VJP at N(0), n = 3840
+        N0 = torch.tensor(cfg["N0"], **f64)
+        rhs = torch.zeros(n, **f64)
+        ap, bp = cfg["agg_sets"][0], cfg["brk_sets"][0]
+
+        def rhs_call():
+            rhs.zero_()
+            pg.check(pg.aggregation_rhs(N0, dx, rhs, ap, stream=stream), "agg")
+            pg.check(pg.breakage_rhs(N0, dx, dtq, dbw, rhs, bp, stream=stream), "brk")
+
+        def vjp_call():
+            gN0.zero_()
+            pg.check(pg.aggregation_rhs_vjp(N0, dx, lam, gN0, ga, ap, stream=stream), "agg vjp")
+            pg.check(pg.breakage_rhs_vjp(N0, dx, dtq, dbw, lam, gN0, gb, bp, stream=stream), "brk vjp")
+        times = {}
+        for name, fn in (("rhs", rhs_call), ("vjp", vjp_call)):
+            for _ in range(3):
+                fn()
+            a.record(stream)
+            for _ in range(20):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times[name] = a.elapsed_time(b) / 20
+    tape.close()
+    g = gN0.cpu().numpy()
+    return {
+        "workload": "n=3840, x_i=1e-21*2^(i/128), Brownian+shear G=100 -> 20 at step 100, "
+                    "power-law selection S0=5e-4 a=1 v_ref=1e-18, power-law daughter p=2 (8 pts), "
+                    "200 RK4 steps dt=0.5 s, checkpoints every 20, L = sum x^(2/3) N(T)",
+        "forward_ms": round(fwd_ms, 3),
+        "backward_ms": round(bwd_ms, 3),
+        "backward_forward_ratio": round(bwd_ms / fwd_ms, 4),
+        "gradient_cost_ratio": round((fwd_ms + bwd_ms) / fwd_ms, 4),
+        "rhs_ms_n3840": round(times["rhs"], 4),
+        "vjp_ms_n3840": round(times["vjp"], 4),
+        "vjp_rhs_ratio_n3840": round(times["vjp"] / times["rhs"], 4),
+        "gradient_finite": bool(np.all(np.isfinite(g))),
+    }
+
+
+def probe_tflops(stream, name) -> float | None:
+    import ctypes
+
+    import pbe_gb300 as pg
+
+    path = os.path.join(os.path.dirname(pg.LIB_PATH), "libpbe_probe.so")
+    if not os.path.isfile(path):
+        return None
+    lib = ctypes.CDLL(path)
+    fn = getattr(lib, name)
+    fn.restype = ctypes.c_double
+    fn.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    v = fn(5, stream.cuda_stream)
+    return v if v > 0 else None
+
+
+def classes_section(dev, stream):
+    """Cells sharing grids by size class (pbe_gb300.grids.config_batched_classes):
+    512 cells, n ~ U[256, 2048], class width 256, per-cell lognormal
+    coefficients. 100 RK4 steps as one graph; the aggregation death term by the
+    per-cell moment form and by the FP64 tensor-core GEMM (mma.sync f64)."""
+    import torch
+
+    import pbe_gb300 as pg
+
+    cfg = pg.grids.config_batched_classes()
+    plan = pg.BatchPlan(cfg["grids"], cfg["cell_n"], cfg["cell_grid"], pg.AGG_BROWNIAN_SHEAR,
+                        pg.SEL_POWERLAW, cfg["t_q"], cfg["bw_q"], tune=True, stream=stream)
+    f64 = dict(dtype=torch.float64, device=dev)
+    dN, P = torch.tensor(cfg["N"], **f64), torch.tensor(cfg["params"], **f64)
+    out = {m: torch.zeros(plan.total, **f64) for m in (pg.DEATH_MOMENTS, pg.DEATH_DMMA)}
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = {}
+    with torch.cuda.stream(stream):
+        for m in (pg.DEATH_MOMENTS, pg.DEATH_DMMA):
+            for _ in range(3):
+                pg.check(plan.death(dN, out[m], P, m, stream=stream), "death")
+            a.record(stream)
+            for _ in range(10):
+                pg.check(plan.death(dN, out[m], P, m, stream=stream), "death")
+            b.record(stream)
+            torch.cuda.synchronize()
+            times[m] = a.elapsed_time(b) / 10
+        ref = out[pg.DEATH_MOMENTS]
+        diff = float(((out[pg.DEATH_DMMA] - ref).abs() / ref.abs().clamp_min(1e-300)).max())
+        steps = 100
+        Y = dN.clone()
+        pg.check(plan.rk4_prepare(Y, P, 0.5, steps), "rk4 prepare")
+        torch.cuda.synchronize()
+        a.record(stream)
+        pg.check(plan.rk4(Y, P, 0.5, steps, stream=stream), "rk4")
+        b.record(stream)
+        torch.cuda.synchronize()
+        graph_ms = a.elapsed_time(b)
+        finite = bool(torch.isfinite(Y).all())
+    plan.close()
+    cn = cfg["cell_n"].astype(np.float64)
+    gemm_flops = float((2.0 * cn * cn).sum() * 2)          # two separable components
+    dmma_peak = probe_tflops(stream, "pbe_probe_dmma_tflops")
+    dmma_tf = gemm_flops / (times[pg.DEATH_DMMA] / 1e3) / 1e12
+    return {
+        "workload": "512 cells, n ~ U[256,2048], grids shared by size class (width 256), "
+                    "x_i = 1e-21*2^(i/128); Brownian+shear + power-law selection, per-cell "
+                    "coefficients lognormal(0.5) around beta_br=6.73e-18, G=50, S0=1e-3; seed 2026",
+        "cell_steps_per_s": round(len(cn) * steps / (graph_ms / 1e3), 1),
+        "graph_ms_100_steps": round(graph_ms, 2),
+        "finite_after_100_steps": finite,
+        "death_moments_ms": round(times[pg.DEATH_MOMENTS], 4),
+        "death_dmma_ms": round(times[pg.DEATH_DMMA], 4),
+        "dmma_over_moments_time": round(times[pg.DEATH_DMMA] / times[pg.DEATH_MOMENTS], 2),
+        "death_max_rel_diff": diff,
+        "dmma_roofline": {"bound": "fp64 tensor (mma.sync f64)", "achieved": round(dmma_tf, 4),
+                          "peak": round(dmma_peak, 4) if dmma_peak else None, "unit": "TFLOP/s",
+                          "frac": round(dmma_tf / dmma_peak, 4) if dmma_peak else None,
+                          "flops_per_call": gemm_flops,
+                          "algorithmic_unit": "2 n^2 flops per cell and separable component "
+                                              "(Brownian, shear)",
+                          "peak_source": "mma.sync m8n8k4 f64 chain probe timed in this run "
+                                         "(libpbe_probe.so), of measured"},
+    }
+
+
 def main():
     ap_ = argparse.ArgumentParser()
     ap_.add_argument("--gpus", type=int, default=1)
@@ -194,6 +465,8 @@ def main():
     ap_.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap_.add_argument("--mode", choices=["gather", "scatter"], default="gather")
     ap_.add_argument("--no-cpu-baseline", action="store_true")
+    ap_.add_argument("--no-extras", action="store_true",
+                     help="skip the batched-cell and adjoint sections")
     args = ap_.parse_args()
 
     import torch
@@ -391,6 +664,10 @@ def main():
             "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
                            "FP64 entry in MEASURED_PEAKS.json",
         }
+    if n_gpus == 1 and args.impl == "ours" and not args.no_extras:
+        out["batched"] = batched_section(dev, stream)
+        out["adjoint"] = adjoint_section(dev, stream)
+        out["classes"] = classes_section(dev, stream)
     if n_gpus == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(x, N, t_q, bw_q, ap, bp)
     print(json.dumps(out))

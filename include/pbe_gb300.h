@@ -231,11 +231,28 @@ int pbe_batch_rhs(pbe_batch_t plan, const double* N, double* rhs,
 int pbe_batch_rk4(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
                   double dt, int n_steps, void* stream);
 
+/* Captures and instantiates the graph pbe_batch_rk4 would launch for these
+ * arguments, without running it (so that a timed or latency-critical first
+ * call does not pay for the capture). */
+int pbe_batch_rk4_prepare(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                          double dt, int n_steps);
+
 /* The same integration as a per-cell launch loop: for every step, cell and
  * stage, the single-instance aggregation and breakage calls plus a stage
  * update kernel (no graph, no batching). Baseline and cross-check. */
 int pbe_batch_rk4_percell(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
                           double dt, int n_steps, void* stream);
+
+/* Aggregation death term of every cell, death[off_c + i] =
+ * N_ci sum_k beta_c(x_i, x_k) N_ck (overwritten; the RHS subtracts it), by
+ *   PBE_DEATH_MOMENTS: five per-cell moments (the form the RHS kernels use);
+ *   PBE_DEATH_DMMA:    a GEMM per grid over the cells sharing it, on the FP64
+ *                      tensor cores (mma.sync f64), one per separable term.
+ * For comparison and for callers that want the death term alone; needs an
+ * aggregation kernel in the plan. */
+enum { PBE_DEATH_MOMENTS = 0, PBE_DEATH_DMMA = 1 };
+int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_params_t* params,
+                    double* death, int method, void* stream);
 
 /* Schedule in use: group_size[c] (16 entries) = threads per tile task for
  * cells with floor(log2(n)) == c (0 where no cell falls), *n_bundles = the

@@ -36,6 +36,8 @@
 // order -> bitwise reproducible. SCATTER mode: geometric tasks are (tile, lag
 // chunk) and flush with FP64 atomicAdd.
 // =============================================================================
+#include <cstdlib>
+
 #include "pbe_internal.cuh"
 #include "agg_tile.cuh"
 
@@ -202,20 +204,22 @@ agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, doub
 
 
 // ---------------------------------------------------------------------------
-// main: persistent CTAs; each task owns the W bins [I, I+W) of one tile and
-// accumulates the slots s = I-1 .. I+W-1 (slot I-1 only feeds the w-part of
-// bin I) with the whole CTA as one group (agg_tile.cuh). Thread-private
-// partial sums are reduced in a fixed order.
+// main: persistent CTAs split into groups of T threads (agg_group_size); each
+// group pulls tasks from the atomic counter on its own. A task owns the W bins
+// [I, I+W) of one tile and accumulates the slots s = I-1 .. I+W-1 (slot I-1
+// only feeds the w-part of bin I) with the shared tile body (agg_tile.cuh).
+// Thread-private partial sums are reduced in a fixed order, so for a given T
+// the gather result is bitwise reproducible.
 // ---------------------------------------------------------------------------
 template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile, int nchunk,
-                int ntasks, double b0, double bbr, double bsh)
+                int ntasks, double b0, double bbr, double bsh, int T)
 {
     extern __shared__ double red[];               // [kRedRows][kMainThreads]
     __shared__ TileShared sm;
-    __shared__ int s_task;
+    __shared__ int s_task[kMaxGroups];
 
     const int tid = threadIdx.x;
     AggCellView v;
@@ -229,13 +233,16 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     v.b0 = b0; v.bbr = bbr; v.bsh = bsh;
 #pragma unroll
     for (int q = 0; q < 5; ++q) v.M[q] = ws.mom[q];
-    const TileGroup G{0, tid, kMainThreads};
+    // groups of T threads pull tasks on their own (no CTA-wide barrier in the loop)
+    const int g = tid / T;
+    const TileGroup G{g, tid - g * T, T};
+    const int lane = G.lane;
 
     for (;;) {
-        if (tid == 0) s_task = atomicAdd(ws.counter, 1);
-        __syncthreads();
-        const int task = s_task;
-        __syncthreads();
+        if (lane == 0) s_task[g] = atomicAdd(ws.counter, 1);
+        G.sync();
+        const int task = s_task[g];
+        G.sync();
         if (task >= ntasks) break;
 
         int tile, chunk = 0;
@@ -253,21 +260,21 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
         // the reference's w*rate even on grids spanning hundreds of octaves.
         const int St = -ilogb(x[I]);
-        agg_tile_accumulate<K>(v, I, d_begin, d_end, St, red, sm, G);
+        agg_tile_accumulate<K>(v, I, d_begin, d_end, St, red + g * T, sm, G);
 
         // clipped pairs of bin n-1 (gather: sum of the clip kernel's partials)
         double clip = 0.0;
         if (!SCATTER && I + W > n - 1) {
             const int nbc = (n + kClipWarps - 1) / kClipWarps;
             double s = 0.0;
-            for (int b = tid; b < nbc; b += kMainThreads) s += ws.clip_part[b];
+            for (int b = lane; b < nbc; b += T) s += ws.clip_part[b];
             clip = group_sum(s, sm, G);
         }
 
-        if (tid < W) {
-            const int i = I + tid;
+        if (lane < W) {
+            const int i = I + lane;
             if (i < n) {
-                double birth = agg_tile_birth(v, I, tid, St, sm.fin[0]);
+                double birth = agg_tile_birth(v, I, lane, St, sm.fin[g]);
                 const bool first = !(SCATTER && v.geo) || chunk == 0;
                 const double death = first ? agg_death<K>(v, i) : 0.0;
                 if constexpr (SCATTER) {
@@ -279,8 +286,26 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 }
             }
         }
-        __syncthreads();
+        G.sync();
     }
+}
+
+// Threads per tile task. A smaller group keeps fewer partial sums per slot
+// (the fixed-order reduction costs 2 (W+1) T FP64 adds per task) but runs
+// each task longer; with few tasks per group slot the last wave idles.
+// PBE_GB300_AGG_GROUP (32, 64, 128 or 256) overrides the rule.
+int agg_group_size(long long ntasks, int num_sms)
+{
+    static const int forced = []() {
+        const char* e = std::getenv("PBE_GB300_AGG_GROUP");
+        const int v = e ? std::atoi(e) : 0;
+        return (v == 32 || v == 64 || v == 128 || v == 256) ? v : 0;
+    }();
+    if (forced) return forced;
+    const long long per_sm = ntasks / (2LL * num_sms);     // tasks per CTA slot at T = 256
+    if (per_sm >= 16) return 64;
+    if (per_sm >= 6) return 128;
+    return 256;
 }
 
 template <int K, bool SC>
@@ -294,7 +319,9 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const long long ntasks_ll = static_cast<long long>(ntile) * nchunk;
     if (ntasks_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int ntasks = static_cast<int>(ntasks_ll);
-    const int grid = static_cast<int>(ntasks < 2LL * num_sms ? ntasks : 2LL * num_sms);
+    const int T = agg_group_size(ntasks, num_sms);
+    const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
+    const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
     const size_t smem = sizeof(double) * kRedRows * kMainThreads;
     cudaError_t e = cudaFuncSetAttribute(agg_main_kernel<K, SC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -307,7 +334,7 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
     agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, nchunk,
-                                                            ntasks, a.beta0, a.beta_br, a.beta_sh);
+                                                            ntasks, a.beta0, a.beta_br, a.beta_sh, T);
     if (prof) cudaEventRecord(g_prof_stop, s);
     return cudaGetLastError();
 }

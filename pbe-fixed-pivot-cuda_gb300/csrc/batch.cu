@@ -49,6 +49,10 @@ struct pbe_batch_plan {
     std::vector<double> t_q, bw_q;
     double* d_tq = nullptr;
     double* d_bw = nullptr;
+    // death-GEMM work items (built on first use)
+    int4* d_death_items = nullptr;
+    int* d_gcells = nullptr;
+    int n_death_items = -1;
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -74,12 +78,14 @@ int n_class(int n)
     return c;
 }
 
+// Default group size per class (what the autotuner picked on GB300 for the
+// 4096-cell workload: the reduction of 2 (W+1) T partial sums per task costs
+// more than the lanes a small group leaves idle), 128 for very large cells.
 int rule_group_size(int cls)
 {
-    if (cls <= 7) return 32;      // n < 256
-    if (cls == 8) return 64;      // n < 512
-    if (cls == 9) return 128;     // n < 1024
-    return 256;
+    if (cls <= 7) return 64;      // n < 256
+    if (cls <= 13) return 32;     // n < 16384
+    return 128;
 }
 
 // ---- tune cache ----------------------------------------------------------------
@@ -463,8 +469,9 @@ cudaError_t enqueue_rk4(pbe_batch_plan* p, double* N, const pbe_batch_cell_param
     return e;
 }
 
-cudaError_t rk4_graph(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
-                      int n_steps, cudaStream_t s)
+// Captures (if the cached graph does not match) without launching.
+cudaError_t rk4_capture(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
+                        int n_steps)
 {
     if (!p->exec || p->g_N != N || p->g_params != prm || p->g_dt != dt || p->g_steps != n_steps) {
         if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
@@ -478,9 +485,21 @@ cudaError_t rk4_graph(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_
         e = cudaGraphInstantiate(&p->exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) { p->exec = nullptr; return e; }
+        // move the executable graph to the device now, not at its first launch
+        e = cudaGraphUpload(p->exec, p->cap);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->cap);
+        if (e != cudaSuccess) return e;
         p->g_N = N; p->g_params = prm; p->g_dt = dt; p->g_steps = n_steps;
     }
-    cudaError_t e = cudaGraphLaunch(p->exec, s);
+    return cudaSuccess;
+}
+
+cudaError_t rk4_graph(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
+                      int n_steps, cudaStream_t s)
+{
+    cudaError_t e = rk4_capture(p, N, prm, dt, n_steps);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphLaunch(p->exec, s);
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
@@ -537,6 +556,45 @@ cudaError_t rk4_percell(pbe_batch_plan* p, double* N, const pbe_batch_cell_param
         }
     }
     return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+// Work items of the death GEMM: the cells of each grid, largest first, in
+// row tiles of 64; each row tile covers the bins below its largest n in
+// column tiles of 64.
+cudaError_t death_items(pbe_batch_plan* p, cudaStream_t s)
+{
+    if (p->n_death_items >= 0) return cudaSuccess;
+    std::vector<int> gcells;
+    std::vector<int4> items;
+    for (int g = 0; g < p->n_grids; ++g) {
+        std::vector<int> cs;
+        for (int c = 0; c < p->n_cells; ++c)
+            if (p->cell_grid[c] == g) cs.push_back(c);
+        std::stable_sort(cs.begin(), cs.end(),
+                         [&](int a, int b) { return p->cell_n[a] > p->cell_n[b]; });
+        const int base = static_cast<int>(gcells.size());
+        gcells.insert(gcells.end(), cs.begin(), cs.end());
+        for (size_t r = 0; r < cs.size(); r += 64) {
+            const int rows = static_cast<int>(std::min<size_t>(64, cs.size() - r));
+            const int nmax = p->cell_n[cs[r]];
+            for (int i0 = 0; i0 < nmax; i0 += 64)
+                items.push_back(make_int4(g, base + static_cast<int>(r), rows, i0));
+        }
+    }
+    int4* di = nullptr;
+    int* dg = nullptr;
+    cudaError_t e = plan_alloc(p, &di, items.size());
+    if (e == cudaSuccess) e = plan_alloc(p, &dg, gcells.size());
+    if (e == cudaSuccess && !items.empty())
+        e = cudaMemcpyAsync(di, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !gcells.empty())
+        e = cudaMemcpyAsync(dg, gcells.data(), gcells.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    p->d_death_items = di;
+    p->d_gcells = dg;
+    p->n_death_items = static_cast<int>(items.size());
+    return cudaSuccess;
 }
 
 } // namespace
@@ -601,6 +659,16 @@ int pbe_batch_rk4(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* pa
     return rk4_graph(plan, N, params, dt, n_steps, static_cast<cudaStream_t>(stream));
 }
 
+int pbe_batch_rk4_prepare(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                          double dt, int n_steps)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (n_steps <= 0 || !std::isfinite(dt)) return cudaErrorInvalidValue;
+    return rk4_capture(plan, N, params, dt, n_steps);
+}
+
 int pbe_batch_rk4_percell(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
                           double dt, int n_steps, void* stream)
 {
@@ -609,6 +677,23 @@ int pbe_batch_rk4_percell(pbe_batch_t plan, double* N, const pbe_batch_cell_para
     if (!N || !params) return cudaErrorInvalidDevicePointer;
     if (n_steps < 0 || !std::isfinite(dt)) return cudaErrorInvalidValue;
     return rk4_percell(plan, N, params, dt, n_steps, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_params_t* params,
+                    double* death, int method, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (plan->kernel < 0 || (method != PBE_DEATH_MOMENTS && method != PBE_DEATH_DMMA))
+        return cudaErrorInvalidValue;
+    if (!N || !params || !death) return cudaErrorInvalidDevicePointer;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (method == PBE_DEATH_DMMA) {
+        e = death_items(plan, s);
+        if (e != cudaSuccess) return e;
+    }
+    return batch_death(plan->d, N, params, death, method, plan->d_death_items,
+                       plan->n_death_items, plan->d_gcells, s);
 }
 
 int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)

@@ -94,6 +94,12 @@ cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
                                const pbe_batch_cell_params_t* params, double* out,
                                bool accumulate, const int4* bundles, const int2* tasks,
                                int n_bundles, cudaStream_t s);
+// Death term N_i sum_k beta(x_i, x_k) N_k of every cell (death_gemm.cu):
+// method 0 = per-cell moments, 1 = FP64 tensor-core GEMM over the work items
+// {grid, first row of gcells, rows <= 64, first bin} (cells grouped by grid).
+cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
+                        double* out, int method, const int4* items, int n_items,
+                        const int* gcells, cudaStream_t s);
 // Per-cell RK4 stage update for the per-cell launch loop (one cell, n bins).
 cudaError_t cell_stage(double* N, const double* k, double* kacc, double* Y, int n, int stage,
                        double c, double dt6, cudaStream_t s);

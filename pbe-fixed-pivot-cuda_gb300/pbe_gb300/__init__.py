@@ -24,6 +24,8 @@ from ._lib import (  # noqa: F401
     SEL_THRESHOLD,
     BATCH_RETUNE,
     BATCH_TUNE,
+    DEATH_DMMA,
+    DEATH_MOMENTS,
     AggregationParams,
     BatchCellParams,
     BreakageParams,

@@ -38,6 +38,23 @@ def cell_params(n_cells: int, **values) -> np.ndarray:
     return out
 
 
+def shard_cells(cell_n: Sequence[int], rank: int, world: int) -> np.ndarray:
+    """Indices of the cells rank `rank` of `world` owns when independent cells
+    are spread over GPUs (one plan per GPU, no exchange between them): a
+    contiguous range in cell order, cut where the running pair count
+    n (n + 1) / 2 crosses k / world of the total, so every rank gets about
+    the same pair work."""
+    if world < 1 or not (0 <= rank < world):
+        raise ValueError("rank %d outside world %d" % (rank, world))
+    n = np.asarray(cell_n, dtype=np.float64)
+    cost = np.cumsum(n * (n + 1) / 2)
+    total = cost[-1] if len(cost) else 0.0
+    cuts = [0] + [int(np.searchsorted(cost, total * k / world, side="left")) + 1
+                  for k in range(1, world)] + [len(n)]
+    cuts = np.minimum(np.maximum.accumulate(cuts), len(n))
+    return np.arange(cuts[rank], cuts[rank + 1])
+
+
 class BatchPlan:
     """A plan over `cell_n` cells; cell c uses the first cell_n[c] pivots of
     grids[cell_grid[c]]. kernel: AGG_* or -1 (no aggregation); selection:
@@ -86,10 +103,21 @@ class BatchPlan:
         return _lib.load().pbe_batch_rk4(self._h, _ptr(N, "N"), _ptr(params, "params"),
                                          float(dt), int(n_steps), _stream(stream))
 
+    def rk4_prepare(self, N, params, dt: float, n_steps: int) -> int:
+        """Capture the graph rk4() would launch, without running it."""
+        return _lib.load().pbe_batch_rk4_prepare(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                                 float(dt), int(n_steps))
+
     def rk4_percell(self, N, params, dt: float, n_steps: int, stream=None) -> int:
         """The same integration as a per-cell launch loop (baseline)."""
         return _lib.load().pbe_batch_rk4_percell(self._h, _ptr(N, "N"), _ptr(params, "params"),
                                                  float(dt), int(n_steps), _stream(stream))
+
+    def death(self, N, death, params, method: int = _lib.DEATH_MOMENTS, stream=None) -> int:
+        """death[off_c + i] = N_ci sum_k beta_c(x_i, x_k) N_ck (overwritten), by the
+        per-cell moments (DEATH_MOMENTS) or the FP64 tensor-core GEMM (DEATH_DMMA)."""
+        return _lib.load().pbe_batch_death(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                           _ptr(death, "death"), int(method), _stream(stream))
 
     def schedule(self):
         """({class: group size} for the section-count classes present, bundles)."""

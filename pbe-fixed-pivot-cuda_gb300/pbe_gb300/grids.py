@@ -33,11 +33,15 @@ def geometric_params(x: np.ndarray) -> tuple[float, float]:
     return math.log(x[0]), 1.0 / math.log(x[1] / x[0])
 
 
-def lognormal_ic(x: np.ndarray, median_bin: int, sigma_ln: float, total: float) -> np.ndarray:
+def lognormal_ic(x: np.ndarray, median_bin: int, sigma_ln: float, total: float,
+                 cut: float = None) -> np.ndarray:
     """N_i proportional to exp(-(ln x_i - ln x_m)^2 / (2 sigma^2)) dln x, summed to `total`.
-    (On a geometric grid dln x is constant, so it cancels in the normalisation.)"""
+    (On a geometric grid dln x is constant, so it cancels in the normalisation.)
+    cut: N_i = 0 exactly where |ln x_i - ln x_m| > cut sigma."""
     z = (np.log(x) - math.log(x[median_bin])) / sigma_ln
     N = np.exp(-0.5 * z * z)
+    if cut is not None:
+        N = np.where(np.abs(z) <= cut, N, 0.0)
     return N * (total / N.sum())
 
 
@@ -76,7 +80,10 @@ def config_batched_cells(n_cells: int = 4096, seed: int = BATCH_SEED, n_max: int
       a ~ U[0.5, 1.5], x_ref = the cell's middle pivot x[n // 2];
       uniform daughter on Gauss-Legendre 8 points;
       lognormal N (sigma_ln = 1, total `total` m^-3) with median at
-      1e-18 m^3, or at bin n // 4 when the cell's grid ends below that.
+      1e-18 m^3, or at bin n // 4 when the cell's grid ends below that, and
+      exactly 0 beyond 5 sigma: on the coarse grids the upper bins reach
+      volumes whose shear death rate times dt is far beyond RK4's stability
+      limit (2.78), so they must start empty.
     Returns dict(grids, q_values, cell_n, cell_grid, params [n_cells, 8],
     N (packed), t_q, bw_q, seed)."""
     from .batch import cell_params
@@ -96,7 +103,7 @@ def config_batched_cells(n_cells: int = 4096, seed: int = BATCH_SEED, n_max: int
     for g, n in zip(qi, cell_n):
         x = grids[g][:n]
         m = min(int(round(q_values[g] * math.log2(1e-18 / 1e-21))), n // 4)
-        parts.append(lognormal_ic(x, m, 1.0, total))
+        parts.append(lognormal_ic(x, m, 1.0, total, cut=5.0))
     t_q, bw_q = uniform(8)
     return dict(grids=grids, q_values=q_values, cell_n=cell_n.astype(np.int32),
                 cell_grid=qi.astype(np.int32), params=params, N=np.concatenate(parts),
@@ -119,10 +126,7 @@ def config_flocculation_adjoint(n: int = 3840, n_steps: int = 200, switch_step: 
     from .quadrature import power_law
 
     x = geometric_pow2(n, 1e-21, 128.0)
-    m = min(640, n // 4)
-    z = (np.log(x) - math.log(x[m])) / 1.0
-    N0 = np.where(np.abs(z) <= 5.0, np.exp(-0.5 * z * z), 0.0)
-    N0 *= 1e12 / N0.sum()
+    N0 = lognormal_ic(x, min(640, n // 4), 1.0, 1e12, cut=5.0)
     t_q, bw_q = power_law(2.0, 4)
     agg = [AggregationParams(n=n, kernel_type=5, beta0=0.0, beta_br=6.73e-18,
                              beta_sh=4.0 * G / 3.0) for G in (100.0, 20.0)]
@@ -131,3 +135,35 @@ def config_flocculation_adjoint(n: int = 3840, n_steps: int = 200, switch_step: 
     step_set = np.array([0 if s < switch_step else 1 for s in range(n_steps)], dtype=np.int32)
     return dict(x=x, N0=N0, t_q=t_q, bw_q=bw_q, agg_sets=agg, brk_sets=brk, step_set=step_set,
                 dt=0.5, n_steps=n_steps, lam_T=x ** (2.0 / 3.0))
+
+
+def config_batched_classes(n_cells: int = 512, seed: int = BATCH_SEED, width: int = 256,
+                           total: float = 1e13):
+    """Batched forward + adjoint workload with grids shared by size classes:
+    `n_cells` cells (numpy.random.default_rng(seed)), n ~ U[256, 2048]; class
+    k holds n in [256 k, 256 (k+1)) and shares one grid x_i = 1e-21 *
+    2**(i/128) m^3 of 256 (k+1) pivots (class width `width`). Per-cell
+    coefficients lognormal (sigma_ln = 0.5) around beta_br = 6.73e-18 m^3/s,
+    beta_sh = 4 G / 3 with G = 50 1/s, S0 = 1e-3 1/s (power-law selection,
+    a = 1, v_ref = 1e-18 m^3; uniform daughter, 4 Gauss-Legendre points).
+    Lognormal N (median bin n // 4, sigma_ln = 1, total `total` m^-3, 0 beyond
+    5 sigma).
+    Returns dict(grids, cell_n, cell_grid, params, N, t_q, bw_q, seed)."""
+    from .batch import cell_params
+    from .quadrature import uniform
+
+    rng = np.random.default_rng(seed)
+    cell_n = rng.integers(256, 2049, size=n_cells)
+    cls = np.minimum(cell_n // width, 2048 // width)
+    classes = np.unique(cls)
+    grids = [geometric_pow2(int(width * (k + 1)), 1e-21, 128.0) for k in classes]
+    cell_grid = np.searchsorted(classes, cls).astype(np.int32)
+    spread = lambda: np.exp(rng.normal(0.0, 0.5, size=n_cells))  # noqa: E731
+    params = cell_params(n_cells, beta0=0.0, beta_br=6.73e-18 * spread(),
+                         beta_sh=4.0 * 50.0 / 3.0 * spread(), S0=1e-3 * spread(), v_ref=1e-18,
+                         alpha=1.0)
+    N = np.concatenate([lognormal_ic(grids[g][:n], n // 4, 1.0, total, cut=5.0)
+                        for g, n in zip(cell_grid, cell_n)])
+    t_q, bw_q = uniform(4)
+    return dict(grids=grids, cell_n=cell_n.astype(np.int32), cell_grid=cell_grid, params=params,
+                N=N, t_q=t_q, bw_q=bw_q, seed=seed)
