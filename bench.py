@@ -457,8 +457,51 @@ def classes_section(dev, stream):
     }
 
 
+def profile_case(name: str) -> None:
+    """A few launches of one kernel family on a mid-size case, for ncu:
+      batched : 1024 cells of the batched workload (seed 2026), 4 batched RHS
+      death   : the 512-cell size-class workload, 3 DMMA and 3 moment death calls
+      adjoint : the n = 3840 flocculation tape, 10 steps forward + backward"""
+    import torch
+
+    import pbe_gb300 as pg
+
+    dev = torch.device("cuda", 0)
+    f64 = dict(dtype=torch.float64, device=dev)
+    if name == "batched":
+        cfg = pg.grids.config_batched_cells(n_cells=1024)
+        with pg.BatchPlan(cfg["grids"], cfg["cell_n"], cfg["cell_grid"], pg.AGG_BROWNIAN_SHEAR,
+                          pg.SEL_POWERLAW, cfg["t_q"], cfg["bw_q"]) as plan:
+            dN, P = torch.tensor(cfg["N"], **f64), torch.tensor(cfg["params"], **f64)
+            out = torch.zeros(plan.total, **f64)
+            for _ in range(4):
+                pg.check(plan.rhs(dN, out, P), "batch rhs")
+    elif name == "death":
+        cfg = pg.grids.config_batched_classes()
+        with pg.BatchPlan(cfg["grids"], cfg["cell_n"], cfg["cell_grid"], pg.AGG_BROWNIAN_SHEAR,
+                          pg.SEL_POWERLAW, cfg["t_q"], cfg["bw_q"]) as plan:
+            dN, P = torch.tensor(cfg["N"], **f64), torch.tensor(cfg["params"], **f64)
+            out = torch.zeros(plan.total, **f64)
+            for m in (pg.DEATH_DMMA, pg.DEATH_MOMENTS) * 3:
+                pg.check(plan.death(dN, out, P, m), "death")
+    elif name == "adjoint":
+        cfg = pg.grids.config_flocculation_adjoint(n_steps=10, switch_step=5)
+        dx, dtq, dbw = (torch.tensor(cfg[k], **f64) for k in ("x", "t_q", "bw_q"))
+        with pg.Rk4Tape(10, cfg["dt"], 5, cfg["agg_sets"], cfg["brk_sets"], cfg["step_set"]) as tape:
+            N = torch.tensor(cfg["N0"], **f64)
+            pg.check(tape.forward(N, dx, dtq, dbw), "tape forward")
+            g = torch.zeros_like(N)
+            ga, gb = torch.zeros(6, **f64), torch.zeros(8, **f64)
+            pg.check(tape.backward(torch.tensor(cfg["lam_T"], **f64), g, ga, gb), "tape backward")
+    else:
+        raise SystemExit("unknown profile case %r" % name)
+    torch.cuda.synchronize()
+
+
 def main():
     ap_ = argparse.ArgumentParser()
+    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint"],
+                     help="run a few launches of one kernel family (for ncu) and exit")
     ap_.add_argument("--gpus", type=int, default=1)
     ap_.add_argument("--steps", type=int, default=200)
     ap_.add_argument("--warmup", type=int, default=5)
@@ -468,6 +511,9 @@ def main():
     ap_.add_argument("--no-extras", action="store_true",
                      help="skip the batched-cell and adjoint sections")
     args = ap_.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
 
     import torch
 

@@ -30,8 +30,8 @@
 //    geometric grid, per row otherwise).
 //
 // Kernels per call: prep (per-bin values, lag tables, moment partials,
-// geometric check) -> fin (one block: moments, flag, counter reset) -> clip ->
-// main (persistent CTAs pulling target tiles from an atomic counter, largest
+// geometric check) -> clip (clipped pairs; block 0 also finishes moments,
+// flag and counter) -> main (persistent CTAs pulling target tiles from an atomic counter, largest
 // first). GATHER mode: one CTA owns each output bin and reduces it in a fixed
 // order -> bitwise reproducible. SCATTER mode: geometric tasks are (tile, lag
 // chunk) and flush with FP64 atomicAdd.
@@ -118,54 +118,52 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     }
 }
 
-// fin: one block. Moments (fixed-order sums), geometric flag, the first lag
-// whose pairs land on their larger member's own slot (Ld[d] == d), counter reset.
-__global__ void __launch_bounds__(256) agg_fin_kernel(const double* __restrict__ x, int n, AggWs ws)
-{
-    __shared__ double sh[8];
-    __shared__ int d0_s;
-    const int nb = (n + kPrepThreads - 1) / kPrepThreads;
-    if (threadIdx.x == 0) d0_s = n;
-    __syncthreads();
-    int d0 = n;      // smallest lag with Ld[d] == d over the prep blocks
-    for (int b = threadIdx.x; b < nb; b += blockDim.x)
-        d0 = min(d0, static_cast<int>(ws.mom_part[b * 8 + 6]));
-    atomicMin(&d0_s, d0);
-    for (int q = 0; q < 5; ++q) {
-        double s = 0.0;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ws.mom_part[b * 8 + q];
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) ws.mom[q] = s;
-    }
-    double mx = 0.0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) mx = fmax(mx, ws.mom_part[b * 8 + 5]);
-    mx = warp_max(mx);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 0; w < 8; ++w) mx = fmax(mx, sh[w]);
-        // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades
-        // of its bracket pivot (precondition of sum_minus_scaled)
-        const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
-        ws.mom[5] = (n >= 2 && mx <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
-        ws.mom[6] = mx;
-        ws.counter[0] = 0;
-        ws.counter[1] = d0_s;     // lags d >= counter[1] have lo(j, j+d) = j + d
-    }
-}
-
 // clip: sum of rates of the pairs with x_j + x_k >= x[n-1] (all deposited on
 // bin n-1, src/aggregation_kernels.cuh:191-192). One warp per lag d on a
 // geometric grid (pairs j in [n-1-Ld, n-1-d]); one warp per row j otherwise
 // (k from the first clipped column to n-1).
+// Every block first reduces the prep partials' geometric deviation (a few
+// dozen L2 reads) to decide the path; block 0 also finishes the moments
+// (fixed-order sums), the geometric flag, the first lag with Ld[d] == d and
+// the task counter for the main kernel, which runs after this kernel.
 template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kClipWarps * 32)
 agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, double* rhs,
                 int n, AggWs ws, double b0, double bbr, double bsh)
 {
     __shared__ double sh[kClipWarps];
-    const bool geo = ws.mom[5] != 0.0;
+    __shared__ int d0_s;
+    const int nb = (n + kPrepThreads - 1) / kPrepThreads;     // prep blocks
+    double mx = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) mx = fmax(mx, ws.mom_part[b * 8 + 5]);
+    mx = warp_max(mx);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+    if (threadIdx.x == 0) d0_s = n;
+    __syncthreads();
+    mx = 0.0;
+    for (int w2 = 0; w2 < kClipWarps; ++w2) mx = fmax(mx, sh[w2]);
+    // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
+    // its bracket pivot (precondition of sum_minus_scaled)
+    const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
+    if (blockIdx.x == 0) {
+        int d0 = n;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x)
+            d0 = min(d0, static_cast<int>(ws.mom_part[b * 8 + 6]));
+        atomicMin(&d0_s, d0);
+        for (int q = 0; q < 5; ++q) {
+            double t = 0.0;
+            for (int b = threadIdx.x; b < nb; b += blockDim.x) t += ws.mom_part[b * 8 + q];
+            t = block_sum(t, sh);
+            if (threadIdx.x == 0) ws.mom[q] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            ws.mom[5] = geo ? 1.0 : 0.0;
+            ws.mom[6] = mx;
+            ws.counter[0] = 0;
+            ws.counter[1] = d0_s;     // lags d >= counter[1] have lo(j, j+d) = j + d
+        }
+    }
     const int w = blockIdx.x * kClipWarps + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     double acc = 0.0;
@@ -328,7 +326,6 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
-    agg_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
     agg_clip_kernel<K, SC><<<nbc, kClipWarps * 32, 0, s>>>(a.N, a.x, a.rhs, n, ws, a.beta0,
                                                           a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;

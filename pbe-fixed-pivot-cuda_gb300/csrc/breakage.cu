@@ -12,10 +12,10 @@
 // GATHER (deterministic): one thread per fragment (q, j) computes its bracket
 // and its two shares; since v = x_j t_q grows with j, the fragments of one q
 // landing on bracket m form a contiguous run of j, whose first index is
-// recorded in first[q][m]. One warp per output bin i then adds, in a fixed
-// order, for every q the hi-shares of bracket i-1 and the lo-shares of
-// bracket i (bin 0 also takes the fragments clipped below x[0]) and finally
-// the death term -S_i N_i.
+// recorded in first[q][m]. The gather kernel then gives each output bin i a
+// segment of lanes, one per quadrature point, which add in a fixed order the
+// hi-shares of bracket i-1 and the lo-shares of bracket i (bin 0 also takes
+// the fragments clipped below x[0]), then the death term -S_i N_i.
 // SCATTER: one thread per fragment adds its shares with FP64 atomicAdd.
 // =============================================================================
 #include "pbe_internal.cuh"
@@ -65,31 +65,53 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
 }
 
-// One warp per output bin: the lanes stride over the fragment runs (bin 0 can
-// collect every fragment clipped below x[0], thousands per quadrature point),
-// then a fixed butterfly sums the lanes -> deterministic.
+// Output bins in groups of 32/nqp per warp, nqp = n_quad rounded up to a power
+// of two (<= 32): lane l works on bin base + l / nqp and quadrature points
+// q = l % nqp (+ nqp, ...), walking that q's few fragments of brackets i-1 and
+// i; a fixed butterfly over the nqp lanes sums them. Bin 0 also collects every
+// fragment clipped below x[0] (up to thousands per q on fine grids): the
+// warp holding bin 0 sums those first, all 32 lanes striding over them.
 __global__ void __launch_bounds__(256)
 brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 {
-    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int nqp = 1;
+    while (nqp < nq && nqp < 32) nqp <<= 1;
+    const int per_warp = 32 / nqp;
+    const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (i >= n) return;                      // whole warp
-    double acc = 0.0;
-    for (int q = 0; q < nq; ++q) {
-        const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-        const double* clo = ws.clo + static_cast<long long>(q) * n;
-        const double* chi = ws.chi + static_cast<long long>(q) * n;
-        // clamp: entries are in [0, n] for monotone brackets (t_q > 0)
-        const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
-        const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
-        const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
-        if (i == 0) { for (int j = lane; j < fb; j += 32) acc += clo[j]; }       // lo == -1
-        else        { for (int j = fa + lane; j < fb; j += 32) acc += chi[j]; }  // lo == i-1
-        for (int j = fb + lane; j < fc; j += 32) acc += clo[j];                  // lo == i
-    }
+    const int base = warp * per_warp;
+    if (base >= n) return;                   // whole warp
+    double clipped = 0.0;
+    if (base == 0) {
+        for (int q = 0; q < nq; ++q) {
+            const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+            const double* clo = ws.clo + static_cast<long long>(q) * n;
+            const int fb = min(max(fq[1], 0), n);       // fragments with lo == -1
+            for (int j = lane; j < fb; j += 32) clipped += clo[j];
+        }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) rhs[i] = (rhs[i] - ws.SN[i]) + acc;
+        for (int o = 16; o > 0; o >>= 1) clipped += __shfl_xor_sync(0xffffffffu, clipped, o);
+    }
+    const int i = base + lane / nqp;
+    double acc = 0.0;
+    if (i < n) {
+        for (int q = lane % nqp; q < nq; q += nqp) {
+            const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+            const double* clo = ws.clo + static_cast<long long>(q) * n;
+            const double* chi = ws.chi + static_cast<long long>(q) * n;
+            // clamp: entries are in [0, n] for monotone brackets (t_q > 0)
+            const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
+            const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
+            const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
+            if (i > 0) for (int j = fa; j < fb; ++j) acc += chi[j];   // lo == i-1
+            for (int j = fb; j < fc; ++j) acc += clo[j];              // lo == i
+        }
+    }
+    for (int o = nqp >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (i < n && (lane % nqp) == 0) {
+        if (i == 0) acc += clipped;
+        rhs[i] = (rhs[i] - ws.SN[i]) + acc;
+    }
 }
 
 template <int F>
@@ -129,7 +151,10 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
         brk_ws_layout(a.n, a.n_quad, static_cast<char*>(ws_base), &ws);
         brk_prep_kernel<F><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n, a.n_quad, ws, a.S0,
                                                 a.v_ref, a.alpha, a.v_min);
-        brk_gather_kernel<<<(a.n + 7) / 8, 256, 0, s>>>(a.rhs, a.n, a.n_quad, ws);
+        int nqp = 1;
+        while (nqp < a.n_quad && nqp < 32) nqp <<= 1;
+        const int per_block = 8 * (32 / nqp);               // bins per 256-thread block
+        brk_gather_kernel<<<(a.n + per_block - 1) / per_block, 256, 0, s>>>(a.rhs, a.n, a.n_quad, ws);
     }
     return cudaGetLastError();
 }
