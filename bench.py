@@ -430,6 +430,29 @@ def classes_section(dev, stream):
         torch.cuda.synchronize()
         graph_ms = a.elapsed_time(b)
         finite = bool(torch.isfinite(Y).all())
+        # adjoint: L = 1/2 |N(T) - N*(T)|^2, N* from coefficients perturbed by 5 %
+        Pstar = P.clone()
+        Pstar[:, 1] *= 1.05
+        Pstar[:, 2] *= 0.95
+        Nstar = dN.clone()
+        pg.check(plan.rk4(Nstar, Pstar, 0.5, steps, stream=stream), "target run")
+        gN0 = torch.zeros(plan.total, **f64)
+        gP = torch.zeros((len(cfg["cell_n"]), 8), **f64)
+        NT = dN.clone()
+        pg.check(plan.tape_forward(NT, P, 0.5, steps, 20, stream=stream), "tape forward warm-up")
+        pg.check(plan.tape_backward(NT - Nstar, gN0, gP, stream=stream), "tape backward warm-up")
+        NT = dN.clone()
+        c_ = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        pg.check(plan.tape_forward(NT, P, 0.5, steps, 20, stream=stream), "tape forward")
+        b.record(stream)
+        lamT = NT - Nstar
+        pg.check(plan.tape_backward(lamT, gN0, gP, stream=stream), "tape backward")
+        c_.record(stream)
+        torch.cuda.synchronize()
+        tape_fwd_ms, tape_bwd_ms = a.elapsed_time(b), b.elapsed_time(c_)
+        grad_finite = bool(torch.isfinite(gN0).all()) and bool(torch.isfinite(gP).all())
     plan.close()
     cn = cfg["cell_n"].astype(np.float64)
     gemm_flops = float((2.0 * cn * cn).sum() * 2)          # two separable components
@@ -442,6 +465,12 @@ def classes_section(dev, stream):
         "cell_steps_per_s": round(len(cn) * steps / (graph_ms / 1e3), 1),
         "graph_ms_100_steps": round(graph_ms, 2),
         "finite_after_100_steps": finite,
+        "adjoint": {"what": "L = 1/2 |N(T) - N*(T)|^2 after 100 RK4 steps, N* from beta_br x 1.05 "
+                            "and beta_sh x 0.95; batched checkpointed tape (every 20 steps): "
+                            "dL/dN(0) and dL/d(7 coefficients) of all 512 cells",
+                    "forward_ms": round(tape_fwd_ms, 2), "backward_ms": round(tape_bwd_ms, 2),
+                    "backward_forward_ratio": round(tape_bwd_ms / tape_fwd_ms, 4),
+                    "gradient_finite": grad_finite},
         "death_moments_ms": round(times[pg.DEATH_MOMENTS], 4),
         "death_dmma_ms": round(times[pg.DEATH_DMMA], 4),
         "dmma_over_moments_time": round(times[pg.DEATH_DMMA] / times[pg.DEATH_MOMENTS], 2),

@@ -254,6 +254,27 @@ enum { PBE_DEATH_MOMENTS = 0, PBE_DEATH_DMMA = 1 };
 int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_params_t* params,
                     double* death, int method, void* stream);
 
+/* Vector-Jacobian product of the batched RHS: for L = sum over cells of
+ * lambda . rhs(N), gN += dL/dN (packed like N) and
+ * gparams[8 c + j] += dL/d(parameter j of cell c), j = beta0, beta_br,
+ * beta_sh, S0, v_ref, alpha, v_min (0: threshold step), 7 unused. Same
+ * formulas as pbe_aggregation_rhs_vjp / pbe_breakage_rhs_vjp per cell;
+ * bitwise reproducible for one plan. */
+int pbe_batch_rhs_vjp(pbe_batch_t plan, const double* N, const double* lambda, double* gN,
+                      double* gparams, const pbe_batch_cell_params_t* params, void* stream);
+
+/* Checkpointed RK4 adjoint of every cell of a plan (the batched form of
+ * pbe_rk4_tape_*). Forward: n_steps RK4 steps in place on N (N(0) -> N(T)),
+ * saving N every checkpoint_every steps in plan-owned memory (grown on first
+ * use: (n_steps / every + 4 every + 5) packed vectors). Backward, given
+ * lambda_T = dL/dN(T) (packed): gN0 = dL/dN(0) and gparams[8 c + j] =
+ * dL/d(parameter j of cell c) over the whole run (both overwritten). params
+ * (device) must stay unchanged between the two calls. */
+int pbe_batch_tape_forward(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                           double dt, int n_steps, int checkpoint_every, void* stream);
+int pbe_batch_tape_backward(pbe_batch_t plan, const double* lambda_T, double* gN0,
+                            double* gparams, void* stream);
+
 /* Schedule in use: group_size[c] (16 entries) = threads per tile task for
  * cells with floor(log2(n)) == c (0 where no cell falls), *n_bundles = the
  * number of bundles in the persistent launch. Either pointer may be NULL. */
@@ -290,6 +311,26 @@ int pbe_rk4_tape_forward(pbe_rk4_tape_t tape, double* N, const double* x, const 
  * NULL for an absent term). Returns cudaErrorInvalidValue before a forward. */
 int pbe_rk4_tape_backward(pbe_rk4_tape_t tape, const double* lambda_T, double* gN0,
                           double* g_agg, double* g_brk, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Daughter tables for the breakage calls (host function, no GPU involved;
+ * the reference documents the convention -- fragment volume t_q x_j, bw_q
+ * fragments per event, include/pbe_cuda/breakage.cuh:43-50 -- but builds the
+ * tables by hand in its examples and has no power-law table):
+ *   PBE_DAUGHTER_SYMMETRIC  t = {1/2}, bw = {2}                      (1 entry)
+ *   PBE_DAUGHTER_EROSION    t = {1 - param, param}, bw = {1, 1}      (2 entries)
+ *   PBE_DAUGHTER_UNIFORM    Gauss-Legendre on (0, 1), bw = 2 w       (order entries)
+ *   PBE_DAUGHTER_POWERLAW   b(v|v') = (p+2) v^p / v'^(p+1), p = param > -1:
+ *                           Gauss-Legendre on (0, s) and (s, 1), s = param2
+ *                           (0 means 1/2), bw = (p+2) t^p w     (2 order entries)
+ * Writes at most `capacity` entries to t_q / bw_q (host arrays) and the count
+ * to *n_quad; with t_q or bw_q NULL and capacity 0 it only reports the count.
+ * Returns 0, or 1 (cudaErrorInvalidValue) for a bad kind, order, parameter or
+ * a too small capacity. */
+enum { PBE_DAUGHTER_SYMMETRIC = 0, PBE_DAUGHTER_EROSION = 1, PBE_DAUGHTER_UNIFORM = 2,
+       PBE_DAUGHTER_POWERLAW = 3 };
+int pbe_daughter_table(int kind, int order, double param, double param2, double* t_q,
+                       double* bw_q, int capacity, int* n_quad);
 
 /* Human-readable name of a return code (cudaGetErrorString). */
 const char* pbe_error_string(int code);

@@ -30,7 +30,8 @@ ORACLE_LIB = os.path.join(ORACLE_BUILD, "liboracle.so")
 REF_RUNNER_LIB = os.path.join(ORACLE_BUILD, "libref_runner.so")
 
 SOURCES = ["aggregation.cu", "breakage.cu", "vjp.cu", "api.cu", "noalloc.cu",
-           "batch_kernels.cu", "batch.cu", "adjoint.cu", "death_gemm.cu"]
+           "batch_kernels.cu", "batch.cu", "adjoint.cu", "death_gemm.cu",
+           "batch_vjp.cu", "daughter.cpp"]
 ARCH = ["-gencode=arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
 
@@ -66,7 +67,7 @@ def _headers() -> list[str]:
 
 
 def build_library(force: bool = False) -> str:
-    """Compile csrc/*.cu for sm_103a and link lib/libpbe_gb300.so."""
+    """Compile the csrc sources (CUDA for sm_103a, host C++) and link lib/libpbe_gb300.so."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = os.path.join(_cuda_home(), "bin", "nvcc")
@@ -75,7 +76,7 @@ def build_library(force: bool = False) -> str:
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or not _newer(o, [s] + hdrs):
             jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])

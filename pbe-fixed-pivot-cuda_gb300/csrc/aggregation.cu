@@ -134,18 +134,16 @@ agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, doub
     __shared__ double sh[kClipWarps];
     __shared__ int d0_s;
     const int nb = (n + kPrepThreads - 1) / kPrepThreads;     // prep blocks
+    // every warp reduces the deviation partials itself (no block barrier)
     double mx = 0.0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) mx = fmax(mx, ws.mom_part[b * 8 + 5]);
+    for (int b = threadIdx.x & 31; b < nb; b += 32) mx = fmax(mx, ws.mom_part[b * 8 + 5]);
     mx = warp_max(mx);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
-    if (threadIdx.x == 0) d0_s = n;
-    __syncthreads();
-    mx = 0.0;
-    for (int w2 = 0; w2 < kClipWarps; ++w2) mx = fmax(mx, sh[w2]);
     // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
     // its bracket pivot (precondition of sum_minus_scaled)
     const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
     if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) d0_s = n;
+        __syncthreads();
         int d0 = n;
         for (int b = threadIdx.x; b < nb; b += blockDim.x)
             d0 = min(d0, static_cast<int>(ws.mom_part[b * 8 + 6]));

@@ -53,6 +53,18 @@ struct pbe_batch_plan {
     int4* d_death_items = nullptr;
     int* d_gcells = nullptr;
     int n_death_items = -1;
+    // batched VJP (set up on first use)
+    bool vjp_ready = false;
+    pbe_gb300::BatchVjpDev vd{};
+    // batched RK4 tape (allocated on first use, grown as needed)
+    double* t_ckpt = nullptr;
+    double* t_segY = nullptr;
+    double* t_work = nullptr;          // tN, lam, lsum, a, mu
+    size_t t_ckpt_cap = 0, t_seg_cap = 0;
+    bool t_recorded = false;
+    int t_steps = 0, t_every = 1;
+    double t_dt = 0.0;
+    const pbe_batch_cell_params_t* t_params = nullptr;
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -134,15 +146,18 @@ long long task_cost(int n, int I, int T)
 
 // Bundles for the cells of the classes selected by `want` (all when null),
 // each class with its group size gs[class]; sorted by work, largest first.
+// vjp: row tiles of the VJP, whose work does not depend on the first row (every
+// row meets all n partners).
 void build_schedule(const pbe_batch_plan& p, const int* gs, const bool* want,
-                    std::vector<int4>& bundles, std::vector<int2>& tasks)
+                    std::vector<int4>& bundles, std::vector<int2>& tasks, bool vjp = false)
 {
     std::vector<std::vector<HostTask>> per(kClasses);
     for (int c = 0; c < p.n_cells; ++c) {
         const int n = p.cell_n[c];
         const int cls = n_class(n);
         if (want && !want[cls]) continue;
-        for (int I = 0; I < n; I += W) per[cls].push_back({c, I, task_cost(n, I, gs[cls])});
+        for (int I = 0; I < n; I += W)
+            per[cls].push_back({c, I, task_cost(n, vjp ? n : I, gs[cls])});
     }
     struct B { long long cost; int cls; int first; int cnt; };
     std::vector<B> bl;
@@ -376,6 +391,7 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     if (e == cudaSuccess) e = plan_alloc(p, &d.bfirst, static_cast<size_t>(foff));
     if (e == cudaSuccess) e = plan_alloc(p, &d.bwlo, static_cast<size_t>(woff));
     if (e == cudaSuccess) e = plan_alloc(p, &d.bwhi, static_cast<size_t>(woff));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.blo, static_cast<size_t>(woff));
     if (e == cudaSuccess) e = plan_alloc(p, &d.Y, C);
     if (e == cudaSuccess) e = plan_alloc(p, &d.Nj, C);
     if (e == cudaSuccess) e = plan_alloc(p, &d.Hj, C);
@@ -558,6 +574,146 @@ cudaError_t rk4_percell(pbe_batch_plan* p, double* N, const pbe_batch_cell_param
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
+cudaError_t vjp_setup(pbe_batch_plan* p, cudaStream_t s)
+{
+    if (p->vjp_ready) return cudaSuccess;
+    BatchVjpDev& vd = p->vd;
+    const size_t C = static_cast<size_t>(p->total);
+    std::vector<int> tile_off(static_cast<size_t>(p->n_cells) + 1, 0);
+    for (int c = 0; c < p->n_cells; ++c) tile_off[c + 1] = tile_off[c] + (p->cell_n[c] + W - 1) / W;
+    std::vector<int4> b;
+    std::vector<int2> t;
+    build_schedule(*p, p->group_size, nullptr, b, t, true);
+    int* dto = nullptr;
+    int4* db = nullptr;
+    int2* dt = nullptr;
+    cudaError_t e = plan_alloc(p, &vd.h, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &vd.D, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &vd.mom, static_cast<size_t>(p->n_cells) * 16);
+    if (e == cudaSuccess) e = plan_alloc(p, &vd.tpart, 2 * static_cast<size_t>(tile_off.back()));
+    if (e == cudaSuccess) e = plan_alloc(p, &dto, tile_off.size());
+    if (e == cudaSuccess) e = plan_alloc(p, &vd.counter, 8);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dto, tile_off.data(), tile_off.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = upload_schedule(p, b, t, &db, &dt, s);
+    if (e == cudaSuccess) e = batch_vjp_setup(p->kernel);
+    if (e != cudaSuccess) return e;
+    vd.tile_off = dto;
+    vd.bundles = db;
+    vd.tasks = dt;
+    vd.n_bundles = static_cast<int>(b.size());
+    p->vjp_ready = true;
+    return cudaSuccess;
+}
+
+// Batched RK4 steps [s0, s1) on N (the plan's stage machinery). first:
+// stage 1 of step s0 evaluates at N as given (else it first closes the
+// previous step). ckpt: N at every step multiple of `every` is copied to
+// ckpt[step / every]. Ys: the stage states of every step are copied to
+// Ys[((step - s0) * 4 + q) * total]. finish: close the last step.
+cudaError_t run_steps(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
+                      int s0, int s1, bool first, double* ckpt, int every, double* Ys,
+                      bool finish, cudaStream_t s)
+{
+    const BatchDev& d = p->d;
+    const double h = 0.5 * dt, dt6 = dt / 6.0;
+    const size_t C = static_cast<size_t>(p->total), bytes = C * sizeof(double);
+    cudaError_t e = cudaSuccess;
+    for (int st = s0; st < s1 && e == cudaSuccess; ++st) {
+        double* Y = Ys ? Ys + static_cast<size_t>(st - s0) * 4 * C : nullptr;
+        e = batch_prep(d, N, prm, (st == s0 && first) ? kStageRhs : kStageNext, 0.0, dt6, s);
+        if (e == cudaSuccess && ckpt && st % every == 0)
+            e = cudaMemcpyAsync(ckpt + static_cast<size_t>(st / every) * C, N, bytes,
+                                cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess && Y) e = cudaMemcpyAsync(Y, N, bytes, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = batch_main(d, N, prm, d.k, false, s);
+        const double cs[3] = {h, h, dt};
+        for (int q = 1; q < 4 && e == cudaSuccess; ++q) {
+            e = batch_prep(d, N, prm, q == 1 ? kStageTwo : kStageThree, cs[q - 1], dt6, s);
+            if (e == cudaSuccess && Y)
+                e = cudaMemcpyAsync(Y + q * C, d.Y, bytes, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess && (q < 3 || finish || st + 1 < s1))
+                e = batch_main(d, d.Y, prm, d.k, false, s);
+        }
+    }
+    if (e == cudaSuccess && finish) e = batch_prep(d, N, prm, kStageFinish, 0.0, dt6, s);
+    return e;
+}
+
+cudaError_t tape_forward(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
+                         double dt, int n_steps, int every, cudaStream_t s)
+{
+    const size_t C = static_cast<size_t>(p->total);
+    const size_t nck = static_cast<size_t>((n_steps + every - 1) / every);
+    const size_t seg = static_cast<size_t>(std::min(every, n_steps));
+    cudaError_t e = vjp_setup(p, s);
+    if (e != cudaSuccess) return e;
+    if (!p->t_work) {
+        e = plan_alloc(p, &p->t_work, 5 * C);
+        if (e != cudaSuccess) return e;
+    }
+    if (nck * C > p->t_ckpt_cap) {
+        e = plan_alloc(p, &p->t_ckpt, nck * C);
+        if (e != cudaSuccess) return e;
+        p->t_ckpt_cap = nck * C;
+    }
+    if (4 * seg * C > p->t_seg_cap) {
+        e = plan_alloc(p, &p->t_segY, 4 * seg * C);
+        if (e != cudaSuccess) return e;
+        p->t_seg_cap = 4 * seg * C;
+    }
+    p->t_recorded = false;
+    e = run_steps(p, N, prm, dt, 0, n_steps, true, p->t_ckpt, every, nullptr, true, s);
+    if (e != cudaSuccess) return e;
+    p->t_recorded = true;
+    p->t_steps = n_steps;
+    p->t_every = every;
+    p->t_dt = dt;
+    p->t_params = prm;
+    return cudaSuccess;
+}
+
+cudaError_t tape_backward(pbe_batch_plan* p, const double* lamT, double* gN0, double* gp,
+                          cudaStream_t s)
+{
+    const size_t C = static_cast<size_t>(p->total), bytes = C * sizeof(double);
+    const long long nC = static_cast<long long>(C);
+    double* tN = p->t_work;
+    double* lam = p->t_work + C;
+    double* lsum = p->t_work + 2 * C;
+    double* a = p->t_work + 3 * C;
+    double* mu = p->t_work + 4 * C;
+    const double dt = p->t_dt, h = 0.5 * dt, c6 = dt / 6.0;
+    const double cs[3] = {h, h, dt};
+    const pbe_batch_cell_params_t* prm = p->t_params;
+    cudaError_t e = cudaMemcpyAsync(lam, lamT, bytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(gp, 0, sizeof(double) * 8 * static_cast<size_t>(p->n_cells), s);
+    const int every = p->t_every;
+    const int nseg = (p->t_steps + every - 1) / every;
+    for (int g = nseg - 1; g >= 0 && e == cudaSuccess; --g) {
+        const int s0 = g * every, s1 = std::min(s0 + every, p->t_steps);
+        e = cudaMemcpyAsync(tN, p->t_ckpt + static_cast<size_t>(g) * C, bytes,
+                            cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = run_steps(p, tN, prm, dt, s0, s1, true, nullptr, every, p->t_segY, false, s);
+        for (int st = s1 - 1; st >= s0 && e == cudaSuccess; --st) {
+            const double* Ys = p->t_segY + static_cast<size_t>(st - s0) * 4 * C;
+            e = cudaMemcpyAsync(lsum, lam, bytes, cudaMemcpyDeviceToDevice, s);
+            for (int q = 3; q >= 0 && e == cudaSuccess; --q) {
+                const double w = (q == 0 || q == 3) ? c6 : 2.0 * c6;
+                e = batch_adj_coeff(a, lam, mu, w, q < 3 ? cs[q] : 0.0, nC, q == 3, s);
+                if (e == cudaSuccess) e = batch_vjp(p->d, p->vd, Ys + q * C, a, mu, gp, prm, s);
+                if (e == cudaSuccess) e = batch_adj_sum(lsum, mu, nC, s);
+            }
+            std::swap(lam, lsum);
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(gN0, lam, bytes, cudaMemcpyDeviceToDevice, s);
+    return e;
+}
+
 // Work items of the death GEMM: the cells of each grid, largest first, in
 // row tiles of 64; each row tile covers the bins below its largest n in
 // column tiles of 64.
@@ -694,6 +850,39 @@ int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_para
     }
     return batch_death(plan->d, N, params, death, method, plan->d_death_items,
                        plan->n_death_items, plan->d_gcells, s);
+}
+
+int pbe_batch_rhs_vjp(pbe_batch_t plan, const double* N, const double* lambda, double* gN,
+                      double* gparams, const pbe_batch_cell_params_t* params, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !lambda || !gN || !gparams || !params) return cudaErrorInvalidDevicePointer;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    e = vjp_setup(plan, s);
+    if (e != cudaSuccess) return e;
+    return batch_vjp(plan->d, plan->vd, N, lambda, gN, gparams, params, s);
+}
+
+int pbe_batch_tape_forward(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                           double dt, int n_steps, int checkpoint_every, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (n_steps <= 0 || checkpoint_every <= 0 || !std::isfinite(dt)) return cudaErrorInvalidValue;
+    return tape_forward(plan, N, params, dt, n_steps, checkpoint_every,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_tape_backward(pbe_batch_t plan, const double* lambda_T, double* gN0,
+                            double* gparams, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!plan->t_recorded) return cudaErrorInvalidValue;
+    if (!lambda_T || !gN0 || !gparams) return cudaErrorInvalidDevicePointer;
+    return tape_backward(plan, lambda_T, gN0, gparams, static_cast<cudaStream_t>(stream));
 }
 
 int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)

@@ -47,6 +47,7 @@ struct BatchDev {
     // lo(q, j) >= m; bwlo / bwhi[woff + q n + j] = bw_q times the shares of the
     // fragment x_j t_q at lo and lo + 1 (all of bw_q at lo when clipped)
     int* bfirst; double* bwlo; double* bwhi;
+    int* blo;       // bracket of fragment (q, j) (-1: below x[0]), same index as bwlo
     // per cell bin (packed by BatchCellDev::off), rewritten every stage
     double* Y;      // stage state (the RHS argument)
     double* Nj;     // j-side N factor: beta N (beta0, beta_br)
@@ -63,6 +64,19 @@ struct BatchDev {
     const int2* tasks;     // {cell, first bin}
     int n_bundles;
     int num_sms;
+};
+
+// Scratch of the batched VJP (batch_vjp.cu).
+struct BatchVjpDev {
+    double* h;             // x N per cell bin
+    double* D;             // lambda slopes per cell bin
+    double* mom;           // [n_cells * 16]: moments of N (0..4) and of lambda N (5..9)
+    double* tpart;         // [2 * tiles]: parameter partials per row tile
+    const int* tile_off;   // [n_cells + 1]: first row-tile slot of each cell
+    const int4* bundles;   // row-tile bundles {first task, tasks, group size, 0}
+    const int2* tasks;     // {cell, first row}
+    int n_bundles;
+    int* counter;
 };
 
 // Stage modes of the per-cell prep kernel (RK4 as the reference examples
@@ -100,6 +114,16 @@ cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
 cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
                         double* out, int method, const int4* items, int n_items,
                         const int* gcells, cudaStream_t s);
+// Batched VJP: gN += dL/dN, gparams[8 c + j] += dL/d(parameter j of cell c)
+// for L = lambda . RHS(N) (batch_vjp.cu). batch_vjp_setup once per plan.
+cudaError_t batch_vjp_setup(int kernel);
+cudaError_t batch_vjp(const BatchDev& d, const BatchVjpDev& vd, const double* N, const double* lam,
+                      double* gN, double* gparams, const pbe_batch_cell_params_t* params,
+                      cudaStream_t s);
+// Adjoint stage helpers over n packed entries: a = w lp (+ c mu), mu = 0; lsum += mu.
+cudaError_t batch_adj_coeff(double* a, const double* lp, double* mu, double w, double c,
+                            long long n, bool first, cudaStream_t s);
+cudaError_t batch_adj_sum(double* lsum, const double* mu, long long n, cudaStream_t s);
 // Per-cell RK4 stage update for the per-cell launch loop (one cell, n bins).
 cudaError_t cell_stage(double* N, const double* k, double* kacc, double* Y, int n, int stage,
                        double c, double dt6, cudaStream_t s);

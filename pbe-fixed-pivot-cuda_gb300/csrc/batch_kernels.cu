@@ -110,6 +110,7 @@ batch_frag_kernel(BatchDev d, const double* __restrict__ t_q, const double* __re
         }
         d.bwlo[gd.woff + q * n + j] = wl;
         d.bwhi[gd.woff + q * n + j] = wh;
+        d.blo[gd.woff + q * n + j] = lo;
         int* fq = d.bfirst + gd.foff + q * (n + 2);
         const int lo_prev = (j == 0) ? -2 : frag_bracket(x, n, x[j - 1] * tq);
         for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;

@@ -74,24 +74,27 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
 __global__ void __launch_bounds__(256)
 brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 {
+    __shared__ double sh[8];
     int nqp = 1;
     while (nqp < nq && nqp < 32) nqp <<= 1;
     const int per_warp = 32 / nqp;
     const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     const int base = warp * per_warp;
-    if (base >= n) return;                   // whole warp
+    // fragments clipped below x[0] (all deposited on bin 0): block 0 sums them
+    // with all its threads, q by q, in a fixed order
     double clipped = 0.0;
-    if (base == 0) {
+    if (blockIdx.x == 0) {
+        double part = 0.0;
         for (int q = 0; q < nq; ++q) {
             const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
             const double* clo = ws.clo + static_cast<long long>(q) * n;
             const int fb = min(max(fq[1], 0), n);       // fragments with lo == -1
-            for (int j = lane; j < fb; j += 32) clipped += clo[j];
+            for (int j = threadIdx.x; j < fb; j += blockDim.x) part += clo[j];
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) clipped += __shfl_xor_sync(0xffffffffu, clipped, o);
+        clipped = block_sum(part, sh);
     }
+    if (base >= n) return;                   // whole warp
     const int i = base + lane / nqp;
     double acc = 0.0;
     if (i < n) {

@@ -25,13 +25,12 @@
 // (PowerLaw: dS/dalpha = S ln(x/v_ref)), dL/dv_min = 0 (threshold step).
 // =============================================================================
 #include "pbe_internal.cuh"
-#include "exact_weight.cuh"
+#include "vjp_tile.cuh"
 
 namespace pbe_gb300 {
 namespace {
 
-constexpr int VW = kTileW;              // rows per task
-constexpr int kVRows = 3 * VW;          // three accumulators per row
+constexpr int VW = kVW;                 // rows per task
 
 // dL/dN needs, per kernel type K, up to three row sums (see vjp_main_kernel):
 //   K=0: R0 = sum P N_k                       f = 1
@@ -124,17 +123,6 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
     }
 }
 
-// sum_k f(m,k) N_k (or lambda_k N_k) from the moments mo[0..4].
-template <int K, int X>   // X: 0 = beta0 / Brownian part, 1 = shear part
-__device__ __forceinline__ double moment_factor(double xm, double am, double iam, const double* mo)
-{
-    if constexpr (K == 0) return mo[1];
-    else if constexpr (K == 1) return fma(xm, mo[1], mo[4]);
-    else if constexpr (K == 2) return xm * mo[4];
-    else if constexpr (X == 0) return fma(am, mo[0], iam * mo[2]) + 2.0 * mo[1];
-    else return fma(xm, mo[1], (3.0 * am) * fma(am, mo[2], mo[3])) + mo[4];
-}
-
 template <int K>
 __global__ void __launch_bounds__(kMainThreads, 2)
 vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
@@ -142,14 +130,16 @@ vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 int ntile, double b0, double bbr, double bsh)
 {
     extern __shared__ double red[];               // [kVRows][kMainThreads]
-    __shared__ double part4[4][kVRows];
-    __shared__ double fin[kVRows];
-    __shared__ double gsh[VW][2];
+    __shared__ VjpShared sm;
     __shared__ int s_task;
 
     const int tid = threadIdx.x;
-    const bool geo = ws.mom[10] != 0.0;
-    const double lamlast = lam[n - 1];
+    VjpCellView v;
+    v.x = x; v.N = N; v.h = ws.h; v.lam = lam; v.D = ws.D; v.a = ws.a; v.ia = ws.ia;
+    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Ld = ws.Ld; v.lag0_scale = 1.0;
+    v.n = n;
+    v.geo = ws.mom[10] != 0.0;
+    const TileGroup G{0, tid, kMainThreads};
 
     for (;;) {
         if (tid == 0) s_task = atomicAdd(ws.counter, 1);
@@ -158,179 +148,23 @@ vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         __syncthreads();
         if (task >= ntile) break;
         const int I = task * VW;
-        const int tmax = min(VW, n - I);          // rows I .. I+tmax-1
-
-        double R0[VW], R1[VW], R2[VW];
-#pragma unroll
-        for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; R2[t] = 0.0; }
-
-        if (geo) {
-            for (int d = tid; d < n; d += kMainThreads) {
-                const int L = __ldg(ws.Ld + d);
-                const double Bf = __ldg(ws.Bf + d), Sf = __ldg(ws.Sf + d);
-                // upper visits: partner k = m + d
-#pragma unroll
-                for (int t = 0; t < VW; ++t) {
-                    const int m = I + t, k = m + d;
-                    if (t < tmax && k < n) {
-                        const double Nk = __ldg(N + k);
-                        const int lo = (L >= kLagClipAll) ? n : m + L;
-                        double P;
-                        if (lo >= n - 1) {
-                            P = lamlast;
-                        } else {
-                            const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + m),
-                                                               __ldg(x + lo), 0);
-                            P = fma(th, __ldg(ws.D + lo), __ldg(lam + lo));
-                        }
-                        if constexpr (K == 2) {
-                            R0[t] = fma(P, __ldg(ws.h + k), R0[t]);
-                        } else {
-                            const double t1 = P * Nk;
-                            if constexpr (K == 0) R0[t] += t1;
-                            if constexpr (K == 1) { R0[t] += t1; R1[t] = fma(P, __ldg(ws.h + k), R1[t]); }
-                            if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
-                            if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sf, R1[t]);
-                        }
-                    }
-                }
-                // lower visits: partner k = m - d (d >= 1)
-                if (d >= 1 && L < kLagClipAll) {
-                    const int e = L - d;
-#pragma unroll
-                    for (int t = 0; t < VW; ++t) {
-                        const int m = I + t, k = m - d;
-                        if (t < tmax && k >= 0) {
-                            const int lo = m + e;
-                            double P;
-                            if (lo >= n - 1) {
-                                P = lamlast;
-                            } else {
-                                const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
-                                                                   __ldg(x + lo), 0);
-                                P = fma(th, __ldg(ws.D + lo), __ldg(lam + lo));
-                            }
-                            if constexpr (K == 2) {
-                                R0[t] = fma(P, __ldg(ws.h + k), R0[t]);
-                            } else {
-                                const double Nk = __ldg(N + k);
-                                if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
-                                if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(ws.h + k), R1[t]); }
-                                if constexpr (K == 3 || K == 5) R0[t] = fma(P * Nk, Bf, R0[t]);
-                                if constexpr (K == 4 || K == 5) R2[t] = fma(P * __ldg(ws.h + k), Sf, R2[t]);
-                            }
-                        }
-                    }
-                } else if (d >= 1) {
-                    // every pair of this lag is clipped: P = lambda_{n-1}
-#pragma unroll
-                    for (int t = 0; t < VW; ++t) {
-                        const int m = I + t, k = m - d;
-                        if (t < tmax && k >= 0) {
-                            if constexpr (K == 2) {
-                                R0[t] = fma(lamlast, __ldg(ws.h + k), R0[t]);
-                            } else {
-                                const double Nk = __ldg(N + k);
-                                if constexpr (K == 0) R0[t] = fma(lamlast, Nk, R0[t]);
-                                if constexpr (K == 1) { R0[t] = fma(lamlast, Nk, R0[t]); R1[t] = fma(lamlast, __ldg(ws.h + k), R1[t]); }
-                                if constexpr (K == 3 || K == 5) R0[t] = fma(lamlast * Nk, Bf, R0[t]);
-                                if constexpr (K == 4 || K == 5) R2[t] = fma(lamlast * __ldg(ws.h + k), Sf, R2[t]);
-                            }
-                        }
-                    }
-                }
-            }
-        } else {
-            // generic grid: thread tid owns the partner chunk [k0, k1), walks the
-            // bracket of x_m + x_k upward along it for every row of the tile
-            const int chunk = (n + kMainThreads - 1) / kMainThreads;
-            const int k0 = min(n, tid * chunk), k1 = min(n, k0 + chunk);
-            const long long blast = dbits(x[n - 1]);
-#pragma unroll 1
-            for (int t = 0; t < tmax; ++t) {
-                const int m = I + t;
-                const double xm = x[m], am = ws.a[m], iam = ws.ia[m];
-                int lo = -1;
-                double r0 = 0.0, r1 = 0.0;
-                for (int k = k0; k < k1; ++k) {
-                    const double xk = x[k];
-                    const double v = xm + xk;
-                    double P;
-                    if (dbits(v) >= blast) {
-                        P = lamlast;
-                    } else {
-                        if (lo < 0) lo = bracket_lo(x, n, v);
-                        while (dbits(x[lo + 1]) <= dbits(v)) ++lo;
-                        P = fma(v - x[lo], ws.D[lo], lam[lo]);
-                    }
-                    const double PN = P * N[k];
-                    if constexpr (K == 0) r0 += PN;
-                    if constexpr (K == 1) r0 = fma(PN, xm + xk, r0);
-                    if constexpr (K == 2) r0 = fma(PN, xm * xk, r0);
-                    if constexpr (K == 3 || K == 5) r0 = fma(PN, fma(am, ws.ia[k], ws.a[k] * iam) + 2.0, r0);
-                    if constexpr (K == 4 || K == 5) { const double s = am + ws.a[k]; r1 = fma(PN, (s * s) * s, r1); }
-                }
-#pragma unroll
-                for (int u = 0; u < VW; ++u)
-                    if (u == t) { R0[u] = r0; R1[u] = r1; }
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < VW; ++t) {
-            red[t * kMainThreads + tid] = R0[t];
-            red[(VW + t) * kMainThreads + tid] = R1[t];
-            red[(2 * VW + t) * kMainThreads + tid] = R2[t];
-        }
-        __syncthreads();
-        if (tid < kVRows * 4) {
-            const int r = tid >> 2, c = tid & 3;
-            const double* p = red + r * kMainThreads + c * 64;
-            double s = 0.0;
-#pragma unroll 8
-            for (int q = 0; q < 64; ++q) s += p[q];
-            part4[c][r] = s;
-        }
-        __syncthreads();
-        if (tid < kVRows) fin[tid] = (part4[0][tid] + part4[1][tid]) + (part4[2][tid] + part4[3][tid]);
-        __syncthreads();
+        const int tmax = min(VW, n - I);
+        vjp_tile_accumulate<K>(v, I, red, sm, G);
         if (tid < VW) {
-            const int t = tid, m = I + t;
             double gB = 0.0, gS = 0.0;
-            if (t < tmax) {
-                const double xm = x[m], am = ws.a[m], iam = ws.ia[m], lm = lam[m], Nm = N[m];
-                const double* M = ws.mom;        // moments of N
-                const double* Lm = ws.mom + 5;   // moments of lambda*N
-                double AX0 = 0.0, AX1 = 0.0;     // A for beta0 / Brownian, and for shear
-                if constexpr (K <= 2) {
-                    double T = fin[t];
-                    if (geo) {
-                        if constexpr (K == 1) T = fma(xm, fin[t], fin[VW + t]);
-                        if constexpr (K == 2) T = xm * fin[t];
-                    }
-                    AX0 = T - fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
-                }
-                if constexpr (K == 3 || K == 5)
-                    AX0 = fin[t] - fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
-                if constexpr (K == 4 || K == 5) {
-                    const double T = geo ? fma(xm, fin[VW + t], fin[2 * VW + t]) : fin[VW + t];
-                    AX1 = T - fma(lm, moment_factor<K, 1>(xm, am, iam, M), moment_factor<K, 1>(xm, am, iam, Lm));
-                }
+            if (tid < tmax) {
                 double g;
-                if constexpr (K <= 2) g = b0 * AX0;
-                else if constexpr (K == 3) g = bbr * AX0;
-                else if constexpr (K == 4) g = bsh * AX1;
-                else g = fma(bbr, AX0, bsh * AX1);
-                gN[m] += g;
-                gB = 0.5 * Nm * AX0;
-                gS = 0.5 * Nm * AX1;
+                vjp_tile_row<K>(v, I + tid, tid, sm.fin[0], ws.mom, ws.mom + 5, b0, bbr, bsh, g,
+                                gB, gS);
+                gN[I + tid] += g;
             }
-            gsh[t][0] = gB;
-            gsh[t][1] = gS;
+            sm.gsh[0][tid][0] = gB;
+            sm.gsh[0][tid][1] = gS;
         }
         __syncthreads();
         if (tid == 0) {
             double s0 = 0.0, s1 = 0.0;
-            for (int t = 0; t < VW; ++t) { s0 += gsh[t][0]; s1 += gsh[t][1]; }
+            for (int t = 0; t < VW; ++t) { s0 += sm.gsh[0][t][0]; s1 += sm.gsh[0][t][1]; }
             // slots: 0 beta0, 1 beta_br, 2 beta_sh
             ws.gpart[task * 4 + 0] = (K <= 2) ? s0 : 0.0;
             ws.gpart[task * 4 + 1] = (K == 3 || K == 5) ? s0 : 0.0;

@@ -80,6 +80,7 @@ class BatchCellParams(ctypes.Structure):
 
 BATCH_TUNE, BATCH_RETUNE = 1, 2
 DEATH_MOMENTS, DEATH_DMMA = 0, 1
+DAUGHTER_SYMMETRIC, DAUGHTER_EROSION, DAUGHTER_UNIFORM, DAUGHTER_POWERLAW = range(4)
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -109,6 +110,10 @@ _SIGNATURES = {
     "pbe_batch_rk4_prepare": (_I, [_P, _P, _P, ctypes.c_double, _I]),
     "pbe_batch_schedule": (_I, [_P, _P, _P]),
     "pbe_batch_death": (_I, [_P, _P, _P, _P, _I, _P]),
+    "pbe_batch_rhs_vjp": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "pbe_daughter_table": (_I, [_I, _I, ctypes.c_double, ctypes.c_double, _P, _P, _I, _P]),
+    "pbe_batch_tape_forward": (_I, [_P, _P, _P, ctypes.c_double, _I, _I, _P]),
+    "pbe_batch_tape_backward": (_I, [_P, _P, _P, _P, _P]),
     "pbe_rk4_tape_create": (_I, [ctypes.POINTER(_P), _I, ctypes.c_double, _I, _I, _P, _P, _P]),
     "pbe_rk4_tape_destroy": (_I, [_P]),
     "pbe_rk4_tape_forward": (_I, [_P, _P, _P, _P, _P, _P]),

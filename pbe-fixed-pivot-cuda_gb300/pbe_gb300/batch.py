@@ -119,6 +119,26 @@ class BatchPlan:
         return _lib.load().pbe_batch_death(self._h, _ptr(N, "N"), _ptr(params, "params"),
                                            _ptr(death, "death"), int(method), _stream(stream))
 
+    def rhs_vjp(self, N, lam, gN, gparams, params, stream=None) -> int:
+        """gN += dL/dN, gparams[c, j] += dL/d(parameter j of cell c) for
+        L = lam . RHS(N); gparams: device array [n_cells, 8]."""
+        return _lib.load().pbe_batch_rhs_vjp(self._h, _ptr(N, "N"), _ptr(lam, "lambda"),
+                                             _ptr(gN, "gN"), _ptr(gparams, "gparams"),
+                                             _ptr(params, "params"), _stream(stream))
+
+    def tape_forward(self, N, params, dt: float, n_steps: int, checkpoint_every: int,
+                     stream=None) -> int:
+        """n_steps RK4 steps in place on N with checkpoints for tape_backward."""
+        return _lib.load().pbe_batch_tape_forward(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                                  float(dt), int(n_steps), int(checkpoint_every),
+                                                  _stream(stream))
+
+    def tape_backward(self, lam_T, gN0, gparams, stream=None) -> int:
+        """gN0 = dL/dN(0), gparams[c, j] = dL/d(parameter j of cell c) (overwritten)."""
+        return _lib.load().pbe_batch_tape_backward(self._h, _ptr(lam_T, "lambda_T"),
+                                                   _ptr(gN0, "gN0"), _ptr(gparams, "gparams"),
+                                                   _stream(stream))
+
     def schedule(self):
         """({class: group size} for the section-count classes present, bundles)."""
         gs = np.zeros(16, dtype=np.int32)

@@ -7,6 +7,9 @@ independence of the checkpoint interval (bitwise). The two-stage flocculation
 workload (shear rate switching mid-run, power-law selection and daughter,
 L = sum x^(2/3) N(T)) is run at full size. A torch.autograd.Function wraps the
 tape here, in the test harness only."""
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -162,8 +165,9 @@ def test_autograd_function_wrapper():
 
 def test_flocculation_two_stage_adjoint_full_size():
     """n = 3840, 200 RK4 steps, checkpoints every 20, shear switching at step
-    100: finite result, mass-like moment sane, gradient checked against central
-    differences for a few initial bins and for the coefficients."""
+    100: the forward equals the serial oracle's run of the same workload
+    (committed golden), the gradient is finite and matches central differences
+    for a few initial bins and for the shear coefficient of both stages."""
     torch = _torch()
     cfg = pg.grids.config_flocculation_adjoint()
     x, N0 = cfg["x"], cfg["N0"]
@@ -172,6 +176,13 @@ def test_flocculation_two_stage_adjoint_full_size():
                                cfg["lam_T"])
     assert np.all(np.isfinite(NT)) and np.all(np.isfinite(gN0))
     assert np.all(np.isfinite(ga)) and np.all(np.isfinite(gb))
+    # forward against the serial oracle's run of the same workload
+    # (tests/golden/flocculation_two_stage.json, make_flocculation_golden.py)
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                       "flocculation_two_stage.json")))
+    assert abs(float(cfg["lam_T"] @ NT) - gold["L"]) <= 1e-11 * abs(gold["L"])
+    np.testing.assert_allclose(NT[::gold["every"]], gold["N_T"], rtol=1e-10,
+                               atol=1e-10 * max(gold["N_T"]))
     dx, dtq, dbw = t(x), t(cfg["t_q"]), t(cfg["bw_q"])
 
     def L(N0_=N0, agg_=agg, brk_=brk):
