@@ -254,6 +254,21 @@ enum { PBE_DEATH_MOMENTS = 0, PBE_DEATH_DMMA = 1 };
 int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_params_t* params,
                     double* death, int method, void* stream);
 
+/* Adaptive integration of every cell from its current N to t_end (time 0 to
+ * t_end) with the embedded Dormand-Prince 5(4) pair, each cell with its own
+ * step size: error = RMS over the cell's bins of the embedded estimate over
+ * atol + rtol max(|N|, |N_new|); a step is accepted when error <= 1, the next
+ * step is dt (0.9 error^(-1/5)) clipped to [0.2, 5] dt (<= dt after a
+ * rejection) and to the time left; first step dt0. Everything runs on the
+ * device; the host reads one counter every 8 attempts. steps / rejects (host,
+ * n_cells, nullable) receive the accepted / rejected steps per cell, *attempts
+ * the attempts made. Returns cudaErrorNotReady (600) when some cell has not
+ * reached t_end within max_attempts (its N is the state it reached). No
+ * counterpart in the reference (its examples step RK4 on the host). */
+int pbe_batch_rk45(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                   double t_end, double rtol, double atol, double dt0, int max_attempts,
+                   int* steps, int* rejects, int* attempts, void* stream);
+
 /* Vector-Jacobian product of the batched RHS: for L = sum over cells of
  * lambda . rhs(N), gN += dL/dN (packed like N) and
  * gparams[8 c + j] += dL/d(parameter j of cell c), j = beta0, beta_br,

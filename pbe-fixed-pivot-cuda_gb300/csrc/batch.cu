@@ -65,6 +65,10 @@ struct pbe_batch_plan {
     int t_steps = 0, t_every = 1;
     double t_dt = 0.0;
     const pbe_batch_cell_params_t* t_params = nullptr;
+    // embedded RK 5(4) state (allocated on first use)
+    double* rk_k = nullptr;            // 7 packed stage derivatives
+    double* rk_cell = nullptr;         // t, dt per cell
+    int* rk_int = nullptr;             // status, steps, rejects per cell; done counter
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -714,6 +718,87 @@ cudaError_t tape_backward(pbe_batch_plan* p, const double* lamT, double* gN0, do
     return e;
 }
 
+// Dormand-Prince 5(4) tableau (Dormand & Prince, J. Comput. Appl. Math. 6 (1980)):
+// stage s (2..7) combines k_1 .. k_{s-1}; the 7th stage is the 5th-order
+// solution (first-same-as-last); kErr = b5 - b4 weights the error estimate.
+const double kDP[6][6] = {
+    {1.0 / 5.0},
+    {3.0 / 40.0, 9.0 / 40.0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
+    {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+const double kDPErr[7] = {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0,
+                          -17253.0 / 339200.0, 22.0 / 525.0, -1.0 / 40.0};
+
+// Adaptive embedded RK 5(4) for every cell to t_end: attempts are enqueued
+// in chunks of 8 (6 RHS evaluations and one control launch each), then the
+// count of finished cells is read back.
+cudaError_t rk45(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double t_end,
+                 double rtol, double atol, double dt0, int max_attempts, int* steps_out,
+                 int* rejects_out, int* attempts_out, cudaStream_t s)
+{
+    const BatchDev& d = p->d;
+    const size_t C = static_cast<size_t>(p->total), nc = static_cast<size_t>(p->n_cells);
+    cudaError_t e = cudaSuccess;
+    if (!p->rk_k) {
+        e = plan_alloc(p, &p->rk_k, 7 * C);
+        if (e == cudaSuccess) e = plan_alloc(p, &p->rk_cell, 2 * nc);
+        if (e == cudaSuccess) e = plan_alloc(p, &p->rk_int, 3 * nc + 1);
+        if (e != cudaSuccess) { p->rk_k = nullptr; return e; }
+    }
+    Rk45Ctl ctl;
+    ctl.t = p->rk_cell;
+    ctl.dt = p->rk_cell + nc;
+    ctl.status = p->rk_int;
+    ctl.steps = p->rk_int + nc;
+    ctl.rejects = p->rk_int + 2 * nc;
+    ctl.done = p->rk_int + 3 * nc;
+    ctl.t_end = t_end;
+    ctl.rtol = rtol;
+    ctl.atol = atol;
+    std::vector<double> init(2 * nc, 0.0);
+    for (size_t c = 0; c < nc; ++c) init[nc + c] = std::min(dt0, t_end);
+    e = cudaMemcpyAsync(p->rk_cell, init.data(), init.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->rk_int, 0, (3 * nc + 1) * sizeof(int), s);
+    double* k[7];
+    for (int j = 0; j < 7; ++j) k[j] = p->rk_k + static_cast<size_t>(j) * C;
+    // first stage of the first step
+    if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageRhs, 0.0, 0.0, s);
+    if (e == cudaSuccess) e = batch_main(d, N, prm, k[0], false, s);
+    StageCombine err{};
+    for (int j = 0; j < 7; ++j) { err.k[j] = k[j]; err.a[j] = kDPErr[j]; }
+    err.nk = 7;
+    err.dt = ctl.dt;
+    int attempts = 0, done = 0;
+    while (e == cudaSuccess && attempts < max_attempts && done < p->n_cells) {
+        const int chunk = std::min(8, max_attempts - attempts);
+        for (int a = 0; a < chunk && e == cudaSuccess; ++a) {
+            for (int st = 2; st <= 7 && e == cudaSuccess; ++st) {
+                StageCombine sc{};
+                for (int j = 0; j < st - 1; ++j) { sc.k[j] = k[j]; sc.a[j] = kDP[st - 2][j]; }
+                sc.nk = st - 1;
+                sc.dt = ctl.dt;
+                e = batch_prep_combine(d, N, prm, sc, s);
+                if (e == cudaSuccess) e = batch_main(d, d.Y, prm, k[st - 1], false, s);
+            }
+            if (e == cudaSuccess) e = batch_rk45_control(d, N, d.Y, err, k[0], ctl, s);
+        }
+        attempts += chunk;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&done, ctl.done, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e == cudaSuccess && steps_out)
+        e = cudaMemcpyAsync(steps_out, ctl.steps, nc * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && rejects_out)
+        e = cudaMemcpyAsync(rejects_out, ctl.rejects, nc * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (attempts_out) *attempts_out = attempts;
+    if (e != cudaSuccess) return e;
+    return done == p->n_cells ? cudaSuccess : cudaErrorNotReady;
+}
+
 // Work items of the death GEMM: the cells of each grid, largest first, in
 // row tiles of 64; each row tile covers the bins below its largest n in
 // column tiles of 64.
@@ -883,6 +968,20 @@ int pbe_batch_tape_backward(pbe_batch_t plan, const double* lambda_T, double* gN
     if (!plan->t_recorded) return cudaErrorInvalidValue;
     if (!lambda_T || !gN0 || !gparams) return cudaErrorInvalidDevicePointer;
     return tape_backward(plan, lambda_T, gN0, gparams, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_rk45(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                   double t_end, double rtol, double atol, double dt0, int max_attempts,
+                   int* steps, int* rejects, int* attempts, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (!(t_end > 0.0) || !std::isfinite(t_end) || !(rtol >= 0.0) || !(atol >= 0.0) ||
+        !(rtol > 0.0 || atol > 0.0) || !(dt0 > 0.0) || max_attempts <= 0)
+        return cudaErrorInvalidValue;
+    return rk45(plan, N, params, t_end, rtol, atol, dt0, max_attempts, steps, rejects, attempts,
+                static_cast<cudaStream_t>(stream));
 }
 
 int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)

@@ -87,6 +87,27 @@ enum BatchStage : int {
     kStageTwo     = 2,  // kacc = k1; Y = N + c k1
     kStageThree   = 3,  // kacc += 2 k; Y = N + c k (stages 3 and 4)
     kStageFinish  = 4,  // kacc += k4; N += dt/6 kacc (no RHS follows)
+    kStageCombine = 5,  // Y = N + dt_c sum_j a_j k_j (embedded RK stages, per-cell dt)
+};
+
+// Stage combination of an explicit RK method with a per-cell step:
+// Y = N + dt[c] (a[0] k[0] + ... + a[nk-1] k[nk-1]), summed in that order.
+struct StageCombine {
+    const double* k[7];    // packed stage derivatives
+    double a[7];
+    int nk;
+    const double* dt;      // [n_cells]
+};
+
+// Per-cell step control of the embedded RK 5(4) integrator.
+struct Rk45Ctl {
+    double* t;             // [n_cells] time reached
+    double* dt;            // [n_cells] next step (0 once done)
+    int* status;           // [n_cells] 0 running, 1 reached t_end, 2 step underflow
+    int* steps;            // [n_cells] accepted steps
+    int* rejects;          // [n_cells] rejected steps
+    int* done;             // [1] cells with status != 0
+    double t_end, rtol, atol;
 };
 
 // Launchers (batch_kernels.cu). All are asynchronous on `s`.
@@ -100,6 +121,15 @@ cudaError_t batch_grid_tables(const BatchDev& d, const double* t_q, const double
 // the RHS is evaluated at (N itself for kStageRhs / kStageNext).
 cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
                        int stage, double c, double dt6, cudaStream_t s);
+// Prep of an embedded-RK stage: Y = N + dt_c sum_j a_j k_j, then as batch_prep.
+cudaError_t batch_prep_combine(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
+                               const StageCombine& sc, cudaStream_t s);
+// Error estimate, accept / reject and next step of every running cell (one
+// CTA per cell): err = RMS over bins of dt sum_j e_j k_j / (atol + rtol
+// max(|N|, |Y|)); accepted: N = Y, k[0] = k[6] (first stage of the next step).
+cudaError_t batch_rk45_control(const BatchDev& d, double* N, const double* Y,
+                               const StageCombine& err, double* k0, const Rk45Ctl& ctl,
+                               cudaStream_t s);
 // Persistent RHS kernel over the plan's bundles: out (+)= RHS(Y) for every cell.
 cudaError_t batch_main(const BatchDev& d, const double* Y, const pbe_batch_cell_params_t* params,
                        double* out, bool accumulate, cudaStream_t s);

@@ -247,7 +247,7 @@ __device__ void cell_breakage(const BatchDev& d, const BatchGridDev& gd, const d
 template <int K>
 __global__ void __launch_bounds__(256)
 batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restrict__ params,
-                  int stage, double c, double dt6)
+                  int stage, double c, double dt6, StageCombine sc)
 {
     __shared__ double sh[8];
     const BatchCellDev cd = d.cells[blockIdx.x];
@@ -267,8 +267,17 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
     const double cN = (K <= 2) ? P.beta0 : P.beta_br;
     const double cH = (K == 1 || K == 2) ? P.beta0 : P.beta_sh;
     double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const double dtc = (stage == kStageCombine) ? sc.dt[blockIdx.x] : 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double y = stage_update(stage, Nc, kc, ac, Yc, i, c, dt6);
+        double y;
+        if (stage == kStageCombine) {
+            double s_ = 0.0;
+            for (int j = 0; j < sc.nk; ++j) s_ = fma(sc.a[j], sc.k[j][off + i], s_);
+            y = fma(dtc, s_, Nc[i]);
+            Yc[i] = y;
+        } else {
+            y = stage_update(stage, Nc, kc, ac, Yc, i, c, dt6);
+        }
         if (stage == kStageFinish) continue;
         const double xi = x[i];
         const double h = xi * y;
@@ -443,19 +452,93 @@ cudaError_t batch_grid_tables(const BatchDev& d, const double* t_q, const double
     return cudaGetLastError();
 }
 
-cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
-                       int stage, double c, double dt6, cudaStream_t s)
+namespace {
+cudaError_t prep_any(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params, int stage,
+                     double c, double dt6, const StageCombine& sc, cudaStream_t s)
 {
     if (d.n_cells <= 0) return cudaErrorInvalidValue;
     switch (d.kernel < 0 ? 0 : d.kernel) {
-    case 0: batch_prep_kernel<0><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
-    case 1: batch_prep_kernel<1><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
-    case 2: batch_prep_kernel<2><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
-    case 3: batch_prep_kernel<3><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
-    case 4: batch_prep_kernel<4><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
-    case 5: batch_prep_kernel<5><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6); break;
+    case 0: batch_prep_kernel<0><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
+    case 1: batch_prep_kernel<1><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
+    case 2: batch_prep_kernel<2><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
+    case 3: batch_prep_kernel<3><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
+    case 4: batch_prep_kernel<4><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
+    case 5: batch_prep_kernel<5><<<d.n_cells, 256, 0, s>>>(d, N, params, stage, c, dt6, sc); break;
     default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256)
+rk45_control_kernel(BatchDev d, double* N, const double* __restrict__ Y, StageCombine e,
+                    double* k0, Rk45Ctl ctl)
+{
+    __shared__ double sh[8];
+    __shared__ int accept_s;
+    const int c = blockIdx.x;
+    if (ctl.status[c] != 0) return;                 // whole block
+    const BatchCellDev cd = d.cells[c];
+    const int off = cd.off, n = cd.n;
+    const double dt = ctl.dt[c];
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s_ = 0.0;
+        for (int j = 0; j < e.nk; ++j) s_ = fma(e.a[j], e.k[j][off + i], s_);
+        const double sc = ctl.atol + ctl.rtol * fmax(fabs(N[off + i]), fabs(Y[off + i]));
+        const double r = (dt * s_) / sc;
+        s2 = fma(r, r, s2);
+    }
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) {
+        const double err = sqrt(s2 / n);
+        const bool finite = (err == err) && err <= 1.7e308;
+        const bool accept = finite && err <= 1.0;
+        double fac;
+        if (!finite) fac = 0.2;
+        else if (err == 0.0) fac = 5.0;
+        else fac = fmin(5.0, fmax(0.2, 0.9 * pow(err, -0.2)));
+        if (!accept) fac = fmin(fac, 1.0);
+        double t = ctl.t[c];
+        if (accept) { t += dt; ctl.t[c] = t; ctl.steps[c] += 1; }
+        else ctl.rejects[c] += 1;
+        const double rem = ctl.t_end - t;
+        double nd = fmin(dt * fac, rem);
+        int st = 0;
+        if (accept && rem <= 1e-12 * fmax(fabs(ctl.t_end), 1.0)) { st = 1; nd = 0.0; }
+        else if (nd <= 1e-14 * fmax(fabs(ctl.t_end), 1.0)) { st = 2; nd = 0.0; }
+        ctl.dt[c] = nd;
+        if (st != 0) { ctl.status[c] = st; atomicAdd(ctl.done, 1); }
+        accept_s = accept ? 1 : 0;
+    }
+    __syncthreads();
+    if (accept_s) {
+        const double* k6 = e.k[6];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            N[off + i] = Y[off + i];
+            k0[off + i] = k6[off + i];     // first stage of the next step (FSAL)
+        }
+    }
+}
+} // namespace
+
+cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
+                       int stage, double c, double dt6, cudaStream_t s)
+{
+    const StageCombine none{};
+    return prep_any(d, N, params, stage, c, dt6, none, s);
+}
+
+cudaError_t batch_prep_combine(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,
+                               const StageCombine& sc, cudaStream_t s)
+{
+    return prep_any(d, N, params, kStageCombine, 0.0, 0.0, sc, s);
+}
+
+cudaError_t batch_rk45_control(const BatchDev& d, double* N, const double* Y,
+                               const StageCombine& err, double* k0, const Rk45Ctl& ctl,
+                               cudaStream_t s)
+{
+    rk45_control_kernel<<<d.n_cells, 256, 0, s>>>(d, N, Y, err, k0, ctl);
     return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@ from ._lib import (  # noqa: F401
     AGG_SUM,
     ERR_INVALID_CONFIGURATION,
     ERR_INVALID_DEVICE_POINTER,
+    ERR_NOT_READY,
     ERR_INVALID_VALUE,
     LIB_PATH,
     MODE_DEFAULT,

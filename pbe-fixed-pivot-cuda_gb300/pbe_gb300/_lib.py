@@ -20,6 +20,7 @@ ERR_INVALID_VALUE = 1
 ERR_MEMORY_ALLOCATION = 2
 ERR_INVALID_CONFIGURATION = 9
 ERR_INVALID_DEVICE_POINTER = 17
+ERR_NOT_READY = 600
 
 # enum values (include/pbe_gb300.h, identical to the reference's enums)
 AGG_CONSTANT, AGG_SUM, AGG_PRODUCT, AGG_BROWNIAN, AGG_SHEAR, AGG_BROWNIAN_SHEAR = range(6)
@@ -111,6 +112,8 @@ _SIGNATURES = {
     "pbe_batch_schedule": (_I, [_P, _P, _P]),
     "pbe_batch_death": (_I, [_P, _P, _P, _P, _I, _P]),
     "pbe_batch_rhs_vjp": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "pbe_batch_rk45": (_I, [_P, _P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_double, _I, _P, _P, _P, _P]),
     "pbe_daughter_table": (_I, [_I, _I, ctypes.c_double, ctypes.c_double, _P, _P, _I, _P]),
     "pbe_batch_tape_forward": (_I, [_P, _P, _P, ctypes.c_double, _I, _I, _P]),
     "pbe_batch_tape_backward": (_I, [_P, _P, _P, _P, _P]),

@@ -108,6 +108,20 @@ class BatchPlan:
         return _lib.load().pbe_batch_rk4_prepare(self._h, _ptr(N, "N"), _ptr(params, "params"),
                                                  float(dt), int(n_steps))
 
+    def rk45(self, N, params, t_end: float, rtol: float = 1e-8, atol: float = 0.0,
+             dt0: float = 1e-3, max_attempts: int = 100000, stream=None):
+        """Adaptive Dormand-Prince 5(4) to t_end, a step size per cell.
+        Returns (code, accepted steps per cell, rejected steps per cell, attempts);
+        code 600 (ERR_NOT_READY) if max_attempts ran out."""
+        steps = np.zeros(self.n_cells, dtype=np.int32)
+        rejects = np.zeros(self.n_cells, dtype=np.int32)
+        att = ctypes.c_int()
+        code = _lib.load().pbe_batch_rk45(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                          float(t_end), float(rtol), float(atol), float(dt0),
+                                          int(max_attempts), steps.ctypes.data, rejects.ctypes.data,
+                                          ctypes.byref(att), _stream(stream))
+        return code, steps, rejects, att.value
+
     def rk4_percell(self, N, params, dt: float, n_steps: int, stream=None) -> int:
         """The same integration as a per-cell launch loop (baseline)."""
         return _lib.load().pbe_batch_rk4_percell(self._h, _ptr(N, "N"), _ptr(params, "params"),
