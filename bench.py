@@ -16,9 +16,14 @@ integrator asks for once per stage).
   e2e   : the same step through the C ABI from pinned HOST buffers: H2D copy of
           N, the RHS, D2H copy of rhs, all inside the timed events.
 
---impl reference runs the reference's own CUDA kernels (built unmodified from
-its sources into oracle/_ref/, launched with its launch geometry) on the same
-GPU, config and timing. The reference has no CPU implementation of the path.
+--impl reference times the reference's path on the machine's host cores. The
+reference implements the path only in CUDA (no CPU implementation), so the arm
+runs the oracle port (oracle/pbe_oracle.cpp: the reference's pair and fragment
+loops restated serially, aggregation rows spread over all host threads) on
+the same workload; each step is one full n = 16384 RHS evaluation and the
+number of timed steps is capped so the arm ends within a few minutes. Our own
+line also carries `reference_kernels_sm103a`: the reference's CUDA kernels,
+built unmodified from its sources (oracle/_ref), timed on the same GPU.
 
 Multi-GPU: the single-instance RHS does not shard; with torchrun each rank runs
 an independent replica on its own GPU ("replicas only"), value = total steps/s.
@@ -490,6 +495,7 @@ def profile_case(name: str) -> None:
     """A few launches of one kernel family on a mid-size case, for ncu:
       batched : 1024 cells of the batched workload (seed 2026), 4 batched RHS
       death   : the 512-cell size-class workload, 3 DMMA and 3 moment death calls
+      vjp     : the n = 16384 workload, 3 aggregation + breakage VJPs
       adjoint : the n = 3840 flocculation tape, 10 steps forward + backward"""
     import torch
 
@@ -513,6 +519,17 @@ def profile_case(name: str) -> None:
             out = torch.zeros(plan.total, **f64)
             for m in (pg.DEATH_DMMA, pg.DEATH_MOMENTS) * 3:
                 pg.check(plan.death(dN, out, P, m), "death")
+    elif name == "vjp":
+        x, N, t_q, bw_q, ap, bp = workload()
+        dN, dx = torch.tensor(N, **f64), torch.tensor(x, **f64)
+        dt, db = torch.tensor(t_q, **f64), torch.tensor(bw_q, **f64)
+        lam = torch.randn(N_BINS, dtype=torch.float64, device=dev,
+                          generator=torch.Generator(device=dev).manual_seed(7))
+        gN = torch.zeros(N_BINS, **f64)
+        ga, gb = torch.zeros(3, **f64), torch.zeros(4, **f64)
+        for _ in range(3):
+            pg.check(pg.aggregation_rhs_vjp(dN, dx, lam, gN, ga, ap), "agg vjp")
+            pg.check(pg.breakage_rhs_vjp(dN, dx, dt, db, lam, gN, gb, bp), "brk vjp")
     elif name == "adjoint":
         cfg = pg.grids.config_flocculation_adjoint(n_steps=10, switch_step=5)
         dx, dtq, dbw = (torch.tensor(cfg[k], **f64) for k in ("x", "t_q", "bw_q"))
@@ -527,9 +544,102 @@ def profile_case(name: str) -> None:
     torch.cuda.synchronize()
 
 
+def reference_arm(args) -> None:
+    """The reference's path on the host cores (oracle port, all threads)."""
+    import pyoracle
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return  # rank 0 alone runs the reference arm
+    x, N, t_q, bw_q, ap, bp = workload()
+    threads = os.cpu_count() or 1
+
+    def step():
+        pyoracle.aggregation_rhs_mt(N, x, ap.kernel_type, ap.beta0, ap.beta_br, ap.beta_sh,
+                                    ap.log_x0, ap.inv_log_r, nthreads=threads)
+        pyoracle.breakage_rhs(N, x, t_q, bw_q, bp.selection, bp.S0, bp.v_ref, bp.alpha, bp.v_min)
+
+    w0 = time.perf_counter()
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    per = (time.perf_counter() - w0) / max(1, min(args.warmup, 2))
+    steps = int(min(args.steps, max(3, 90.0 / max(per, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    el = time.perf_counter() - t0
+    value = steps / el
+    sample = ("%d full n=16384 agg+brk RHS evaluations (%.1f s), oracle port with aggregation "
+              "rows over %d host threads, breakage serial" % (steps, el, threads))
+    out = {
+        "metric": "Agg+br RHS evals/s at N=16384 FP64",
+        "value": round(value, 4),
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": steps,
+        "steps_requested": args.steps,
+        "warmup": max(1, min(args.warmup, 2)),
+        "ms_per_step": round(el / steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded lognormal N on the stated grid)",
+        "config": {"workload": "single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), "
+                               "Brownian+shear (beta_br=6.73e-18, beta_sh=4*50/3) + threshold "
+                               "breakage (S0=1e-3, v_min=x_8192), symmetric daughter as n_quad=16",
+                   "n": N_BINS, "n_quad": N_QUAD, "pairs_per_eval": PAIRS,
+                   "fragments_per_eval": FRAGMENTS, "parallelism": "host cores"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "evals/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "reference_note": "the reference implements this path only in CUDA; the oracle port "
+                          "restates its loops on the CPU (oracle/pbe_oracle.cpp)",
+    }
+    print(json.dumps(out))
+
+
+def reference_kernels_section(dev, stream, dN, dx, dt, db, rhs, ap, bp, flush, steps=20):
+    """The reference's CUDA kernels (built unmodified from its sources into
+    oracle/_ref, launched with its launch geometry) on the same GPU, step and
+    timing as the main value (L2 flushed before each timed step)."""
+    import torch
+
+    import pbe_gb300 as pg
+    import pyoracle
+
+    try:
+        ref = pyoracle.RefRunner()
+    except (FileNotFoundError, OSError, RuntimeError) as exc:
+        return {"unavailable": str(exc)}
+
+    def step():
+        rhs.zero_()
+        pg.check(ref.aggregation_rhs(dN, dx, rhs, ap, stream), "reference aggregation")
+        pg.check(ref.breakage_rhs(dN, dx, dt, db, rhs, bp, stream), "reference breakage")
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            step()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    return {"evals_per_s": round(1e3 / ms, 3), "ms_per_eval": round(ms, 3), "steps": steps,
+            "what": "acuoci/pbe-fixed-pivot-cuda src/aggregation.cu + src/breakage.cu, unmodified, "
+                    "nvcc -O3 for sm_103a (oracle/build_ref.sh), its launch geometry, same GPU"}
+
+
 def main():
     ap_ = argparse.ArgumentParser()
-    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint"],
+    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint", "vjp"],
                      help="run a few launches of one kernel family (for ncu) and exit")
     ap_.add_argument("--gpus", type=int, default=1)
     ap_.add_argument("--steps", type=int, default=200)
@@ -543,17 +653,18 @@ def main():
     if args.profile_case:
         profile_case(args.profile_case)
         return
+    if args.impl == "reference":
+        reference_arm(args)
+        return
 
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference" and world > 1 and rank != 0:
-        return  # the reference arm runs on rank 0 only
     torch.cuda.set_device(local)
     dist = None
-    if world > 1 and args.impl == "ours":
+    if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -572,22 +683,14 @@ def main():
     hR = torch.empty(N_BINS, dtype=torch.float64).pin_memory()
 
     mode = pg.MODE_GATHER if args.mode == "gather" else pg.MODE_SCATTER
-    if args.impl == "reference":
-        import pyoracle
 
-        ref = pyoracle.RefRunner()
-
-        def step(n_dev):
-            rhs.zero_()
-            pg.check(ref.aggregation_rhs(n_dev, dx, rhs, ap, stream), "reference aggregation")
-            pg.check(ref.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream), "reference breakage")
-        launches_per_step = 3
-    else:
-        def step(n_dev):
-            rhs.zero_()
-            pg.check(pg.aggregation_rhs(n_dev, dx, rhs, ap, stream=stream, mode=mode), "aggregation")
-            pg.check(pg.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream=stream, mode=mode), "breakage")
-        launches_per_step = 4 + (2 if mode == pg.MODE_GATHER else 1)
+    def step(n_dev):
+        rhs.zero_()
+        pg.check(pg.aggregation_rhs(n_dev, dx, rhs, ap, stream=stream, mode=mode), "aggregation")
+        pg.check(pg.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream=stream, mode=mode), "breakage")
+    # aggregation: prep, clip, pair kernel; breakage: prep + gather (gather
+    # mode) or one scatter kernel
+    launches_per_step = 3 + (2 if mode == pg.MODE_GATHER else 1)
 
     clocks = ClockSampler(local)
     with torch.cuda.stream(stream):
@@ -611,18 +714,16 @@ def main():
         wall0 = time.perf_counter()
         for k in range(args.steps):
             flush.zero_()
-            if args.impl == "ours":
-                pg.load().pbe_set_profile_events(main_evs[k][0].cuda_event, main_evs[k][1].cuda_event)
+            pg.load().pbe_set_profile_events(main_evs[k][0].cuda_event, main_evs[k][1].cuda_event)
             evs[k][0].record(stream)
             step(dN)
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
-        if args.impl == "ours":
-            pg.load().pbe_set_profile_events(None, None)
+        pg.load().pbe_set_profile_events(None, None)
         step_ms = [a.elapsed_time(b) for a, b in evs]
         total_ms = sum(step_ms)
-        main_ms = [a.elapsed_time(b) for a, b in main_evs] if args.impl == "ours" else []
+        main_ms = [a.elapsed_time(b) for a, b in main_evs]
 
         # ---- e2e: host buffers through the C ABI, copies inside the timing ----
         e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -640,28 +741,27 @@ def main():
 
         # ---- adjoint: aggregation + breakage VJP of the same step ----------
         vjp_ms = None
-        if args.impl == "ours":
-            lam = torch.randn(N_BINS, dtype=torch.float64, device=dev,
-                              generator=torch.Generator(device=dev).manual_seed(7))
-            gN = torch.zeros(N_BINS, **f64)
-            ga = torch.zeros(3, **f64)
-            gb = torch.zeros(4, **f64)
+        lam = torch.randn(N_BINS, dtype=torch.float64, device=dev,
+                          generator=torch.Generator(device=dev).manual_seed(7))
+        gN = torch.zeros(N_BINS, **f64)
+        ga = torch.zeros(3, **f64)
+        gb = torch.zeros(4, **f64)
 
-            def vjp_step():
-                gN.zero_()
-                pg.check(pg.aggregation_rhs_vjp(dN, dx, lam, gN, ga, ap, stream=stream), "agg vjp")
-                pg.check(pg.breakage_rhs_vjp(dN, dx, dt, db, lam, gN, gb, bp, stream=stream), "brk vjp")
-            for _ in range(3):
-                vjp_step()
-            v_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                     for _ in range(max(args.steps // 4, 5))]
-            for a_, b_ in v_evs:
-                flush.zero_()
-                a_.record(stream)
-                vjp_step()
-                b_.record(stream)
-            torch.cuda.synchronize()
-            vjp_ms = sum(a_.elapsed_time(b_) for a_, b_ in v_evs) / len(v_evs)
+        def vjp_step():
+            gN.zero_()
+            pg.check(pg.aggregation_rhs_vjp(dN, dx, lam, gN, ga, ap, stream=stream), "agg vjp")
+            pg.check(pg.breakage_rhs_vjp(dN, dx, dt, db, lam, gN, gb, bp, stream=stream), "brk vjp")
+        for _ in range(3):
+            vjp_step()
+        v_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(max(args.steps // 4, 5))]
+        for a_, b_ in v_evs:
+            flush.zero_()
+            a_.record(stream)
+            vjp_step()
+            b_.record(stream)
+        torch.cuda.synchronize()
+        vjp_ms = sum(a_.elapsed_time(b_) for a_, b_ in v_evs) / len(v_evs)
         time.sleep(0.2)
         clk = clocks.stop()
 
@@ -693,7 +793,7 @@ def main():
         "config": {"workload": "single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), "
                                "Brownian+shear (beta_br=6.73e-18, beta_sh=4*50/3) + threshold "
                                "breakage (S0=1e-3, v_min=x_8192), symmetric daughter as n_quad=16",
-                   "n": N_BINS, "n_quad": N_QUAD, "mode": args.mode if args.impl == "ours" else "reference",
+                   "n": N_BINS, "n_quad": N_QUAD, "mode": args.mode,
                    "pairs_per_eval": PAIRS, "fragments_per_eval": FRAGMENTS,
                    "l2": "flushed before every timed step (512 MiB write)",
                    "parallelism": "replicas" if n_gpus > 1 else "single GPU"},
@@ -701,7 +801,7 @@ def main():
         "wall_s_timed_loop": round(wall, 4),
         "e2e": {"value": round(e2e_value, 3), "unit": "evals/s",
                 "h2d_bytes_per_step": N_BINS * 8, "d2h_bytes_per_step": N_BINS * 8},
-        "gpu_launches": launches_per_step * args.steps if args.impl == "ours" else 0,
+        "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
     }
     if vjp_ms is not None:
@@ -709,37 +809,34 @@ def main():
                       "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
                       "what": "aggregation + breakage VJP (dL/dN and parameter gradients) of "
                               "the same n=16384 step, device-resident, L2 flushed"}
-    if args.impl == "reference":
-        out["impl"] = "reference"
-        out["reference_build"] = ("acuoci/pbe-fixed-pivot-cuda src/aggregation.cu + src/breakage.cu, "
-                                  "unmodified, nvcc -O3 for sm_103a (oracle/build_ref.sh), "
-                                  "launched with the reference launch geometry")
-        out["reference_kernel_launches"] = launches_per_step * args.steps
-    else:
-        peak = fp64_peak_tflops(stream)
-        mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
-        achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
-        instr = fp64_instr_per_launch(x)
-        instr_rate = instr / mk if mk else None
-        out["roofline"] = {
-            "bound": "fp64",
-            "kernel": "agg_main_kernel<5>",
-            "achieved": round(achieved, 4) if achieved else None,
-            "peak": round(peak, 4) if peak else None,
-            "unit": "TFLOP/s",
-            "frac": round(achieved / peak, 4) if (achieved and peak) else None,
-            "traffic": MAIN_KERNEL_DRAM_BYTES,
-            "kernel_ms": round(mk * 1e3, 5) if mk else None,
-            "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
-            "algorithmic_unit": "22 FP64 flops per pair interaction (reference formula, cube roots "
-                                "per bin); frac > 1 because the kernel executes %.2f FP64 "
-                                "instructions per pair" % (instr / PAIRS),
-            "fp64_instr_per_launch": instr,
-            "fp64_pipe_frac": round(instr_rate / (peak * 1e12 / 2.0), 4) if (instr_rate and peak) else None,
-            "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
-                           "FP64 entry in MEASURED_PEAKS.json",
-        }
-    if n_gpus == 1 and args.impl == "ours" and not args.no_extras:
+    peak = fp64_peak_tflops(stream)
+    mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
+    achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
+    instr = fp64_instr_per_launch(x)
+    instr_rate = instr / mk if mk else None
+    out["roofline"] = {
+        "bound": "fp64",
+        "kernel": "agg_main_kernel<5>",
+        "achieved": round(achieved, 4) if achieved else None,
+        "peak": round(peak, 4) if peak else None,
+        "unit": "TFLOP/s",
+        "frac": round(achieved / peak, 4) if (achieved and peak) else None,
+        "traffic": MAIN_KERNEL_DRAM_BYTES,
+        "kernel_ms": round(mk * 1e3, 5) if mk else None,
+        "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
+        "algorithmic_unit": "22 FP64 flops per pair interaction (reference formula, cube roots "
+                            "per bin); frac > 1 because the kernel executes %.2f FP64 "
+                            "instructions per pair" % (instr / PAIRS),
+        "fp64_instr_per_launch": instr,
+        "fp64_pipe_frac": round(instr_rate / (peak * 1e12 / 2.0), 4) if (instr_rate and peak) else None,
+        "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
+                       "FP64 entry in MEASURED_PEAKS.json",
+    }
+    if n_gpus == 1 and not args.no_extras:
+        rk = reference_kernels_section(dev, stream, dN, dx, dt, db, rhs, ap, bp, flush)
+        if "evals_per_s" in rk:
+            rk["speedup_of_value"] = round(value / rk["evals_per_s"], 2)
+        out["reference_kernels_sm103a"] = rk
         out["batched"] = batched_section(dev, stream)
         out["adjoint"] = adjoint_section(dev, stream)
         out["classes"] = classes_section(dev, stream)

@@ -1,7 +1,9 @@
 """Adaptive embedded Dormand-Prince 5(4) on the batched plan (pbe_batch_rk45):
 accuracy against the oracle's fixed-step RK4 with a step 100 times smaller
 than the adaptive steps, per-cell step sizes (a faster cell takes more steps),
-determinism, and the not-ready return when the attempt budget runs out."""
+determinism, and the not-ready return when the attempt budget runs out.
+The oracle reference uses 20 RK4 steps for every accepted adaptive step
+(at least 200); bound 1e-6 relative + 1e-7 of the cell's largest N."""
 import numpy as np
 import pytest
 
@@ -12,17 +14,24 @@ from gpu_util import t
 pytestmark = pytest.mark.gpu
 
 
-def batch(n_cells=6, n=96, fast=(2,)):
+def batch(n_cells=6, n=96):
+    """Cells 0 and 1 are identical except that every rate of cell 1 is 30 times
+    larger (so over the same interval it goes through 30 times more of its
+    evolution); the others differ in grid, n and coefficients."""
     rng = np.random.default_rng(21)
     grids = [pg.grids.geometric_pow2(n, 1e-21, 8.0), pg.grids.geometric_pow2(n, 1e-20, 16.0)]
     cell_grid = np.arange(n_cells) % 2
+    cell_grid[1] = cell_grid[0]
     cell_n = rng.integers(n // 2, n + 1, size=n_cells)
+    cell_n[1] = cell_n[0]
     N = [pg.grids.lognormal_ic(grids[g][:m], m // 4, 1.0, 1e13, cut=5.0) for g, m in zip(cell_grid, cell_n)]
-    G = np.full(n_cells, 50.0)
-    G[list(fast)] *= 20.0                      # faster aggregation in these cells
+    G = rng.uniform(20.0, 100.0, size=n_cells)
+    G[1] = G[0]
+    scale = np.ones(n_cells)
+    scale[1] = 30.0
     v_ref = np.array([grids[g][m // 2] for g, m in zip(cell_grid, cell_n)])
-    params = pg.batch.cell_params(n_cells, beta0=0.0, beta_br=6.73e-18, beta_sh=4 * G / 3,
-                                  S0=1e-3, v_ref=v_ref, alpha=1.0)
+    params = pg.batch.cell_params(n_cells, beta0=0.0, beta_br=6.73e-18 * scale,
+                                  beta_sh=4 * G / 3 * scale, S0=1e-3 * scale, v_ref=v_ref, alpha=1.0)
     t_q, bw_q = pg.quadrature.uniform(4)
     return grids, cell_n, cell_grid, N, params, t_q, bw_q
 
@@ -38,7 +47,7 @@ def test_rk45_matches_fine_rk4_oracle_and_adapts_per_cell():
         torch.cuda.synchronize()
         assert code == 0, pg.error_string(code)
         got = plan.split(dN.cpu().numpy())
-    assert steps[2] > steps[[0, 1, 3, 4, 5]].max()       # the fast cell needs more steps
+    assert steps[1] > steps[0]                # the same cell at 30x the rates needs more steps
     for c in range(len(cell_n)):
         x = grids[cell_grid[c]][:cell_n[c]]
         p = params[c]
