@@ -141,7 +141,7 @@ __device__ void batch_vjp_task(const BatchDev& d, const BatchVjpDev& vd, const d
         else if (l == 12) val = params[c].beta_sh;
         sm.cinfo[G.g][l] = val;
     }
-    vjp_tile_accumulate<K>(v, I, red, sm, G);          // syncs the group first
+    vjp_tile_accumulate<K>(v, I, 0, n, red, sm, G);    // syncs the group first
     const int tmax = min(VW, n - I);
     if (G.lane < VW) {
         double gB = 0.0, gS = 0.0;

@@ -24,6 +24,8 @@
 //   dL/dN_j = S_j Q_j, dL/dS0 = sum_j (S_j/S0) N_j Q_j, dL/dv_ref, dL/dalpha
 // (PowerLaw: dS/dalpha = S ln(x/v_ref)), dL/dv_min = 0 (threshold step).
 // =============================================================================
+#include <cmath>
+
 #include "pbe_internal.cuh"
 #include "vjp_tile.cuh"
 
@@ -123,11 +125,13 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
     }
 }
 
+// Pair sums: task = (row tile, partner chunk); the whole CTA is one group.
+// Each task stores its rows' three sums per chunk; vjp_rows_kernel adds the
+// chunks in order and finishes the rows.
 template <int K>
 __global__ void __launch_bounds__(kMainThreads, 2)
 vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
-                const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
-                int ntile, double b0, double bbr, double bsh)
+                const double* __restrict__ lam, VjpWs ws, int n, int ntile, int nch)
 {
     extern __shared__ double red[];               // [kVRows][kMainThreads]
     __shared__ VjpShared sm;
@@ -140,37 +144,62 @@ vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     v.n = n;
     v.geo = ws.mom[10] != 0.0;
     const TileGroup G{0, tid, kMainThreads};
+    const int span = (n + nch - 1) / nch;
 
     for (;;) {
         if (tid == 0) s_task = atomicAdd(ws.counter, 1);
         __syncthreads();
         const int task = s_task;
         __syncthreads();
-        if (task >= ntile) break;
-        const int I = task * VW;
-        const int tmax = min(VW, n - I);
-        vjp_tile_accumulate<K>(v, I, red, sm, G);
-        if (tid < VW) {
-            double gB = 0.0, gS = 0.0;
-            if (tid < tmax) {
-                double g;
-                vjp_tile_row<K>(v, I + tid, tid, sm.fin[0], ws.mom, ws.mom + 5, b0, bbr, bsh, g,
-                                gB, gS);
-                gN[I + tid] += g;
-            }
-            sm.gsh[0][tid][0] = gB;
-            sm.gsh[0][tid][1] = gS;
-        }
+        if (task >= ntile * nch) break;
+        const int tile = task / nch, chunk = task - tile * nch;
+        const int r0 = min(n, chunk * span), r1 = min(n, r0 + span);
+        vjp_tile_accumulate<K>(v, tile * VW, r0, r1, red, sm, G);
+        if (tid < kVRows) ws.vpart[(static_cast<size_t>(tile) * nch + chunk) * kVRows + tid] = sm.fin[0][tid];
         __syncthreads();
-        if (tid == 0) {
-            double s0 = 0.0, s1 = 0.0;
-            for (int t = 0; t < VW; ++t) { s0 += sm.gsh[0][t][0]; s1 += sm.gsh[0][t][1]; }
-            // slots: 0 beta0, 1 beta_br, 2 beta_sh
-            ws.gpart[task * 4 + 0] = (K <= 2) ? s0 : 0.0;
-            ws.gpart[task * 4 + 1] = (K == 3 || K == 5) ? s0 : 0.0;
-            ws.gpart[task * 4 + 2] = (K == 4 || K == 5) ? s1 : 0.0;
-        }
-        __syncthreads();
+    }
+}
+
+// Rows: one warp per row tile. Sums the tile's chunks in order, adds each
+// row's dL/dN_m and stores the tile's parameter partials (fixed order).
+template <int K>
+__global__ void __launch_bounds__(256)
+vjp_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
+                int ntile, int nch, double b0, double bbr, double bsh)
+{
+    __shared__ double fin[8][kVRows];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * 8 + w;
+    if (tile >= ntile) return;                    // whole warp
+    for (int r = lane; r < kVRows; r += 32) {
+        double s = 0.0;
+        for (int c = 0; c < nch; ++c) s += ws.vpart[(static_cast<size_t>(tile) * nch + c) * kVRows + r];
+        fin[w][r] = s;
+    }
+    __syncwarp();
+    VjpCellView v;
+    v.x = x; v.N = N; v.h = ws.h; v.lam = lam; v.D = ws.D; v.a = ws.a; v.ia = ws.ia;
+    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Ld = ws.Ld; v.lag0_scale = 1.0;
+    v.n = n;
+    v.geo = ws.mom[10] != 0.0;
+    const int I = tile * VW;
+    double gB = 0.0, gS = 0.0;
+    if (lane < VW && I + lane < n) {
+        double g;
+        vjp_tile_row<K>(v, I + lane, lane, fin[w], ws.mom, ws.mom + 5, b0, bbr, bsh, g, gB, gS);
+        gN[I + lane] += g;
+    }
+    double s0 = 0.0, s1 = 0.0;
+    for (int t = 0; t < VW; ++t) {
+        s0 += __shfl_sync(0xffffffffu, gB, t);
+        s1 += __shfl_sync(0xffffffffu, gS, t);
+    }
+    if (lane == 0) {
+        // slots: 0 beta0, 1 beta_br, 2 beta_sh
+        ws.gpart[tile * 4 + 0] = (K <= 2) ? s0 : 0.0;
+        ws.gpart[tile * 4 + 1] = (K == 3 || K == 5) ? s0 : 0.0;
+        ws.gpart[tile * 4 + 2] = (K == 4 || K == 5) ? s1 : 0.0;
     }
 }
 
@@ -238,21 +267,42 @@ brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
     }
 }
 
+// Partner chunks per row tile: the row tiles cost the same, so with ntile
+// tasks on 2 num_sms CTA slots the last wave can run half empty; pick the
+// chunk count (<= kVjpMaxChunks, chunks of >= 512 partners) whose waves come
+// closest to whole numbers, the smaller count on near ties.
+int vjp_chunks(int ntile, int num_sms, int n)
+{
+    const double slots = 2.0 * num_sms;
+    int best = 1;
+    double best_eff = 0.0;
+    for (int c = 1; c <= kVjpMaxChunks; ++c) {
+        if (c > 1 && n / c < 512) break;
+        const double w = ntile * c / slots;
+        const double eff = w / std::ceil(w);
+        if (eff > best_eff + 0.02) { best_eff = eff; best = c; }
+    }
+    return best;
+}
+
 template <int K>
 cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStream_t s)
 {
     const int n = a.n;
     const int nb = (n + kPrepThreads - 1) / kPrepThreads;
     const int ntile = (n + VW - 1) / VW;
-    const int grid = ntile < 2 * num_sms ? ntile : 2 * num_sms;
+    const int nch = vjp_chunks(ntile, num_sms, n);
+    const int ntasks = ntile * nch;
+    const int grid = ntasks < 2 * num_sms ? ntasks : 2 * num_sms;
     const size_t smem = sizeof(double) * kVRows * kMainThreads;
     cudaError_t e = cudaFuncSetAttribute(vjp_main_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     vjp_prep_kernel<<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
     vjp_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
-    vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, a.beta0,
-                                                         a.beta_br, a.beta_sh);
+    vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, ws, n, ntile, nch);
+    vjp_rows_kernel<K><<<(ntile + 7) / 8, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, nch,
+                                                       a.beta0, a.beta_br, a.beta_sh);
     vjp_gfin_kernel<<<1, 256, 0, s>>>(ntile, ws, a.gp, 3);
     return cudaGetLastError();
 }

@@ -57,9 +57,12 @@ struct VjpShared {
 
 // Row sums of the task's rows into sm.fin[G.g]; red: the group's first column
 // of the kVRows x kMainThreads reduction buffer (row stride kMainThreads).
+// Row sums over the partner range [r_begin, r_end) (lags on a geometric
+// grid, partner indices otherwise); the whole range is [0, n).
 template <int K>
-__device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I, double* red,
-                                                    VjpShared& sm, const TileGroup& G)
+__device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I, int r_begin,
+                                                    int r_end, double* red, VjpShared& sm,
+                                                    const TileGroup& G)
 {
     constexpr int VW = kVW;
     constexpr int RS = kMainThreads;
@@ -78,7 +81,7 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
     for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; R2[t] = 0.0; }
 
     if (v.geo) {
-        for (int d = lane; d < n; d += T) {
+        for (int d = r_begin + lane; d < r_end; d += T) {
             const int L = __ldg(v.Ld + d);
             const double sc = (d == 0) ? v.lag0_scale : 1.0;
             const double Bf = __ldg(v.Bf + d) * sc, Sf = __ldg(v.Sf + d) * sc;
@@ -108,8 +111,9 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
                     }
                 }
             }
-            // lower visits: partner k = m - d (d >= 1)
-            if (d >= 1 && L < kLagClipAll) {
+            // lower visits: partner k = m - d (d >= 1); a lag whose every pair
+            // is clipped (L = kLagClipAll) gives lo >= n - 1 -> P = lambda_{n-1}
+            if (d >= 1) {
                 const int e = L - d;
 #pragma unroll
                 for (int t = 0; t < VW; ++t) {
@@ -135,30 +139,14 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
                         }
                     }
                 }
-            } else if (d >= 1) {
-                // every pair of this lag is clipped: P = lambda_{n-1}
-#pragma unroll
-                for (int t = 0; t < VW; ++t) {
-                    const int m = I + t, k = m - d;
-                    if (t < tmax && k >= 0) {
-                        if constexpr (K == 2) {
-                            R0[t] = fma(lamlast, __ldg(h + k), R0[t]);
-                        } else {
-                            const double Nk = __ldg(N + k);
-                            if constexpr (K == 0) R0[t] = fma(lamlast, Nk, R0[t]);
-                            if constexpr (K == 1) { R0[t] = fma(lamlast, Nk, R0[t]); R1[t] = fma(lamlast, __ldg(h + k), R1[t]); }
-                            if constexpr (K == 3 || K == 5) R0[t] = fma(lamlast * Nk, Bf, R0[t]);
-                            if constexpr (K == 4 || K == 5) R2[t] = fma(lamlast * __ldg(h + k), Sf, R2[t]);
-                        }
-                    }
-                }
             }
         }
     } else {
         // generic grid: thread `lane` owns the partner chunk [k0, k1) and walks
         // the bracket of x_m + x_k upward along it for every row of the tile
-        const int chunk = (n + T - 1) / T;
-        const int k0 = min(n, lane * chunk), k1 = min(n, k0 + chunk);
+        const int span = r_end - r_begin;
+        const int chunk = (span + T - 1) / T;
+        const int k0 = min(r_end, r_begin + lane * chunk), k1 = min(r_end, k0 + chunk);
         const long long blast = dbits(x[n - 1]);
 #pragma unroll 1
         for (int t = 0; t < tmax; ++t) {
