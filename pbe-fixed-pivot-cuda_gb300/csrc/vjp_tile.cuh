@@ -81,6 +81,9 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
     for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; R2[t] = 0.0; }
 
     if (v.geo) {
+        // two passes over the lags (upper visits, then lower visits), so each
+        // hot loop is half the code: the unrolled 12-row body with the inlined
+        // weight emulation otherwise overflows the instruction cache
         for (int d = r_begin + lane; d < r_end; d += T) {
             const int L = __ldg(v.Ld + d);
             const double sc = (d == 0) ? v.lag0_scale : 1.0;
@@ -111,32 +114,35 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
                     }
                 }
             }
+        }
+        for (int d = r_begin + lane; d < r_end; d += T) {
             // lower visits: partner k = m - d (d >= 1); a lag whose every pair
             // is clipped (L = kLagClipAll) gives lo >= n - 1 -> P = lambda_{n-1}
-            if (d >= 1) {
-                const int e = L - d;
+            if (d == 0) continue;
+            const int L = __ldg(v.Ld + d);
+            const double Bf = __ldg(v.Bf + d), Sf = __ldg(v.Sf + d);
+            const int e = L - d;
 #pragma unroll
-                for (int t = 0; t < VW; ++t) {
-                    const int m = I + t, k = m - d;
-                    if (t < tmax && k >= 0) {
-                        const int lo = m + e;
-                        double P;
-                        if (lo >= n - 1) {
-                            P = lamlast;
-                        } else {
-                            const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
-                                                               __ldg(x + lo), 0);
-                            P = fma(th, __ldg(D + lo), __ldg(lam + lo));
-                        }
-                        if constexpr (K == 2) {
-                            R0[t] = fma(P, __ldg(h + k), R0[t]);
-                        } else {
-                            const double Nk = __ldg(N + k);
-                            if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
-                            if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(h + k), R1[t]); }
-                            if constexpr (K == 3 || K == 5) R0[t] = fma(P * Nk, Bf, R0[t]);
-                            if constexpr (K == 4 || K == 5) R2[t] = fma(P * __ldg(h + k), Sf, R2[t]);
-                        }
+            for (int t = 0; t < VW; ++t) {
+                const int m = I + t, k = m - d;
+                if (t < tmax && k >= 0) {
+                    const int lo = m + e;
+                    double P;
+                    if (lo >= n - 1) {
+                        P = lamlast;
+                    } else {
+                        const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
+                                                           __ldg(x + lo), 0);
+                        P = fma(th, __ldg(D + lo), __ldg(lam + lo));
+                    }
+                    if constexpr (K == 2) {
+                        R0[t] = fma(P, __ldg(h + k), R0[t]);
+                    } else {
+                        const double Nk = __ldg(N + k);
+                        if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
+                        if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(h + k), R1[t]); }
+                        if constexpr (K == 3 || K == 5) R0[t] = fma(P * Nk, Bf, R0[t]);
+                        if constexpr (K == 4 || K == 5) R2[t] = fma(P * __ldg(h + k), Sf, R2[t]);
                     }
                 }
             }
