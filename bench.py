@@ -57,8 +57,9 @@ FLOPS_PER_FRAGMENT = 8   # per breakage fragment
 # lags with lo = k: q (DMUL, DFMA) + R (DADD) + TH (DFMA) = 4. The weight
 # numerator runs on the integer pipe. fp64_instr_per_launch() counts the
 # evaluations of both kinds the kernel performs on a given grid (each 12-bin
-# tile also evaluates its left neighbour slot); profiles/ cross-checks the
-# count with the SASS instruction counters.
+# tile also evaluates its left neighbour slot), plus 4 per clipped pair (the
+# clip tasks); profiles/ cross-checks the count with the SASS instruction
+# counters.
 FP64_PHASE1, FP64_PHASE2, TILE_W = 5, 4, 12
 
 
@@ -67,6 +68,10 @@ def fp64_instr_per_launch(x) -> int:
     v = x[0] + x
     L = np.searchsorted(x, v, side="right") - 1          # bracket of x_0 + x_d
     L = np.where(v >= x[-1], 1 << 30, L)
+    # clipped pairs (summed by the clip tasks): rate (3) + accumulation (1)
+    d_all = np.arange(n)
+    jlo = np.where(L >= (1 << 30), 0, np.maximum(0, n - 1 - L))
+    clipped = int(np.maximum(0, (n - 1 - d_all) - jlo + 1).sum())
     e0 = np.flatnonzero(L == np.arange(n))
     D0 = int(e0[0]) if len(e0) else n
     total = 0
@@ -78,7 +83,7 @@ def fp64_instr_per_launch(x) -> int:
         tlo = np.maximum(0, L - I + 1)
         cnt = np.where(ok, np.maximum(0, thi - tlo + 1), 0)
         total += FP64_PHASE1 * int(cnt[d_idx < D0].sum()) + FP64_PHASE2 * int(cnt[d_idx >= D0].sum())
-    return total
+    return total + 4 * clipped
 # dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
 # this workload, from the ncu capture in profiles/agg_main_kernel_n16384.md.
 MAIN_KERNEL_DRAM_BYTES = 1343488

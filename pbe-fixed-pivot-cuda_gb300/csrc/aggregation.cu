@@ -26,12 +26,14 @@
 //    the pairs at n = 16384) N_k is a per-slot constant and is factored out.
 //  * Generic grids: per-pair brackets by a monotone walk over k, beta from
 //    per-bin cube roots.
-//  * Pairs clipped at x[n-1] are summed by a separate kernel (per lag on a
-//    geometric grid, per row otherwise).
+//  * Pairs clipped at x[n-1] are summed by up to 32 extra tasks of the main
+//    kernel (interleaved lags on a geometric grid, rows otherwise); in gather
+//    mode the last of them and of the task owning bin n-1 adds their parts, in
+//    order, to rhs[n-1].
 //
 // Kernels per call: prep (per-bin values, lag tables, moment partials,
-// geometric check) -> clip (clipped pairs; block 0 also finishes moments,
-// flag and counter) -> main (persistent CTAs pulling target tiles from an atomic counter, largest
+// geometric check; its last block finishes moments, flag and counters) ->
+// main (persistent CTAs pulling target tiles from an atomic counter, largest
 // first). GATHER mode: one CTA owns each output bin and reduces it in a fixed
 // order -> bitwise reproducible. SCATTER mode: geometric tasks are (tile, lag
 // chunk) and flush with FP64 atomicAdd.
@@ -110,94 +112,110 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     __syncthreads();
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
     __syncthreads();
+    __shared__ int last_s;
     if (threadIdx.x == 0) {
         double mx = 0.0;
         for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
         ws.mom_part[blockIdx.x * 8 + 5] = mx;
         ws.mom_part[blockIdx.x * 8 + 6] = static_cast<double>(d0_s);
+        __threadfence();                       // partials visible before the ticket
+        last_s = (atomicAdd(ws.counter + 2, 1) == static_cast<int>(gridDim.x) - 1);
+    }
+    __syncthreads();
+    if (!last_s) return;
+    // The last block to finish reduces every block's partials (read through L2)
+    // in a fixed order: moments, geometric flag, first lag with Ld[d] == d,
+    // counters of the main kernel. No block waits for another.
+    __threadfence();
+    const int nb = gridDim.x;
+    // warps 0-4: one moment each; warp 5: largest deviation; warp 6: smallest
+    // D0 candidate (lanes stride over the blocks, fixed butterflies)
+    const int wq = threadIdx.x >> 5, lq = threadIdx.x & 31;
+    if (wq < 5) {
+        double t = 0.0;
+        for (int b = lq; b < nb; b += 32) t += __ldcg(ws.mom_part + b * 8 + wq);
+        t = warp_sum(t);
+        if (lq == 0) ws.mom[wq] = t;
+    } else if (wq == 5) {
+        double m5 = 0.0;
+        for (int b = lq; b < nb; b += 32) m5 = fmax(m5, __ldcg(ws.mom_part + b * 8 + 5));
+        m5 = warp_max(m5);
+        if (lq == 0) sh[0] = m5;
+    } else if (wq == 6) {
+        int dmin = n;
+        for (int b = lq; b < nb; b += 32)
+            dmin = min(dmin, static_cast<int>(__ldcg(ws.mom_part + b * 8 + 6)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmin = min(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+        if (lq == 0) d0_s = dmin;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double mx = sh[0];
+        // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
+        // its bracket pivot (precondition of sum_minus_scaled)
+        const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
+        ws.mom[5] = geo ? 1.0 : 0.0;
+        ws.mom[6] = mx;
+        ws.counter[0] = 0;          // task counter of the main kernel
+        ws.counter[1] = d0_s;       // lags d >= counter[1] have lo(j, j+d) = j + d
+        ws.counter[3] = 0;          // contributors to bin n-1 done (clip tasks + top tile)
     }
 }
 
-// clip: sum of rates of the pairs with x_j + x_k >= x[n-1] (all deposited on
-// bin n-1, src/aggregation_kernels.cuh:191-192). One warp per lag d on a
-// geometric grid (pairs j in [n-1-Ld, n-1-d]); one warp per row j otherwise
-// (k from the first clipped column to n-1).
-// Every block first reduces the prep partials' geometric deviation (a few
-// dozen L2 reads) to decide the path; block 0 also finishes the moments
-// (fixed-order sums), the geometric flag, the first lag with Ld[d] == d and
-// the task counter for the main kernel, which runs after this kernel.
-template <int K, bool SCATTER>
-__global__ void __launch_bounds__(kClipWarps * 32)
-agg_clip_kernel(const double* __restrict__ N, const double* __restrict__ x, double* rhs,
-                int n, AggWs ws, double b0, double bbr, double bsh)
+// Clipped pairs (x_j + x_k >= x[n-1], all deposited on bin n-1,
+// src/aggregation_kernels.cuh:191-192), part c of nclip: the lags
+// d = c + nclip (lane + T k) on a geometric grid (pairs j in [n-1-Ld, n-1-d];
+// interleaving spreads the long lags near d = 0 over the parts), the rows
+// j = c + nclip (lane + T k) otherwise.
+template <int K>
+__device__ double clip_part_sum(const AggCellView& v, int c, int nclip, const TileGroup& G)
 {
-    __shared__ double sh[kClipWarps];
-    __shared__ int d0_s;
-    const int nb = (n + kPrepThreads - 1) / kPrepThreads;     // prep blocks
-    // every warp reduces the deviation partials itself (no block barrier)
-    double mx = 0.0;
-    for (int b = threadIdx.x & 31; b < nb; b += 32) mx = fmax(mx, ws.mom_part[b * 8 + 5]);
-    mx = warp_max(mx);
-    // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
-    // its bracket pivot (precondition of sum_minus_scaled)
-    const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
-    if (blockIdx.x == 0) {
-        if (threadIdx.x == 0) d0_s = n;
-        __syncthreads();
-        int d0 = n;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x)
-            d0 = min(d0, static_cast<int>(ws.mom_part[b * 8 + 6]));
-        atomicMin(&d0_s, d0);
-        for (int q = 0; q < 5; ++q) {
-            double t = 0.0;
-            for (int b = threadIdx.x; b < nb; b += blockDim.x) t += ws.mom_part[b * 8 + q];
-            t = block_sum(t, sh);
-            if (threadIdx.x == 0) ws.mom[q] = t;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            ws.mom[5] = geo ? 1.0 : 0.0;
-            ws.mom[6] = mx;
-            ws.counter[0] = 0;
-            ws.counter[1] = d0_s;     // lags d >= counter[1] have lo(j, j+d) = j + d
-        }
-    }
-    const int w = blockIdx.x * kClipWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
+    const int n = v.n;
     double acc = 0.0;
-    if (w < n) {
-        if (geo) {
-            const int d = w;
-            const int L = ws.Ld[d];
+    if (v.geo) {
+        for (int d = c + nclip * G.lane; d < n; d += nclip * G.T) {
+            const int L = v.Ld[d];
             const int jhi = n - 1 - d;
             const int jlo = (L >= kLagClipAll) ? 0 : max(0, n - 1 - L);
-            const double B = ws.Bd[d], S = ws.Sd[d];
-            for (int j = jlo + lane; j <= jhi; j += 32) {
-                const double hj = NeedH<K>::j ? ws.h[j] : 0.0;
-                const double hk = NeedH<K>::k ? ws.h[j + d] : 0.0;
-                acc += rate_geo<K>(B, S, N[j], hj, N[j + d], hk);
+            const double B = v.Bd[d], S = v.Sd[d];
+            for (int j = jlo; j <= jhi; ++j) {
+                const double hj = NeedH<K>::j ? v.Hj[j] : 0.0;
+                const double hk = NeedH<K>::k ? v.Hk[j + d] : 0.0;
+                acc += rate_geo<K>(B, S, v.Nj[j], hj, v.Nk[j + d], hk);
             }
-        } else {
-            const int j = w;
-            const double xj = x[j];
-            const long long tb = dbits(x[n - 1]);
+        }
+    } else {
+        const long long tb = dbits(v.x[n - 1]);
+        for (int j = c + nclip * G.lane; j < n; j += nclip * G.T) {
+            const double xj = v.x[j];
             int lo = j, hi = n - 1;   // xj + x[n-1] >= x[n-1] always holds
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (dbits(xj + x[mid]) >= tb) hi = mid; else lo = mid + 1;
+                if (dbits(xj + v.x[mid]) >= tb) hi = mid; else lo = mid + 1;
             }
-            const double Nj = N[j], hj = ws.h[j], aj = ws.a[j], iaj = ws.ia[j];
-            for (int k = lo + lane; k < n; k += 32)
-                acc += rate_gen<K>(j == k, b0, bbr, bsh, Nj, hj, aj, iaj, N[k], ws.h[k], ws.a[k], ws.ia[k]);
+            const double Nj = v.Nk[j], hj = v.Hk[j], aj = v.a[j], iaj = v.ia[j];
+            for (int k = lo; k < n; ++k)
+                acc += rate_gen<K>(j == k, v.b0, v.bbr, v.bsh, Nj, hj, aj, iaj, v.Nk[k], v.Hk[k],
+                                   v.a[k], v.ia[k]);
         }
     }
-    const double s = block_sum(acc, sh);
-    if (threadIdx.x == 0) {
-        if constexpr (SCATTER) { if (s != 0.0) atomicAdd(rhs + (n - 1), s); }
-        else ws.clip_part[blockIdx.x] = s;
-    }
+    return acc;
 }
 
+// Gather mode: the clip tasks and the task that owns bin n-1 each take a
+// ticket after their contribution is stored; the last of the nclip + 1 adds
+// the clip parts, in order, to rhs[n-1]. Called by one thread.
+__device__ __forceinline__ void clip_contributor_done(double* rhs, int n, const AggWs& ws,
+                                                      int nclip)
+{
+    __threadfence();
+    if (atomicAdd(ws.counter + 3, 1) != nclip) return;
+    __threadfence();
+    double s = 0.0;
+    for (int c = 0; c < nclip; ++c) s += __ldcg(ws.clip_part + c);
+    rhs[n - 1] = __ldcg(rhs + (n - 1)) + s;
+}
 
 // ---------------------------------------------------------------------------
 // main: persistent CTAs split into groups of T threads (agg_group_size); each
@@ -211,7 +229,7 @@ template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile, int nchunk,
-                int ntasks, double b0, double bbr, double bsh, int T)
+                int ntasks, int nclip, double b0, double bbr, double bsh, int T)
 {
     extern __shared__ double red[];               // [kRedRows][kMainThreads]
     __shared__ TileShared sm;
@@ -237,9 +255,25 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     for (;;) {
         if (lane == 0) s_task[g] = atomicAdd(ws.counter, 1);
         G.sync();
-        const int task = s_task[g];
+        int task = s_task[g];
         G.sync();
         if (task >= ntasks) break;
+
+        if (task < nclip) {
+            // a part of the pairs clipped at x[n-1]
+            const double sc = group_sum(clip_part_sum<K>(v, task, nclip, G), sm, G);
+            if (lane == 0) {
+                if constexpr (SCATTER) {
+                    if (sc != 0.0) atomicAdd(rhs + (n - 1), sc);
+                } else {
+                    ws.clip_part[task] = sc;
+                    clip_contributor_done(rhs, n, ws, nclip);
+                }
+            }
+            G.sync();
+            continue;
+        }
+        task -= nclip;
 
         int tile, chunk = 0;
         if (SCATTER && v.geo) { tile = ntile - 1 - task / nchunk; chunk = task % nchunk; }
@@ -258,15 +292,6 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         const int St = -ilogb(x[I]);
         agg_tile_accumulate<K>(v, I, d_begin, d_end, St, red + g * T, sm, G);
 
-        // clipped pairs of bin n-1 (gather: sum of the clip kernel's partials)
-        double clip = 0.0;
-        if (!SCATTER && I + W > n - 1) {
-            const int nbc = (n + kClipWarps - 1) / kClipWarps;
-            double s = 0.0;
-            for (int b = lane; b < nbc; b += T) s += ws.clip_part[b];
-            clip = group_sum(s, sm, G);
-        }
-
         if (lane < W) {
             const int i = I + lane;
             if (i < n) {
@@ -277,8 +302,8 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                     const double val = birth - death;
                     if (val != 0.0) atomicAdd(rhs + i, val);
                 } else {
-                    if (i == n - 1) birth += clip;
                     rhs[i] = rhs[i] + (birth - death);
+                    if (i == n - 1) clip_contributor_done(rhs, n, ws, nclip);
                 }
             }
         }
@@ -304,15 +329,23 @@ int agg_group_size(long long ntasks, int num_sms)
     return 256;
 }
 
+// Tasks that sum the clipped pairs (about n + q^2 pairs on a grid with q bins
+// per octave, more on generic grids), spread over parts of ~1024 lags or rows.
+int agg_clip_tasks(int n)
+{
+    const int c = (n + 1023) / 1024;
+    return c < 1 ? 1 : (c > kMaxClipTasks ? kMaxClipTasks : c);
+}
+
 template <int K, bool SC>
 cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_t s)
 {
     const int n = a.n;
     const int nb = agg_prep_blocks(n);
-    const int nbc = agg_clip_blocks(n);
     const int ntile = (n + W - 1) / W;
     const int nchunk = SC ? (n + kScatterChunk - 1) / kScatterChunk : 1;
-    const long long ntasks_ll = static_cast<long long>(ntile) * nchunk;
+    const int nclip = agg_clip_tasks(n);
+    const long long ntasks_ll = static_cast<long long>(ntile) * nchunk + nclip;
     if (ntasks_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int ntasks = static_cast<int>(ntasks_ll);
     const int T = agg_group_size(ntasks, num_sms);
@@ -323,13 +356,14 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(ws.counter, 0, 8 * sizeof(int), s);   // prep's block tickets
+    if (e != cudaSuccess) return e;
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
-    agg_clip_kernel<K, SC><<<nbc, kClipWarps * 32, 0, s>>>(a.N, a.x, a.rhs, n, ws, a.beta0,
-                                                          a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
     agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, nchunk,
-                                                            ntasks, a.beta0, a.beta_br, a.beta_sh, T);
+                                                            ntasks, nclip, a.beta0, a.beta_br,
+                                                            a.beta_sh, T);
     if (prof) cudaEventRecord(g_prof_stop, s);
     return cudaGetLastError();
 }

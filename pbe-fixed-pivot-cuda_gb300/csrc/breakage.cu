@@ -41,36 +41,51 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const double* __restrict__ t_q, const double* __restrict__ bw_q, int n, int nq,
                 BrkWs ws, double S0, double v_ref, double alpha, double v_min)
 {
+    __shared__ double sh[8];
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= static_cast<long long>(n) * nq) return;
-    const int q = static_cast<int>(idx / n);
-    const int j = static_cast<int>(idx - static_cast<long long>(q) * n);
-    const double xj = x[j], Nj = N[j];
-    const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
-    const bool active = (S != 0.0) && (Nj > kBreakageNMin);
-    const double tq = t_q[q];
-    const double contrib = active ? S * Nj * bw_q[q] : 0.0;
-    const double v = xj * tq;
-    const int lo = frag_bracket(x, n, v);
-    double clo, chi;
-    frag_shares(x, n, lo, v, contrib, clo, chi);
-    ws.clo[idx] = clo;
-    ws.chi[idx] = chi;
-    // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
-    int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-    const int lo_prev = (j == 0) ? -2 : frag_bracket(x, n, x[j - 1] * tq);
-    for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
-    if (j == n - 1)
-        for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
-    if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
+    const bool live = idx < static_cast<long long>(n) * nq;   // every lane takes part in the shuffle
+    const int lane = threadIdx.x & 31;
+    int q = 0, j = 0, lo = -2;
+    double clipped = 0.0;
+    double tq = 0.0;
+    if (live) {
+        q = static_cast<int>(idx / n);
+        j = static_cast<int>(idx - static_cast<long long>(q) * n);
+        const double xj = x[j], Nj = N[j];
+        const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
+        const bool active = (S != 0.0) && (Nj > kBreakageNMin);
+        tq = t_q[q];
+        const double contrib = active ? S * Nj * bw_q[q] : 0.0;
+        const double v = xj * tq;
+        lo = frag_bracket(x, n, v);
+        double clo, chi;
+        frag_shares(x, n, lo, v, contrib, clo, chi);
+        ws.clo[idx] = clo;
+        ws.chi[idx] = chi;
+        if (lo < 0) clipped = clo;               // all of it goes to bin 0
+        if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
+    }
+    // bracket of the previous parent's fragment (same q): the lane below has it
+    const int lo_left = __shfl_up_sync(0xffffffffu, lo, 1);
+    if (live) {
+        // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
+        int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+        const int lo_prev = (j == 0) ? -2 : (lane > 0 ? lo_left : frag_bracket(x, n, x[j - 1] * tq));
+        for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
+        if (j == n - 1)
+            for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
+    }
+    // this block's fragments clipped below x[0], summed in a fixed order
+    const double cs = block_sum(clipped, sh);
+    if (threadIdx.x == 0) ws.clipsum[blockIdx.x] = cs;
 }
 
 // Output bins in groups of 32/nqp per warp, nqp = n_quad rounded up to a power
 // of two (<= 32): lane l works on bin base + l / nqp and quadrature points
 // q = l % nqp (+ nqp, ...), walking that q's few fragments of brackets i-1 and
 // i; a fixed butterfly over the nqp lanes sums them. Bin 0 also collects every
-// fragment clipped below x[0] (up to thousands per q on fine grids): the
-// warp holding bin 0 sums those first, all 32 lanes striding over them.
+// fragment clipped below x[0] (thousands on fine grids), pre-summed per prep
+// block.
 __global__ void __launch_bounds__(256)
 brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 {
@@ -81,17 +96,13 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
     const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     const int base = warp * per_warp;
-    // fragments clipped below x[0] (all deposited on bin 0): block 0 sums them
-    // with all its threads, q by q, in a fixed order
+    // fragments clipped below x[0] (all deposited on bin 0): block 0 adds the
+    // prep blocks' sums in a fixed order
     double clipped = 0.0;
     if (blockIdx.x == 0) {
+        const int nbp = static_cast<int>((static_cast<long long>(n) * nq + 255) / 256);
         double part = 0.0;
-        for (int q = 0; q < nq; ++q) {
-            const int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-            const double* clo = ws.clo + static_cast<long long>(q) * n;
-            const int fb = min(max(fq[1], 0), n);       // fragments with lo == -1
-            for (int j = threadIdx.x; j < fb; j += blockDim.x) part += clo[j];
-        }
+        for (int b = threadIdx.x; b < nbp; b += blockDim.x) part += ws.clipsum[b];
         clipped = block_sum(part, sh);
     }
     if (base >= n) return;                   // whole warp
@@ -107,6 +118,7 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
             const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
             const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
             if (i > 0) for (int j = fa; j < fb; ++j) acc += chi[j];   // lo == i-1
+            // (lo == -1 for i == 0: the clipped fragments, added below)
             for (int j = fb; j < fc; ++j) acc += clo[j];              // lo == i
         }
     }

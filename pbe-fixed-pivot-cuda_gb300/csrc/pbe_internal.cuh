@@ -22,7 +22,7 @@ namespace pbe_gb300 {
 constexpr int kTileW        = 12;    // output bins owned by one task (125 regs, no spill)
 constexpr int kMainThreads  = 256;   // threads per aggregation task CTA
 constexpr int kPrepThreads  = 256;
-constexpr int kClipWarps    = 8;     // warps per block of the clip kernel
+constexpr int kMaxClipTasks = 32;    // tasks summing the pairs clipped at x[n-1]
 constexpr int kScatterChunk = 2048;  // lags per task in scatter mode
 constexpr int kRedRows      = 2 * (kTileW + 1);   // R[0..W], TH[0..W]
 
@@ -167,12 +167,12 @@ struct AggWs {
     int*    Ld;        // [n]  bracket offset of lag d: lo(j, j+d) = j + Ld[d]
     double* mom_part;  // [nb_prep * 8] per-block moment partials
     double* mom;       // [8]  M_{-1/3}, M_0, M_{1/3}, M_{2/3}, M_1, geo flag, max dev
-    double* clip_part; // [nb_clip] per-block sums of clipped pair rates
-    int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d
+    double* clip_part; // [kMaxClipTasks] sums of clipped pair rates, one per clip task
+    int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d,
+                       //      [2] prep blocks done, [3] bin n-1 contributors done
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
-constexpr int agg_clip_blocks(int n) { return (n + kClipWarps - 1) / kClipWarps; }
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -184,7 +184,7 @@ constexpr size_t agg_ws_bytes(int n)
     return 6 * dn + align256(sizeof(int) * static_cast<size_t>(n))
          + align256(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n)))
          + align256(sizeof(double) * 8)
-         + align256(sizeof(double) * static_cast<size_t>(agg_clip_blocks(n)))
+         + align256(sizeof(double) * kMaxClipTasks)
          + align256(sizeof(int) * 8);
 }
 
@@ -204,7 +204,7 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.Ld        = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(n)));
     w.mom_part  = reinterpret_cast<double*>(take(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n))));
     w.mom       = reinterpret_cast<double*>(take(sizeof(double) * 8));
-    w.clip_part = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(agg_clip_blocks(n))));
+    w.clip_part = reinterpret_cast<double*>(take(sizeof(double) * kMaxClipTasks));
     w.counter   = reinterpret_cast<int*>(take(sizeof(int) * 8));
     if (ws) *ws = w;
     return off;
@@ -218,6 +218,7 @@ struct BrkWs {
     double* chi;   // [nq * n]  share deposited at lo + 1
     int*    first; // [nq * (n + 2)]  first[q][m+1] = first j with lo(q, j) >= m, m in [-1, n]
     double* SN;    // [n]  S(x_j) N_j (0 where the guard skips bin j)
+    double* clipsum; // [nq * n / 256] per prep block: shares clipped below x[0]
 };
 
 inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
@@ -230,6 +231,7 @@ inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
     w.chi   = reinterpret_cast<double*>(take(sizeof(double) * m));
     w.first = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(nq) * (static_cast<size_t>(n) + 2)));
     w.SN    = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(n)));
+    w.clipsum = reinterpret_cast<double*>(take(sizeof(double) * ((m + 255) / 256)));
     if (ws) *ws = w;
     return off;
 }

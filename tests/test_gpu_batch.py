@@ -212,3 +212,40 @@ def test_batch_plan_rejects_bad_input():
         pg.BatchPlan(g, [10], [0], -1, -1)                  # nothing to compute
     with pg.BatchPlan(g, [10, 20], [0, 0], 5) as plan:
         assert plan.rhs(0, 0, 0) == pg.ERR_INVALID_DEVICE_POINTER
+
+
+@pytest.mark.parametrize("kernel,selection", [(3, -1), (-1, 2), (1, 0)])
+def test_batch_rk4_single_term_plans_match_oracle(kernel, selection):
+    """RK4 graph of plans with only aggregation, only breakage, or Sum +
+    constant selection, against the oracle's rk4_step per cell."""
+    import torch
+
+    rng = np.random.default_rng(40 + kernel)
+    grids = [pg.grids.geometric_pow2(120, 1e-21, 8.0), make_grid("generic", 120, rng)]
+    cell_n = np.array([120, 37, 1, 90])
+    cell_grid = np.array([0, 1, 0, 1])
+    N = [pg.grids.lognormal_ic(grids[g][:n], max(0, n // 4), 1.0, 1e12, cut=5.0)
+         for g, n in zip(cell_grid, cell_n)]
+    k = [kk for kk in AGG_KERNELS if kk[0] == max(kernel, 0)][0]
+    v_ref = np.array([grids[g][n // 2] for g, n in zip(cell_grid, cell_n)])
+    # coefficients that keep every rate well inside RK4's stability region
+    params = pg.batch.cell_params(len(cell_n), beta0=1e-20, beta_br=k[2], beta_sh=k[3],
+                                  S0=1e-3, v_ref=v_ref, alpha=1.2)
+    t_q, bw_q = pg.quadrature.uniform(4)
+    dt, steps = 0.5, 3
+    with pg.BatchPlan(grids, cell_n, cell_grid, kernel, selection, t_q, bw_q) as plan:
+        dN = t(np.concatenate(N))
+        assert plan.rk4(dN, t(params), dt, steps) == 0
+        torch.cuda.synchronize()
+        got = plan.split(dN.cpu().numpy())
+    for c in range(len(cell_n)):
+        x = grids[cell_grid[c]][:cell_n[c]]
+        p = params[c]
+        ref = N[c].copy()
+        agg = dict(kernel=kernel, beta0=p[0], beta_br=p[1], beta_sh=p[2]) if kernel >= 0 else None
+        brk = (dict(t_q=t_q, bw_q=bw_q, selection=selection, S0=p[3], v_ref=p[4], alpha=p[5],
+                    v_min=p[6]) if selection >= 0 else None)
+        for _ in range(steps):
+            ref = pyoracle.rk4_step(ref, x, dt, agg=agg, brk=brk)
+        np.testing.assert_allclose(got[c], ref, rtol=1e-11, atol=1e-11 * np.abs(N[c]).max(),
+                                   err_msg="k=%d sel=%d cell %d" % (kernel, selection, c))
