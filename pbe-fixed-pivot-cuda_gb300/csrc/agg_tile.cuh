@@ -3,8 +3,8 @@
 // kernel (aggregation.cu) and the batched-cell kernel (batch_kernels.cu).
 //
 // A tile task owns the kTileW output bins [I, I + kTileW) of one cell and
-// accumulates, for the slots s = I-1 .. I+kTileW-1, R_s = sum of the rates of
-// the pairs whose bracket is lo = s and TH_s = sum rate * (v - x_s) 2^St
+// accumulates, for its slots s, R_s = sum of the rates of the pairs whose
+// bracket is lo = s and TH_s = sum rate * (v - x_s) 2^St
 // (reference: src/aggregation_kernels.cuh:145-239, regrouped; the file header
 // of aggregation.cu gives the derivation). A task runs on a "group" of T
 // threads (T = 32, 64, 128 or 256, a runtime value) synchronised by a named
@@ -118,12 +118,22 @@ struct AggCellView {
 
 constexpr int kMaxGroups = kMainThreads / 32;
 
+// Slots of a tile task. Without carry: s = I-1 .. I+W-1, slot I-1 feeding only
+// the w-part of bin I, so every pair on a tile boundary is evaluated by both
+// tiles. With carry: s = I .. I+W-1; the w-part of slot I+W-1 leaves the task
+// as a carry into bin I+W, which the neighbour tile combines.
+template <bool CARRY> struct TileSlots {
+    static constexpr int first = CARRY ? 0 : -1;        // slot t is s = I + first + t
+    static constexpr int count = CARRY ? kTileW : kTileW + 1;
+    static constexpr int rows = 2 * count;              // R[0..count), TH[0..count)
+};
+
 // Static shared memory of a CTA running tile tasks (per group g < kMaxGroups).
 struct TileShared {
-    double xs[kMaxGroups][kTileW + 2];    // x[I-1 .. I+W]
+    double xs[kMaxGroups][kTileW + 2];    // x of the task's slots and of the pivot above
     double fs[kMaxGroups][kTileW + 2];    // per-slot factor
     double part[kMaxGroups][kRedRows];    // 32-column chunk partials (chunk index g*T/32 + c)
-    double fin[kMaxGroups][kRedRows];     // R[0..W], TH[0..W] of the task
+    double fin[kMaxGroups][kRedRows];     // R and TH of the task's slots
     double wsum[kMaxGroups];              // per-warp partials of group sums
     double extra[kMaxGroups][kTileW];     // per-bin additions (batched breakage)
     double cinfo[kMaxGroups][8];          // per-task cell values for the epilogue (batched)
@@ -158,21 +168,24 @@ __device__ __forceinline__ double group_sum(double v, TileShared& sm, const Tile
 // (geometric grid) or over every row (generic grid) into sm.fin[G.g].
 // red: this group's first column of the CTA's kRedRows x kMainThreads
 // reduction buffer (row stride kMainThreads). St: exponent shift of the
-// weight numerators (-ilogb(x[I])).
-template <int K>
+// weight numerators (-ilogb(x[max(I, 0)])). I may be negative (a tile whose
+// lowest bins lie below bin 0).
+template <int K, bool CARRY>
 __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I, int d_begin,
                                                     int d_end, int St, double* red,
                                                     TileShared& sm, const TileGroup& G)
 {
     constexpr int W = kTileW;
+    constexpr int NS = TileSlots<CARRY>::count;
     constexpr int RS = kMainThreads;     // row stride of red
     const int n = v.n;
     const int lane = G.lane, T = G.T;
+    const int base = I + TileSlots<CARRY>::first;   // slot of t = 0
     const int smax = min(I + W - 1, n - 2);     // highest non-clipped slot
     double* xs = sm.xs[G.g];
     double* fs = sm.fs[G.g];
-    if (lane < W + 2) {
-        const int s = I - 1 + lane;
+    if (lane < NS + 1) {
+        const int s = base + lane;
         const bool in = (s >= 0 && s < n);
         xs[lane] = in ? v.x[s] : 0.0;
         fs[lane] = in ? v.Fs[s] : 0.0;
@@ -181,10 +194,10 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
     G.sync();
 
     if (v.geo) {
-        double R[W + 1], TH[W + 1];
+        double R[NS], TH[NS];
 #pragma unroll
-        for (int t = 0; t <= W; ++t) { R[t] = 0.0; TH[t] = 0.0; }
-        const int thi = smax - (I - 1);   // slot index t <= thi
+        for (int t = 0; t < NS; ++t) { R[t] = 0.0; TH[t] = 0.0; }
+        const int thi = smax - base;      // slot index t <= thi
         // lags d >= D0 put every pair on its larger member's own slot (lo = k)
         const int D0 = (K == 1) ? n : v.D0;
         const double* __restrict__ Nj_ = v.Nj;
@@ -198,10 +211,10 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
             const int L = __ldg(v.Ld + d);
             if (L > smax) { d = d_end; break; }   // Ld is nondecreasing in d
             const double B = __ldg(v.Bd + d), S = __ldg(v.Sd + d);
-            const int jb = I - 1 - L;      // j of slot t is jb + t, k = jb + d + t
+            const int jb = base - L;       // j of slot t is jb + t, k = jb + d + t
             const int tlo = max(0, -jb);
 #pragma unroll
-            for (int t = 0; t <= W; ++t) {
+            for (int t = 0; t < NS; ++t) {
                 if (t >= tlo && t <= thi) {
                     const int j = jb + t, k = j + d;
                     const double Nj = __ldg(Nj_ + j), Nk = __ldg(Nk_ + k);
@@ -211,15 +224,15 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
                     // (fl(x_j + x_k) - x_lo) 2^St on the integer pipe, bit-identical
                     // to the reference's two FP64 additions
                     const double th = sum_minus_scaled(__ldg(x_ + k), __ldg(x_ + j), xs[t], St);
-                    if (t > 0) R[t] += rate;
+                    if (CARRY || t > 0) R[t] += rate;
                     TH[t] = fma(rate, th, TH[t]);
                 }
             }
         }
 #pragma unroll
-        for (int t = 0; t <= W; ++t) {
+        for (int t = 0; t < NS; ++t) {
             red[t * RS + lane] = R[t];
-            red[(W + 1 + t) * RS + lane] = TH[t];
+            red[(NS + t) * RS + lane] = TH[t];
             R[t] = 0.0;
             TH[t] = 0.0;
         }
@@ -230,36 +243,36 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
                 const int L = __ldg(v.Ld + d);
                 if (L > smax) break;
                 const double B = __ldg(v.Bd + d), S = __ldg(v.Sd + d);
-                const int jb = I - 1 - L;
+                const int jb = base - L;
                 const int tlo = max(0, -jb);
 #pragma unroll
-                for (int t = 0; t <= W; ++t) {
+                for (int t = 0; t < NS; ++t) {
                     if (t >= tlo && t <= thi) {
                         const int j = jb + t;
                         const double Nj = __ldg(Nj_ + j);
                         const double hj = NeedH<K>::j ? __ldg(Hj_ + j) : 0.0;
                         const double q = q_slot<K>(B, S, Nj, hj);
                         const double th = sum_minus_scaled(xs[t], __ldg(x_ + j), xs[t], St);
-                        if (t > 0) R[t] += q;
+                        if (CARRY || t > 0) R[t] += q;
                         TH[t] = fma(q, th, TH[t]);
                     }
                 }
             }
 #pragma unroll
-            for (int t = 0; t <= W; ++t) {
+            for (int t = 0; t < NS; ++t) {
                 double* r0 = red + t * RS + lane;
-                double* r1 = red + (W + 1 + t) * RS + lane;
+                double* r1 = red + (NS + t) * RS + lane;
                 *r0 = fma(fs[t], R[t], *r0);
                 *r1 = fma(fs[t], TH[t], *r1);
             }
         }
     } else {
 #pragma unroll
-        for (int r = 0; r < kRedRows; ++r) red[r * RS + lane] = 0.0;
-        const int s_first = max(I - 1, 0);
+        for (int r = 0; r < 2 * NS; ++r) red[r * RS + lane] = 0.0;
+        const int s_first = max(base, 0);
         if (smax >= s_first) {
-            const int t_first = s_first - (I - 1);
-            const int t_last = smax - (I - 1);
+            const int t_first = s_first - base;
+            const int t_last = smax - base;
             const long long blo = dbits(xs[t_first]);
             const long long bhi = dbits(xs[t_last + 1]);
             const double* __restrict__ xsc = v.x;
@@ -289,7 +302,7 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
                     const long long vb = dbits(vs);
                     while (t < t_last && dbits(xs[t + 1]) <= vb) {
                         red[t * RS + lane] += Rc;
-                        red[(W + 1 + t) * RS + lane] += THc;
+                        red[(NS + t) * RS + lane] += THc;
                         Rc = 0.0; THc = 0.0; ++t;
                     }
                     const double rate = rate_gen<K>(j == k, v.b0, v.bbr, v.bsh, Nj, hj, aj, iaj,
@@ -298,7 +311,7 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
                     THc = fma(rate, scale_pow2(vs - xs[t], St20), THc);
                 }
                 red[t * RS + lane] += Rc;
-                red[(W + 1 + t) * RS + lane] += THc;
+                red[(NS + t) * RS + lane] += THc;
             }
         }
     }
@@ -308,7 +321,7 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
     // rotated by the worker's lane so the chunk reads hit distinct banks),
     // then the chunks of a row in order
     const int nch = T >> 5;
-    if (lane < kRedRows * nch) {
+    if (lane < 2 * NS * nch) {
         const int r = lane / nch, c = lane - r * nch;
         const double* p = red + r * RS + c * 32;
         const int rot = lane & 31;
@@ -318,7 +331,7 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
         sm.part[G.g * nch + c][r] = s;
     }
     G.sync();
-    if (lane < kRedRows) {
+    if (lane < 2 * NS) {
         double s = 0.0;
         for (int c = 0; c < nch; ++c) s += sm.part[G.g * nch + c][lane];
         sm.fin[G.g][lane] = s;
@@ -326,17 +339,32 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
     G.sync();
 }
 
-// Birth of bin i = I + t from the task's slot sums (TH carried times 2^St).
+// Birth of bin i = I + t (0 <= i < n) from the task's slot sums (TH carried
+// times 2^St). With carry, bin I lacks the w-part of slot I-1 (the lower
+// neighbour's carry).
+template <bool CARRY>
 __device__ __forceinline__ double agg_tile_birth(const AggCellView& v, int I, int t, int St,
                                                  const double* fin)
 {
-    constexpr int W = kTileW;
+    constexpr int NS = TileSlots<CARRY>::count;
+    constexpr int o = -TileSlots<CARRY>::first;        // slot index of bin I
     const int i = I + t;
     double birth = 0.0;
     if (i <= v.n - 2)
-        birth = fma(-fin[W + 1 + t + 1], scalbn(v.inv_dx[i], -St), fin[t + 1]);
-    if (i >= 1) birth = fma(fin[W + 1 + t], scalbn(v.inv_dx[i - 1], -St), birth);
+        birth = fma(-fin[NS + t + o], scalbn(v.inv_dx[i], -St), fin[t + o]);
+    if (i >= 1 && (!CARRY || t >= 1))
+        birth = fma(fin[NS + t + o - 1], scalbn(v.inv_dx[i - 1], -St), birth);
     return birth;
+}
+
+// With carry: the w-part of slot I+W-1, owed to bin I+W (0 when that slot is
+// clipped, i.e. bin I+W does not exist or is bin n-1's own clip slot).
+__device__ __forceinline__ double agg_tile_carry(const AggCellView& v, int I, int St,
+                                                 const double* fin)
+{
+    constexpr int NS = TileSlots<true>::count;
+    const int s = I + kTileW - 1;
+    return (s >= 0 && s <= v.n - 2) ? fin[NS + kTileW - 1] * scalbn(v.inv_dx[s], -St) : 0.0;
 }
 
 template <int K>

@@ -65,11 +65,17 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
 {
     __shared__ double sh[kPrepThreads / 32];
     __shared__ int d0_s;
+    __shared__ double ax0_s;
+    __shared__ GeoFit fit_s;
     const int i = blockIdx.x * kPrepThreads + threadIdx.x;
     double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     double dev = 0.0;
     int d0 = n;      // this thread's lag if its pairs land on their larger member (Ld == d)
-    if (threadIdx.x == 0) d0_s = n;
+    if (threadIdx.x == 0) {
+        d0_s = n;
+        ax0_s = cbrt(x[0]);
+        fit_s = geo_fit(x[0], x[n - 1], n);
+    }
     __syncthreads();
     if (i < n) {
         const double xi = x[i], Ni = N[i];
@@ -87,18 +93,19 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         double B = 0.0, S = 0.0;
         if constexpr (K <= 2) B = c * b0;
         if constexpr (K >= 3) {
-            const double rho = ai / cbrt(x0);
+            const double rho = ai / ax0_s;
             if constexpr (K == 3 || K == 5) B = c * bbr * (rho + 1.0 / rho + 2.0);
             if constexpr (K == 4 || K == 5) { const double s = 1.0 + rho; S = c * bsh * (s * s) * s; }
         }
         ws.Bd[i] = B;
         ws.Sd[i] = S;
-        const double v = x0 + xi;
-        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        const double v = x0 + xi;       // x[i] <= v: its bracket is at or above i
+        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         ws.Ld[i] = L;
         if (L == i) d0 = i;
+        if (i < agg_tiles(n)) ws.tticket[i] = 0;
         if (n >= 2) {
-            dev = geo_dev(geo_fit(x0, x[n - 1], n), xi, i);
+            dev = geo_dev(fit_s, xi, i);
             if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
         }
     }
@@ -206,6 +213,7 @@ __device__ double clip_part_sum(const AggCellView& v, int c, int nclip, const Ti
 // Gather mode: the clip tasks and the task that owns bin n-1 each take a
 // ticket after their contribution is stored; the last of the nclip + 1 adds
 // the clip parts, in order, to rhs[n-1]. Called by one thread.
+// (Bin n-1 is never a tile's first bin: tiles are aligned to the top.)
 __device__ __forceinline__ void clip_contributor_done(double* rhs, int n, const AggWs& ws,
                                                       int nclip)
 {
@@ -217,13 +225,27 @@ __device__ __forceinline__ void clip_contributor_done(double* rhs, int n, const 
     rhs[n - 1] = __ldcg(rhs + (n - 1)) + s;
 }
 
+// Gather mode: tile `tile`'s first bin I receives the tile's own value and
+// the carry of the tile below; each stores its part and takes a ticket, the
+// second writes rhs[I] += own + carry (a sum of two: the same whichever is
+// second). Called by one thread.
+__device__ __forceinline__ void first_bin_done(double* rhs, int I, const AggWs& ws, int tile)
+{
+    __threadfence();
+    if (atomicAdd(ws.tticket + tile, 1) != 1) return;
+    __threadfence();
+    rhs[I] = __ldcg(rhs + I) + (__ldcg(ws.tfirst + tile) + __ldcg(ws.tcarry + tile));
+}
+
 // ---------------------------------------------------------------------------
 // main: persistent CTAs split into groups of T threads (agg_group_size); each
-// group pulls tasks from the atomic counter on its own. A task owns the W bins
-// [I, I+W) of one tile and accumulates the slots s = I-1 .. I+W-1 (slot I-1
-// only feeds the w-part of bin I) with the shared tile body (agg_tile.cuh).
-// Thread-private partial sums are reduced in a fixed order, so for a given T
-// the gather result is bitwise reproducible.
+// group pulls tasks from the atomic counter on its own. Tiles are aligned to
+// the top: tile t owns the W bins [I, I+W), I = n - W (t + 1) (the lowest tile
+// may start below bin 0), and accumulates the slots s = I .. I+W-1 with the
+// shared tile body (agg_tile.cuh). The w-part of slot I+W-1 belongs to bin
+// I+W, the first bin of tile t-1: it is handed over as a carry, so each pair
+// is evaluated once. Thread-private partial sums are reduced in a fixed
+// order, so for a given T the gather result is bitwise reproducible.
 // ---------------------------------------------------------------------------
 template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
@@ -231,7 +253,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile, int nchunk,
                 int ntasks, int nclip, double b0, double bbr, double bsh, int T)
 {
-    extern __shared__ double red[];               // [kRedRows][kMainThreads]
+    extern __shared__ double red[];               // [2 W][kMainThreads]
     __shared__ TileShared sm;
     __shared__ int s_task[kMaxGroups];
 
@@ -275,11 +297,11 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         }
         task -= nclip;
 
-        int tile, chunk = 0;
-        if (SCATTER && v.geo) { tile = ntile - 1 - task / nchunk; chunk = task % nchunk; }
-        else { if (task >= ntile) continue; tile = ntile - 1 - task; }
+        int tile, chunk = 0;     // tile 0 is the top one (largest first)
+        if (SCATTER && v.geo) { tile = task / nchunk; chunk = task % nchunk; }
+        else { if (task >= ntile) continue; tile = task; }
 
-        const int I = tile * W;
+        const int I = n - W * (tile + 1);
         const int smax = min(I + W - 1, n - 2);
         const int d_begin = (SCATTER && v.geo) ? chunk * kScatterChunk : 0;
         const int d_end = (SCATTER && v.geo) ? min(n, d_begin + kScatterChunk) : n;
@@ -289,22 +311,34 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         // Per-task exponent shift of the weight numerators: th ~ x_I (r-1) is
         // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
         // the reference's w*rate even on grids spanning hundreds of octaves.
-        const int St = -ilogb(x[I]);
-        agg_tile_accumulate<K>(v, I, d_begin, d_end, St, red + g * T, sm, G);
+        const int St = -ilogb(x[max(I, 0)]);
+        agg_tile_accumulate<K, true>(v, I, d_begin, d_end, St, red + g * T, sm, G);
 
         if (lane < W) {
             const int i = I + lane;
-            if (i < n) {
-                double birth = agg_tile_birth(v, I, lane, St, sm.fin[g]);
+            if (i >= 0) {
+                const double birth = agg_tile_birth<true>(v, I, lane, St, sm.fin[g]);
                 const bool first = !(SCATTER && v.geo) || chunk == 0;
                 const double death = first ? agg_death<K>(v, i) : 0.0;
+                const double val = birth - death;
                 if constexpr (SCATTER) {
-                    const double val = birth - death;
                     if (val != 0.0) atomicAdd(rhs + i, val);
+                } else if (lane == 0 && I >= 1) {
+                    ws.tfirst[tile] = val;
+                    first_bin_done(rhs, I, ws, tile);
                 } else {
-                    rhs[i] = rhs[i] + (birth - death);
+                    rhs[i] = rhs[i] + val;
                     if (i == n - 1) clip_contributor_done(rhs, n, ws, nclip);
                 }
+            }
+        } else if (lane == W && tile >= 1) {
+            // carry into bin I+W, the first bin of the tile above
+            const double c = agg_tile_carry(v, I, St, sm.fin[g]);
+            if constexpr (SCATTER) {
+                if (c != 0.0) atomicAdd(rhs + I + W, c);
+            } else {
+                ws.tcarry[tile - 1] = c;
+                first_bin_done(rhs, I + W, ws, tile - 1);
             }
         }
         G.sync();
@@ -351,7 +385,7 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const int T = agg_group_size(ntasks, num_sms);
     const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
     const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
-    const size_t smem = sizeof(double) * kRedRows * kMainThreads;
+    const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
     cudaError_t e = cudaFuncSetAttribute(agg_main_kernel<K, SC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));

@@ -63,7 +63,7 @@ batch_grid_kernel(BatchDev d)
         d.gBd[gd->off + i] = brownian_like ? c * (rho + 1.0 / rho + 2.0) : c;
         d.gSd[gd->off + i] = c * (s * s) * s;
         const double v = x0 + xi;
-        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         d.gLd[gd->off + i] = L;
         if (L == i) d0 = min(d0, i);
         if (n >= 2) {
@@ -357,7 +357,7 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
 
     const int St = -ilogb(v.x[I]);
     if (agg) {
-        agg_tile_accumulate<K>(v, I, 0, n, St, red, sm, G);   // syncs the group first
+        agg_tile_accumulate<K, false>(v, I, 0, n, St, red, sm, G);   // syncs the group first
 #pragma unroll
         for (int q = 0; q < 5; ++q) v.M[q] = sm.cinfo[G.g][q];
         v.b0 = sm.cinfo[G.g][5]; v.bbr = sm.cinfo[G.g][6]; v.bsh = sm.cinfo[G.g][7];
@@ -367,7 +367,7 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
         if (i < n) {
             double val = 0.0;
             if (agg) {
-                double birth = agg_tile_birth(v, I, G.lane, St, sm.fin[G.g]);
+                double birth = agg_tile_birth<false>(v, I, G.lane, St, sm.fin[G.g]);
                 if (i == n - 1) birth += d.mom[c * 8 + 5];     // clipped pairs (prep)
                 val = birth - agg_death<K>(v, i);
             }

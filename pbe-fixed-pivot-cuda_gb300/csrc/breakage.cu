@@ -75,9 +75,14 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
         if (j == n - 1)
             for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
     }
-    // this block's fragments clipped below x[0], summed in a fixed order
-    const double cs = block_sum(clipped, sh);
-    if (threadIdx.x == 0) ws.clipsum[blockIdx.x] = cs;
+    // this block's fragments clipped below x[0], summed in a fixed order (most
+    // blocks have none: one barrier tells)
+    if (__syncthreads_or(clipped != 0.0)) {
+        const double cs = block_sum(clipped, sh);
+        if (threadIdx.x == 0) ws.clipsum[blockIdx.x] = cs;
+    } else if (threadIdx.x == 0) {
+        ws.clipsum[blockIdx.x] = 0.0;
+    }
 }
 
 // Output bins in groups of 32/nqp per warp, nqp = n_quad rounded up to a power

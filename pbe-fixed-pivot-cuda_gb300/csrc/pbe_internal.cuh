@@ -131,6 +131,26 @@ __device__ __forceinline__ int bracket_lo(const double* __restrict__ x, int n, d
     return lo;
 }
 
+// Same bracket, for a v known to satisfy x[start] <= v < x[n-1]: gallops up
+// from start (1, 2, 4, ... pivots), then bisects the last step. One load when
+// v < x[start+1], as for most lags of x_0 + x_d on a fine geometric grid.
+__device__ __forceinline__ int bracket_from(const double* __restrict__ x, int n, double v,
+                                            int start)
+{
+    const long long vb = dbits(v);
+    int lo = start, step = 1;
+    while (lo + step < n - 1 && dbits(__ldg(x + lo + step)) <= vb) {
+        lo += step;
+        step <<= 1;
+    }
+    int hi = min(lo + step, n - 1);          // x[hi] > v
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (dbits(__ldg(x + mid)) <= vb) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 // Selection function S(v) (reference src/breakage_kernels.cuh:51-65).
 template <int F>
 __device__ __forceinline__ double selection(double v, double S0, double v_ref, double alpha,
@@ -168,11 +188,15 @@ struct AggWs {
     double* mom_part;  // [nb_prep * 8] per-block moment partials
     double* mom;       // [8]  M_{-1/3}, M_0, M_{1/3}, M_{2/3}, M_1, geo flag, max dev
     double* clip_part; // [kMaxClipTasks] sums of clipped pair rates, one per clip task
+    double* tfirst;    // [ntile] gather mode: tile's own value of its first bin
+    double* tcarry;    // [ntile] gather mode: the lower neighbour's carry into that bin
+    int*    tticket;   // [ntile] contributors to the tile's first bin done (0, 1, 2)
     int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d,
                        //      [2] prep blocks done, [3] bin n-1 contributors done
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
+__host__ __device__ constexpr int agg_tiles(int n) { return (n + kTileW - 1) / kTileW; }
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -185,6 +209,8 @@ constexpr size_t agg_ws_bytes(int n)
          + align256(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n)))
          + align256(sizeof(double) * 8)
          + align256(sizeof(double) * kMaxClipTasks)
+         + 2 * align256(sizeof(double) * static_cast<size_t>(agg_tiles(n)))
+         + align256(sizeof(int) * static_cast<size_t>(agg_tiles(n)))
          + align256(sizeof(int) * 8);
 }
 
@@ -205,6 +231,10 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.mom_part  = reinterpret_cast<double*>(take(sizeof(double) * 8 * static_cast<size_t>(agg_prep_blocks(n))));
     w.mom       = reinterpret_cast<double*>(take(sizeof(double) * 8));
     w.clip_part = reinterpret_cast<double*>(take(sizeof(double) * kMaxClipTasks));
+    const size_t nt = static_cast<size_t>(agg_tiles(n));
+    w.tfirst    = reinterpret_cast<double*>(take(sizeof(double) * nt));
+    w.tcarry    = reinterpret_cast<double*>(take(sizeof(double) * nt));
+    w.tticket   = reinterpret_cast<int*>(take(sizeof(int) * nt));
     w.counter   = reinterpret_cast<int*>(take(sizeof(int) * 8));
     if (ws) *ws = w;
     return off;

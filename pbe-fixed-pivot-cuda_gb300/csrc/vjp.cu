@@ -54,10 +54,17 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const double* __restrict__ lam, int n, VjpWs ws)
 {
     __shared__ double sh[kPrepThreads / 32];
+    __shared__ double ax0_s;
+    __shared__ GeoFit fit_s;
     const int i = blockIdx.x * kPrepThreads + threadIdx.x;
     double m[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) m[q] = 0.0;
+    if (threadIdx.x == 0) {
+        ax0_s = cbrt(x[0]);
+        fit_s = geo_fit(x[0], x[n - 1], n);
+    }
+    __syncthreads();
     double dev = 0.0;
     if (i < n) {
         const double xi = x[i], Ni = N[i], li = lam[i];
@@ -73,14 +80,14 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
             m[5 + q] = w[q] * (li * Ni);
         }
         const double x0 = x[0];
-        const double rho = ai / cbrt(x0);
+        const double rho = ai / ax0_s;
         ws.Bf[i] = rho + 1.0 / rho + 2.0;
         const double s = 1.0 + rho;
         ws.Sf[i] = (s * s) * s;
         const double v = x0 + xi;
-        ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_lo(x, n, v);
+        ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         if (n >= 2) {
-            dev = geo_dev(geo_fit(x0, x[n - 1], n), xi, i);
+            dev = geo_dev(fit_s, xi, i);
             if (!(dev == dev)) dev = 1.0;
         }
     }
