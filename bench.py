@@ -56,16 +56,14 @@ FLOPS_PER_FRAGMENT = 8   # per breakage fragment
 # lags with lo > k: rate (DMUL, DFMA, DMUL) + R += rate (DADD) + TH (DFMA) = 5;
 # lags with lo = k: q (DMUL, DFMA) + R (DADD) + TH (DFMA) = 4. The weight
 # numerator runs on the integer pipe. fp64_instr_per_launch() counts the
-# evaluations of both kinds the kernel performs on a given grid, plus 4 per
-# clipped pair (the clip tasks). The single-instance kernel evaluates each
-# pair once (tiles hand the w-part of their top slot to the tile above); the
-# batched kernel's 12-bin tiles also evaluate their left neighbour slot
-# (carry=False). profiles/ cross-checks the count with the SASS instruction
-# counters.
-FP64_PHASE1, FP64_PHASE2, TILE_W = 5, 4, 12
+# evaluations of both kinds the kernel performs on a given grid (each pair
+# once: tiles hand the w-part of their top slot to the tile above), plus 4 per
+# clipped pair (the clip tasks); profiles/ cross-checks the count with the
+# SASS instruction counters.
+FP64_PHASE1, FP64_PHASE2 = 5, 4
 
 
-def fp64_instr_per_launch(x, carry=True) -> int:
+def fp64_instr_per_launch(x) -> int:
     n = len(x)
     v = x[0] + x
     L = np.searchsorted(x, v, side="right") - 1          # bracket of x_0 + x_d
@@ -76,21 +74,10 @@ def fp64_instr_per_launch(x, carry=True) -> int:
     clipped = int(np.maximum(0, (n - 1 - d_all) - jlo + 1).sum())
     e0 = np.flatnonzero(L == np.arange(n))
     D0 = int(e0[0]) if len(e0) else n
-    d_idx = np.arange(n)
-    if carry:
-        # pair (j, j + d) lands on slot j + L[d] <= n - 2
-        cnt = np.where(L <= n - 2, np.maximum(0, n - 1 - L), 0)
-        return (FP64_PHASE1 * int(cnt[d_idx < D0].sum()) + FP64_PHASE2 * int(cnt[d_idx >= D0].sum())
-                + 4 * clipped)
-    total = 0
-    for I in range(0, n, TILE_W):
-        smax = min(I + TILE_W - 1, n - 2)
-        thi = smax - I + 1
-        ok = L <= smax
-        tlo = np.maximum(0, L - I + 1)
-        cnt = np.where(ok, np.maximum(0, thi - tlo + 1), 0)
-        total += FP64_PHASE1 * int(cnt[d_idx < D0].sum()) + FP64_PHASE2 * int(cnt[d_idx >= D0].sum())
-    return total + 4 * clipped
+    # pair (j, j + d) lands on slot j + L[d] <= n - 2
+    cnt = np.where(L <= n - 2, np.maximum(0, n - 1 - L), 0)
+    return (FP64_PHASE1 * int(cnt[d_all < D0].sum()) + FP64_PHASE2 * int(cnt[d_all >= D0].sum())
+            + 4 * clipped)
 # dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
 # this workload, from the ncu capture in profiles/agg_main_kernel_n16384.md.
 MAIN_KERNEL_DRAM_BYTES = 1343488
@@ -207,7 +194,7 @@ def fp64_instr_tiles(x, n_cell=None) -> int:
     """FP64 instructions of the tile kernel for a cell with the first n_cell
     pivots of x (same counting as fp64_instr_per_launch)."""
     x = x[:n_cell] if n_cell else x
-    return fp64_instr_per_launch(x, carry=False)
+    return fp64_instr_per_launch(x)
 
 
 def batched_section(dev, stream):

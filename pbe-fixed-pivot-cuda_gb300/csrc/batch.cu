@@ -160,8 +160,12 @@ void build_schedule(const pbe_batch_plan& p, const int* gs, const bool* want,
         const int n = p.cell_n[c];
         const int cls = n_class(n);
         if (want && !want[cls]) continue;
-        for (int I = 0; I < n; I += W)
-            per[cls].push_back({c, I, task_cost(n, vjp ? n : I, gs[cls])});
+        if (vjp) {
+            for (int I = 0; I < n; I += W) per[cls].push_back({c, I, task_cost(n, n, gs[cls])});
+        } else {
+            // forward tiles aligned to the top: the lowest may start below bin 0
+            for (int I = n - W; I > -W; I -= W) per[cls].push_back({c, I, task_cost(n, I, gs[cls])});
+        }
     }
     struct B { long long cost; int cls; int first; int cnt; };
     std::vector<B> bl;
@@ -369,10 +373,13 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     std::vector<BatchCellDev> hc(static_cast<size_t>(n_cells));
     p->offsets.resize(static_cast<size_t>(n_cells) + 1);
     long long off = 0;
+    long long tiles = 0;
     for (int c = 0; c < n_cells; ++c) {
-        hc[c] = BatchCellDev{static_cast<int>(off), cell_n[c], cell_grid[c], 0};
+        hc[c] = BatchCellDev{static_cast<int>(off), cell_n[c], cell_grid[c],
+                             static_cast<int>(tiles)};
         p->offsets[c] = off;
         off += cell_n[c];
+        tiles += (cell_n[c] + W - 1) / W;
         p->max_n = std::max(p->max_n, cell_n[c]);
     }
     p->offsets[n_cells] = off;
@@ -406,6 +413,9 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     if (e == cudaSuccess) e = plan_alloc(p, &d.kacc, C);
     if (e == cudaSuccess) e = plan_alloc(p, &d.mom, static_cast<size_t>(n_cells) * 8);
     if (e == cudaSuccess) e = plan_alloc(p, &d.counter, 8);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.tfirst, static_cast<size_t>(tiles));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.tcarry, static_cast<size_t>(tiles));
+    if (e == cudaSuccess) e = plan_alloc(p, &d.tticket, static_cast<size_t>(tiles));
     if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_tq, static_cast<size_t>(p->nq));
     if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_bw, static_cast<size_t>(p->nq));
     if (e != cudaSuccess) return e;
@@ -414,6 +424,7 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     // finite for the loads that the tile body issues unconditionally
     for (double* a : {d.Y, d.Nj, d.Hj, d.Hk, d.SN, d.Bk, d.k, d.kacc})
         if (e == cudaSuccess) e = cudaMemsetAsync(a, 0, C * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.tticket, 0, static_cast<size_t>(tiles) * sizeof(int), s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d.grids, hg.data(), hg.size() * sizeof(BatchGridDev),
                             cudaMemcpyHostToDevice, s);

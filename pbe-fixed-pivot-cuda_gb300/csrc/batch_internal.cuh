@@ -27,10 +27,10 @@ struct BatchGridDev {
 };
 
 struct BatchCellDev {
-    int off;     // first bin in the packed cell arrays
-    int n;       // sections of the cell (<= its grid's n)
+    int off;       // first bin in the packed cell arrays
+    int n;         // sections of the cell (<= its grid's n)
     int grid;
-    int pad;
+    int tile_off;  // first hand-over slot of the cell's tiles (tile t at tile_off + t)
 };
 
 // Device pointers of a plan: grid tables (static) and per-stage cell arrays.
@@ -59,6 +59,10 @@ struct BatchDev {
     double* kacc;   // k1 + 2 k2 + 2 k3 (+ k4)
     double* mom;    // [n_cells * 8] moments of the stage state (death term), [5] clip sum
     int* counter;   // [8] task counter of the persistent kernel
+    // hand-over of a tile's first bin (tiles aligned to the cell's top; tile t
+    // owns bins [n - W (t+1), n - W t)): its own value, the carry of the tile
+    // below, and a ticket that both bump once per launch (odd = second)
+    double* tfirst; double* tcarry; int* tticket;   // [sum of the cells' tiles]
     // schedule
     const int4* bundles;   // {first task, tasks, group size, 0}
     const int2* tasks;     // {cell, first bin}

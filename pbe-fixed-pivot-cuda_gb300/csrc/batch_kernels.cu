@@ -322,6 +322,21 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
     if (d.nq > 0) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
 }
 
+// Hand-over of bin `bin` of a cell (the first bin of tile slot `slot`): its
+// owner tile and the tile below each store their part and bump the ticket;
+// the second (odd count: each launch adds two) writes own + carry. The sum of
+// two is the same whichever is second. Called by one thread.
+__device__ __forceinline__ void batch_first_done(const BatchDev& d, double* out, bool accumulate,
+                                                 int bin, int slot)
+{
+    __threadfence();
+    if ((atomicAdd(d.tticket + slot, 1) & 1) == 0) return;
+    __threadfence();
+    const double v = __ldcg(d.tfirst + slot) + __ldcg(d.tcarry + slot);
+    double* o = out + bin;
+    *o = accumulate ? __ldcg(o) + v : v;
+}
+
 template <int K>
 __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                            const pbe_batch_cell_params_t* __restrict__ params, double* out,
@@ -355,26 +370,38 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                                    : (l == 5 ? P.beta0 : (l == 6 ? P.beta_br : P.beta_sh));
     }
 
-    const int St = -ilogb(v.x[I]);
+    // tiles are aligned to the cell's top: I = n - W (tile + 1), I > -W
+    const int tile = (n - I) / W - 1;
+    const int St = -ilogb(v.x[max(I, 0)]);
     if (agg) {
-        agg_tile_accumulate<K, false>(v, I, 0, n, St, red, sm, G);   // syncs the group first
+        agg_tile_accumulate<K, true>(v, I, 0, n, St, red, sm, G);    // syncs the group first
 #pragma unroll
         for (int q = 0; q < 5; ++q) v.M[q] = sm.cinfo[G.g][q];
         v.b0 = sm.cinfo[G.g][5]; v.bbr = sm.cinfo[G.g][6]; v.bsh = sm.cinfo[G.g][7];
     }
     if (G.lane < W) {
         const int i = I + G.lane;
-        if (i < n) {
+        if (i >= 0) {
             double val = 0.0;
             if (agg) {
-                double birth = agg_tile_birth<false>(v, I, G.lane, St, sm.fin[G.g]);
+                double birth = agg_tile_birth<true>(v, I, G.lane, St, sm.fin[G.g]);
                 if (i == n - 1) birth += d.mom[c * 8 + 5];     // clipped pairs (prep)
                 val = birth - agg_death<K>(v, i);
             }
             if (d.nq > 0) val += d.Bk[cd.off + i];             // breakage (prep)
-            double* o = out + cd.off + i;
-            *o = accumulate ? *o + val : val;
+            if (agg && G.lane == 0 && I >= 1) {
+                // the w-part of slot I-1 comes from the tile below
+                d.tfirst[cd.tile_off + tile] = val;
+                batch_first_done(d, out, accumulate, cd.off + I, cd.tile_off + tile);
+            } else {
+                double* o = out + cd.off + i;
+                *o = accumulate ? *o + val : val;
+            }
         }
+    } else if (agg && G.lane == W && tile >= 1) {
+        // carry into bin I+W, the first bin of the tile above
+        d.tcarry[cd.tile_off + tile - 1] = agg_tile_carry(v, I, St, sm.fin[G.g]);
+        batch_first_done(d, out, accumulate, cd.off + I + W, cd.tile_off + tile - 1);
     }
 }
 
@@ -384,7 +411,7 @@ batch_main_kernel(BatchDev d, const double* __restrict__ Y,
                   const pbe_batch_cell_params_t* __restrict__ params, double* out, int accumulate,
                   const int4* __restrict__ bundles, const int2* __restrict__ tasks, int n_bundles)
 {
-    extern __shared__ double red[];     // [kRedRows][kMainThreads]
+    extern __shared__ double red[];     // [2 W][kMainThreads]
     __shared__ TileShared sm;
     __shared__ int s_b;
     const int tid = threadIdx.x;
@@ -410,7 +437,7 @@ cudaError_t main_k(const BatchDev& d, const double* Y, const pbe_batch_cell_para
                    double* out, bool accumulate, const int4* bundles, const int2* tasks,
                    int n_bundles, cudaStream_t s)
 {
-    const size_t smem = sizeof(double) * kRedRows * kMainThreads;
+    const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
     cudaError_t e = cudaMemsetAsync(d.counter, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     if (n_bundles <= 0) return cudaSuccess;
@@ -424,7 +451,7 @@ template <int K>
 cudaError_t attr_k()
 {
     return cudaFuncSetAttribute(batch_main_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(sizeof(double) * kRedRows * kMainThreads));
+                                static_cast<int>(sizeof(double) * TileSlots<true>::rows * kMainThreads));
 }
 
 } // namespace
