@@ -33,6 +33,29 @@ def test_aggregation_matches_oracle(kernel, b0, bbr, bsh, grid, mode):
             assert_close(got, ref, scale, "k=%d grid=%s n=%d ic=%s" % (kernel, grid, n, ic))
 
 
+@pytest.mark.parametrize("mode", MODES, ids=["gather", "scatter"])
+@pytest.mark.parametrize("case", ["subnormal", "tiny", "wide"])
+@pytest.mark.parametrize("kernel,b0,bbr,bsh", AGG_KERNELS, ids=[str(k[0]) for k in AGG_KERNELS])
+def test_aggregation_product_scope_edges(kernel, b0, bbr, bsh, case, mode):
+    """Number densities at the edges of the double range: a subnormal N, N so
+    small that beta N underflows, and N spread over ~180 decades."""
+    rng = np.random.default_rng(31 + kernel)
+    for n in (40, 300):
+        x = make_grid("geo_fine", n, rng)
+        N = make_N("random", x, rng)
+        if case == "subnormal":
+            N[rng.integers(0, n, 3)] = 3e-310
+        elif case == "tiny":
+            N[rng.integers(0, n, 5)] = 1e-290          # beta * N underflows for small beta
+        else:
+            N *= np.exp(rng.uniform(-300.0, 120.0, size=n))
+        p = agg_params(n, kernel, b0, bbr, bsh, x, geometric=True)
+        code, got = gpu_agg(N, x, p, mode)
+        assert code == 0, pg.error_string(code)
+        ref, scale, _ = oracle_agg(N, x, p)
+        assert_close(got, ref, scale, "k=%d case=%s n=%d" % (kernel, case, n))
+
+
 DAUGHTERS = {
     "symmetric": pg.quadrature.symmetric_binary(),
     "symmetric16": pg.quadrature.symmetric_binary_split(16),
