@@ -290,6 +290,34 @@ int pbe_batch_tape_forward(pbe_batch_t plan, double* N, const pbe_batch_cell_par
 int pbe_batch_tape_backward(pbe_batch_t plan, const double* lambda_T, double* gN0,
                             double* gparams, void* stream);
 
+/* Jacobian-vector product of the batched RHS: out = J(N) v for every cell
+ * (packed like N; overwritten), J = d rhs / dN of aggregation plus breakage.
+ * Aggregation is quadratic in N, so J(N) v = T(N, v) + T(v, N) with T(a, b)
+ * the pair sum of src/aggregation_kernels.cuh:145-239 with the rate
+ * beta a_j b_k (1/2 on the diagonal): two passes of the pair kernel, exact
+ * (no difference quotient). Breakage (src/breakage_kernels.cuh:115-251) is
+ * linear in N where its guard S != 0 && N > 2.2e-308 passes: its product is
+ * the breakage RHS of v restricted to the bins whose N passes the guard. No
+ * counterpart in the reference. */
+int pbe_batch_jvp(pbe_batch_t plan, const double* N, const double* v,
+                  const pbe_batch_cell_params_t* params, double* out, void* stream);
+
+/* Linearly implicit integration of every cell: n_steps steps of size dt of
+ * the two-stage Rosenbrock method ROS2 (second order, L-stable,
+ * gamma = 1 + 1/sqrt(2)):
+ *   (I - gamma dt J) k1 = rhs(N),  (I - gamma dt J) k2 = rhs(N + dt k1) - 2 k1,
+ *   N += 3/2 dt k1 + 1/2 dt k2,  J = J(N) for both stages.
+ * Each linear system is solved matrix-free by GMRES with krylov_dim
+ * (1..64) Arnoldi steps and no restart, right-preconditioned by
+ * 1 + gamma dt (death and breakage loss rate of bin i); every Arnoldi step
+ * takes one pbe_batch_jvp. resid (device, n_cells, may be NULL) receives per
+ * cell the largest relative least-squares residual of the call's solves
+ * (0: solved exactly within round-off). Plan-owned memory grows on first use
+ * by (krylov_dim + 8) packed vectors. The reference leaves time integration
+ * to the caller (examples/common/pbe_examples_utils.hpp:391-456). */
+int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,
+                   int n_steps, int krylov_dim, double* resid, void* stream);
+
 /* Schedule in use: group_size[c] (16 entries) = threads per tile task for
  * cells with floor(log2(n)) == c (0 where no cell falls), *n_bundles = the
  * number of bundles in the persistent launch. Either pointer may be NULL. */

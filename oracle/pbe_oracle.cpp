@@ -170,6 +170,75 @@ void aggregation_row(const double* N, const double* x, double* rhs,
     }
 }
 
+// Row j of J(N) v for the aggregation RHS: the pairs of aggregation_row with
+// the rate's derivative along v, beta (N_j v_k + v_j N_k) (times 1/2 on the
+// diagonal), deposited like the rate (exact bracket).
+void aggregation_row_jvp(const double* N, const double* v, const double* x, double* out,
+                         double* scale, int n, int j, int kernel, double b0, double b_br,
+                         double b_sh)
+{
+    const double xj = x[j];
+    for (int k = j; k < n; ++k) {
+        const double xk = x[k];
+        double rate = beta_ref(kernel, xj, xk, b0, b_br, b_sh) * (N[j] * v[k] + v[j] * N[k]);
+        const bool diagonal = (j == k);
+        if (diagonal) rate *= 0.5;
+        if (diagonal) {
+            dep(out, scale, j, -2.0 * rate);
+        } else {
+            dep(out, scale, j, -rate);
+            dep(out, scale, k, -rate);
+        }
+        const double vs = xj + xk;
+        if (vs >= x[n - 1]) {
+            dep(out, scale, n - 1, rate);
+        } else if (vs <= x[0]) {
+            dep(out, scale, 0, rate);
+        } else {
+            const int hi = bin_index_ref(x, n, vs, 0.0, 0.0);
+            const int lo = hi - 1;
+            const double w = (vs - x[lo]) / (x[hi] - x[lo]);
+            dep(out, scale, lo, (1.0 - w) * rate);
+            dep(out, scale, hi, w * rate);
+        }
+    }
+}
+
+// Breakage RHS (src/breakage_kernels.cuh:115-133, :160-251) of the values V
+// with the guard S != 0 && G > 2.2e-308 taken on G: V = G = N is the RHS;
+// G = N, V = v its Jacobian-vector product (the RHS is linear in N wherever
+// the guard passes, and the guard is a property of the state).
+void breakage_core(const double* G, const double* V, const double* x, const double* t_q,
+                   const double* bw_q, double* rhs, double* scale, int n, int n_quad,
+                   int selection, double S0, double v_ref, double alpha, double v_min)
+{
+    // death kernel runs first on the stream (src/breakage.cu:30-50)
+    for (int j = 0; j < n; ++j) {
+        double Sj = selection_ref(selection, x[j], S0, v_ref, alpha, v_min);
+        if (Sj != 0.0 && G[j] > 2.2e-308) dep(rhs, scale, j, -(Sj * V[j]));
+    }
+    for (int j = 0; j < n; ++j) {
+        const double xj = x[j], Vj = V[j];
+        const double Sj = selection_ref(selection, xj, S0, v_ref, alpha, v_min);
+        if (!(Sj != 0.0 && G[j] > 2.2e-308)) continue;
+        for (int q = 0; q < n_quad; ++q) {
+            const double contrib = Sj * Vj * bw_q[q];
+            const double vf = xj * t_q[q];
+            if (vf <= x[0]) {
+                dep(rhs, scale, 0, contrib);
+            } else if (vf >= x[n - 1]) {
+                dep(rhs, scale, n - 1, contrib);
+            } else {
+                int lo = bin_search_ref(x, n, vf);
+                int hi = lo + 1;
+                double eta = (vf - x[lo]) / (x[hi] - x[lo]);
+                dep(rhs, scale, lo, (1.0 - eta) * contrib);
+                dep(rhs, scale, hi, eta * contrib);
+            }
+        }
+    }
+}
+
 } // namespace
 
 extern "C" {
@@ -236,31 +305,32 @@ int oracle_breakage_rhs(const double* N, const double* x, const double* t_q,
     if (n <= 0 || n_quad <= 0) return 1;
     if (!N || !x || !t_q || !bw_q || !rhs) return 1;
     if (selection < 0 || selection > 3) return 1;
-    // death kernel runs first on the stream (src/breakage.cu:30-50)
-    for (int j = 0; j < n; ++j) {
-        double Sj = selection_ref(selection, x[j], S0, v_ref, alpha, v_min);
-        if (Sj != 0.0 && N[j] > 2.2e-308) dep(rhs, scale, j, -(Sj * N[j]));
-    }
-    for (int j = 0; j < n; ++j) {
-        const double xj = x[j], Nj = N[j];
-        const double Sj = selection_ref(selection, xj, S0, v_ref, alpha, v_min);
-        if (!(Sj != 0.0 && Nj > 2.2e-308)) continue;
-        for (int q = 0; q < n_quad; ++q) {
-            const double contrib = Sj * Nj * bw_q[q];
-            const double v = xj * t_q[q];
-            if (v <= x[0]) {
-                dep(rhs, scale, 0, contrib);
-            } else if (v >= x[n - 1]) {
-                dep(rhs, scale, n - 1, contrib);
-            } else {
-                int lo = bin_search_ref(x, n, v);
-                int hi = lo + 1;
-                double eta = (v - x[lo]) / (x[hi] - x[lo]);
-                dep(rhs, scale, lo, (1.0 - eta) * contrib);
-                dep(rhs, scale, hi, eta * contrib);
-            }
-        }
-    }
+    breakage_core(N, N, x, t_q, bw_q, rhs, scale, n, n_quad, selection, S0, v_ref, alpha, v_min);
+    return 0;
+}
+
+// J(N) v of the aggregation RHS (+= into out): aggregation_row_jvp over all
+// rows. Returns 1 on the argument errors of oracle_aggregation_rhs.
+int oracle_aggregation_rhs_jvp(const double* N, const double* v, const double* x, double* out,
+                               double* scale, int n, int kernel, double beta0, double beta_br,
+                               double beta_sh)
+{
+    if (n <= 0 || !N || !v || !x || !out || kernel < 0 || kernel > 5) return 1;
+    for (int j = 0; j < n; ++j)
+        aggregation_row_jvp(N, v, x, out, scale, n, j, kernel, beta0, beta_br, beta_sh);
+    return 0;
+}
+
+// J(N) v of the breakage RHS (+= into out): breakage_core with the guard on N
+// and the values v.
+int oracle_breakage_rhs_jvp(const double* N, const double* v, const double* x, const double* t_q,
+                            const double* bw_q, double* out, double* scale, int n, int n_quad,
+                            int selection, double S0, double v_ref, double alpha, double v_min)
+{
+    if (n <= 0 || n_quad <= 0) return 1;
+    if (!N || !v || !x || !t_q || !bw_q || !out) return 1;
+    if (selection < 0 || selection > 3) return 1;
+    breakage_core(N, v, x, t_q, bw_q, out, scale, n, n_quad, selection, S0, v_ref, alpha, v_min);
     return 0;
 }
 

@@ -51,6 +51,13 @@ def _lib():
         lib.oracle_breakage_rhs_vjp.argtypes = [_D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        lib.oracle_aggregation_rhs_jvp.restype = ctypes.c_int
+        lib.oracle_aggregation_rhs_jvp.argtypes = [_D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        lib.oracle_breakage_rhs_jvp.restype = ctypes.c_int
+        lib.oracle_breakage_rhs_jvp.argtypes = [_D, _D, _D, _D, _D, _D, _D, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double, ctypes.c_double]
         lib.oracle_rk4_adjoint.restype = ctypes.c_int
         lib.oracle_rk4_adjoint.argtypes = [_D, _D, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int), ctypes.c_int, _D, _D, _D,
@@ -156,6 +163,70 @@ def breakage_rhs_vjp(N, x, t_q, bw_q, lam, selection, S0=1.0, v_ref=1.0, alpha=1
     if with_scale:
         return gN, gp, sN, sp, code
     return gN, gp, code
+
+
+def aggregation_rhs_jvp(N, v, x, kernel, beta0=1.0, beta_br=0.0, beta_sh=0.0):
+    """(J(N) v, per-bin scale sum |contribution|, code) of the aggregation RHS."""
+    N, v, x = _f64(N), _f64(v), _f64(x)
+    out, scale = np.zeros(len(x)), np.zeros(len(x))
+    code = _lib().oracle_aggregation_rhs_jvp(_dp(N), _dp(v), _dp(x), _dp(out), _dp(scale), len(x),
+                                             int(kernel), float(beta0), float(beta_br),
+                                             float(beta_sh))
+    return out, scale, code
+
+
+def breakage_rhs_jvp(N, v, x, t_q, bw_q, selection, S0=1.0, v_ref=1.0, alpha=1.0, v_min=0.0):
+    """(J(N) v, per-bin scale, code) of the breakage RHS (guard on N)."""
+    N, v, x = _f64(N), _f64(v), _f64(x)
+    t_q, bw_q = _f64(t_q), _f64(bw_q)
+    out, scale = np.zeros(len(x)), np.zeros(len(x))
+    code = _lib().oracle_breakage_rhs_jvp(_dp(N), _dp(v), _dp(x), _dp(t_q), _dp(bw_q), _dp(out),
+                                          _dp(scale), len(x), len(t_q), int(selection), float(S0),
+                                          float(v_ref), float(alpha), float(v_min))
+    return out, scale, code
+
+
+def _rhs(N, x, agg, brk):
+    out = np.zeros(len(x))
+    if agg:
+        out = aggregation_rhs(N, x, agg["kernel"], agg.get("beta0", 1.0), agg.get("beta_br", 0.0),
+                              agg.get("beta_sh", 0.0), rhs=out, exact_bracket=True)[0]
+    if brk:
+        out = breakage_rhs(N, x, brk["t_q"], brk["bw_q"], brk["selection"], brk.get("S0", 1.0),
+                           brk.get("v_ref", 1.0), brk.get("alpha", 1.0), brk.get("v_min", 0.0),
+                           rhs=out)[0]
+    return out
+
+
+def jacobian(N, x, agg=None, brk=None):
+    """Dense J(N) = d rhs / dN (column k = J e_k from the Jacobian-vector products)."""
+    n = len(x)
+    J = np.zeros((n, n))
+    for k in range(n):
+        e = np.zeros(n)
+        e[k] = 1.0
+        col = np.zeros(n)
+        if agg:
+            col += aggregation_rhs_jvp(N, e, x, agg["kernel"], agg.get("beta0", 1.0),
+                                       agg.get("beta_br", 0.0), agg.get("beta_sh", 0.0))[0]
+        if brk:
+            col += breakage_rhs_jvp(N, e, x, brk["t_q"], brk["bw_q"], brk["selection"],
+                                    brk.get("S0", 1.0), brk.get("v_ref", 1.0),
+                                    brk.get("alpha", 1.0), brk.get("v_min", 0.0))[0]
+        J[:, k] = col
+    return J
+
+
+def ros2_step(N, x, dt, agg=None, brk=None):
+    """One ROS2 step (gamma = 1 + 1/sqrt 2) with the dense Jacobian at N and
+    direct solves: (I - gamma dt J) k1 = R(N); (I - gamma dt J) k2 = R(N + dt k1)
+    - 2 k1; N + 3/2 dt k1 + 1/2 dt k2. agg / brk as for rk4_step."""
+    N, x = _f64(N), _f64(x)
+    g = 1.0 + 1.0 / np.sqrt(2.0)
+    A = np.eye(len(x)) - g * dt * jacobian(N, x, agg, brk)
+    k1 = np.linalg.solve(A, _rhs(N, x, agg, brk))
+    k2 = np.linalg.solve(A, _rhs(N + dt * k1, x, agg, brk) - 2.0 * k1)
+    return N + (1.5 * dt * k1 + 0.5 * dt * k2)
 
 
 def rk4_step(N, x, dt, agg=None, brk=None):

@@ -102,6 +102,9 @@ struct AggCellView {
     const double* Hk;      // x N [n] (K = 1, 2 and the generic path of those)
     const double* Nj;      // j-side N factor [n]
     const double* Hj;      // j-side x N factor [n]
+    const double* Aj;      // j-side N, no coefficient [n] (generic path, clipped pairs): N,
+                           // or the first vector of a Jacobian-vector pass
+    const double* AHj;     // x Aj [n] (K = 1, 2 on the generic path)
     const double* Fs;      // per-slot factor of lo = k lags [n]: N (x N for K = 2)
     const double* a;       // x^(1/3) [n]
     const double* ia;      // x^(-1/3) [n]
@@ -294,7 +297,7 @@ __device__ __forceinline__ void agg_tile_accumulate(const AggCellView& v, int I,
                 }
                 const int kb = lo;
                 if (ka >= kb) continue;
-                const double Nj = v.Nk[j], hj = v.Hk[j], aj = v.a[j], iaj = v.ia[j];
+                const double Nj = v.Aj[j], hj = v.AHj[j], aj = v.a[j], iaj = v.ia[j];
                 int t = t_first;
                 double Rc = 0.0, THc = 0.0;
                 for (int k = ka; k < kb; ++k) {

@@ -201,7 +201,7 @@ __device__ double clip_part_sum(const AggCellView& v, int c, int nclip, const Ti
                 const int mid = (lo + hi) >> 1;
                 if (dbits(xj + v.x[mid]) >= tb) hi = mid; else lo = mid + 1;
             }
-            const double Nj = v.Nk[j], hj = v.Hk[j], aj = v.a[j], iaj = v.ia[j];
+            const double Nj = v.Aj[j], hj = v.AHj[j], aj = v.a[j], iaj = v.ia[j];
             for (int k = lo; k < n; ++k)
                 acc += rate_gen<K>(j == k, v.b0, v.bbr, v.bsh, Nj, hj, aj, iaj, v.Nk[k], v.Hk[k],
                                    v.a[k], v.ia[k]);
@@ -259,7 +259,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 
     const int tid = threadIdx.x;
     AggCellView v;
-    v.x = x; v.Nk = N; v.Hk = ws.h; v.Nj = N; v.Hj = ws.h;
+    v.x = x; v.Nk = N; v.Hk = ws.h; v.Nj = N; v.Hj = ws.h; v.Aj = N; v.AHj = ws.h;
     v.Fs = (K == 2) ? ws.h : N;
     v.a = ws.a; v.ia = ws.ia; v.inv_dx = ws.inv_dx;
     v.Bd = ws.Bd; v.Sd = ws.Sd; v.Ld = ws.Ld;

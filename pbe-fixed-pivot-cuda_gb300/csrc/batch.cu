@@ -69,6 +69,10 @@ struct pbe_batch_plan {
     double* rk_k = nullptr;            // 7 packed stage derivatives
     double* rk_cell = nullptr;         // t, dt per cell
     int* rk_int = nullptr;             // status, steps, rejects per cell; done counter
+    // linearly implicit (Rosenbrock) integrator: GMRES state and stage vectors
+    pbe_gb300::GmresDev gm{};
+    int gm_cap = 0;                    // Krylov dimension the GMRES buffers hold
+    double* ros = nullptr;             // F, K1, K2, Y (4 packed vectors)
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -742,6 +746,108 @@ const double kDP[6][6] = {
 const double kDPErr[7] = {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0,
                           -17253.0 / 339200.0, 22.0 / 525.0, -1.0 / 40.0};
 
+// ---- Jacobian-vector products and the Rosenbrock integrator -------------------
+// J(N) v = T(N, v) + T(v, N) for the aggregation part (two passes of the pair
+// kernel with the j side from the first vector, batch_kernels.cu) plus the
+// breakage Jacobian at N applied to v (first pass).
+cudaError_t jvp(pbe_batch_plan* p, const double* N, const double* v,
+                const pbe_batch_cell_params_t* prm, double* out, cudaStream_t s)
+{
+    if (!p->d.Ha) {
+        cudaError_t e = plan_alloc(p, &p->d.Ha, static_cast<size_t>(p->total));
+        if (e != cudaSuccess) { p->d.Ha = nullptr; return e; }
+    }
+    const BatchDev& d = p->d;
+    BatchDev d1 = d;
+    d1.A = N;
+    cudaError_t e = batch_jvp_prep(d, N, v, N, prm, true, s);
+    if (e == cudaSuccess) e = batch_main(d1, v, prm, out, false, s);
+    BatchDev d2 = d;
+    d2.A = v;
+    if (e == cudaSuccess) e = batch_jvp_prep(d, v, N, N, prm, false, s);
+    if (e == cudaSuccess) e = batch_main(d2, N, prm, out, true, s);
+    return e;
+}
+
+cudaError_t gmres_alloc(pbe_batch_plan* p, int m)
+{
+    if (p->gm_cap >= m) return cudaSuccess;
+    const size_t C = static_cast<size_t>(p->total), nc = static_cast<size_t>(p->n_cells);
+    const size_t M = static_cast<size_t>(m);
+    GmresDev g{};
+    cudaError_t e = plan_alloc(p, &g.V, (M + 1) * C);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.Z, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.W, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.P, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.H, nc * (M + 1) * M);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.gv, nc * (M + 1));
+    if (e == cudaSuccess) e = plan_alloc(p, &g.cs, nc * M);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.sn, nc * M);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.beta0, nc);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.kval, nc);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.done, nc);
+    if (e != cudaSuccess) return e;
+    p->gm = g;
+    p->gm_cap = m;
+    return cudaSuccess;
+}
+
+// x = (I - gt J(N))^-1 r for every cell: GMRES(m) without restart, right
+// preconditioned (batch_implicit.cu); resid[c] = max(resid[c], relative
+// least-squares residual).
+cudaError_t gmres_solve(pbe_batch_plan* p, const double* N, const double* r, double* x,
+                        const pbe_batch_cell_params_t* prm, double* resid, cudaStream_t s)
+{
+    const BatchDev& d = p->d;
+    const GmresDev& g = p->gm;
+    cudaError_t e = batch_gmres_start(d, g, N, r, prm, s);
+    for (int j = 0; j < g.m && e == cudaSuccess; ++j) {
+        e = jvp(p, N, g.Z, prm, g.W, s);
+        if (e == cudaSuccess) e = batch_gmres_arnoldi(d, g, j, s);
+    }
+    if (e == cudaSuccess) e = batch_gmres_finish(d, g, x, resid, s);
+    return e;
+}
+
+// ROS2 (two-stage, second order, L-stable; gamma = 1 + 1/sqrt 2):
+//   (I - gamma dt J) k1 = R(N)
+//   (I - gamma dt J) k2 = R(N + dt k1) - 2 k1
+//   N += 3/2 dt k1 + 1/2 dt k2
+// with J = J(N) for both stages, every cell of the plan at once.
+cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
+                 int n_steps, int m, double* resid, cudaStream_t s)
+{
+    const size_t C = static_cast<size_t>(p->total);
+    cudaError_t e = gmres_alloc(p, m);
+    if (e == cudaSuccess && !p->ros) {
+        e = plan_alloc(p, &p->ros, 4 * C);
+        if (e != cudaSuccess) p->ros = nullptr;
+    }
+    if (e != cudaSuccess) return e;
+    p->gm.m = m;
+    p->gm.total = static_cast<long long>(C);
+    p->gm.gt = (1.0 + 1.0 / std::sqrt(2.0)) * dt;
+    double* F = p->ros;
+    double* K1 = p->ros + C;
+    double* K2 = p->ros + 2 * C;
+    double* Y = p->ros + 3 * C;
+    const BatchDev& d = p->d;
+    const long long T = static_cast<long long>(C);
+    if (resid) e = cudaMemsetAsync(resid, 0, static_cast<size_t>(p->n_cells) * sizeof(double), s);
+    for (int st = 0; st < n_steps && e == cudaSuccess; ++st) {
+        e = batch_prep(d, N, prm, kStageRhs, 0.0, 0.0, s);
+        if (e == cudaSuccess) e = batch_main(d, N, prm, F, false, s);
+        if (e == cudaSuccess) e = gmres_solve(p, N, F, K1, prm, resid, s);
+        if (e == cudaSuccess) e = batch_lincomb(Y, 1.0, N, dt, K1, T, p->num_sms, s);
+        if (e == cudaSuccess) e = batch_prep(d, Y, prm, kStageRhs, 0.0, 0.0, s);
+        if (e == cudaSuccess) e = batch_main(d, Y, prm, F, false, s);
+        if (e == cudaSuccess) e = batch_lincomb(F, 1.0, F, -2.0, K1, T, p->num_sms, s);
+        if (e == cudaSuccess) e = gmres_solve(p, N, F, K2, prm, resid, s);
+        if (e == cudaSuccess) e = batch_ros_update(N, 1.5 * dt, K1, 0.5 * dt, K2, T, p->num_sms, s);
+    }
+    return e;
+}
+
 // Adaptive embedded RK 5(4) for every cell to t_end: attempts are enqueued
 // in chunks of 8 (6 RHS evaluations and one control launch each), then the
 // count of finished cells is read back.
@@ -993,6 +1099,28 @@ int pbe_batch_rk45(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* p
         return cudaErrorInvalidValue;
     return rk45(plan, N, params, t_end, rtol, atol, dt0, max_attempts, steps, rejects, attempts,
                 static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_jvp(pbe_batch_t plan, const double* N, const double* v,
+                  const pbe_batch_cell_params_t* params, double* out, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !v || !params || !out) return cudaErrorInvalidDevicePointer;
+    return jvp(plan, N, v, params, out, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,
+                   int n_steps, int krylov_dim, double* resid, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (n_steps < 0 || !(dt > 0.0) || !std::isfinite(dt) || krylov_dim < 1 ||
+        krylov_dim > kGmresMaxDim)
+        return cudaErrorInvalidValue;
+    if (n_steps == 0) return cudaSuccess;
+    return ros2(plan, N, params, dt, n_steps, krylov_dim, resid, static_cast<cudaStream_t>(stream));
 }
 
 int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)

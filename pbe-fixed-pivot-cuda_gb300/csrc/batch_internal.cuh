@@ -57,6 +57,10 @@ struct BatchDev {
     double* Bk;     // breakage term of the stage (gathered by the prep kernel)
     double* k;      // stage derivative (RK4)
     double* kacc;   // k1 + 2 k2 + 2 k3 (+ k4)
+    // Jacobian-vector passes (batch_jvp.cu): the j-side vector of the pass,
+    // unscaled (null for an RHS evaluation), and x times it
+    const double* A;
+    double* Ha;
     double* mom;    // [n_cells * 8] moments of the stage state (death term), [5] clip sum
     int* counter;   // [8] task counter of the persistent kernel
     // hand-over of a tile's first bin (tiles aligned to the cell's top; tile t
@@ -114,6 +118,25 @@ struct Rk45Ctl {
     double t_end, rtol, atol;
 };
 
+// GMRES(m) state of the batched Rosenbrock solves (batch_implicit.cu).
+constexpr int kGmresMaxDim = 64;
+struct GmresDev {
+    double* V;       // [(m + 1) * total] Arnoldi vectors, packed like the cell state
+    double* Z;       // [total] P^-1 v_j: the operand of the next Jacobian-vector product
+    double* W;       // [total] J z on entry of an Arnoldi step, then its new direction
+    double* P;       // [total] diagonal preconditioner
+    double* H;       // [n_cells * (m + 1) * m] rotated Hessenberg columns (column-major)
+    double* gv;      // [n_cells * (m + 1)] rotated right-hand side of the least squares
+    double* cs;      // [n_cells * m] Givens rotations
+    double* sn;
+    double* beta0;   // [n_cells] |r|
+    int* kval;       // [n_cells] Arnoldi steps taken
+    int* done;       // [n_cells] solve ended (converged, breakdown or m steps)
+    long long total;
+    int m;
+    double gt;       // gamma dt
+};
+
 // Launchers (batch_kernels.cu). All are asynchronous on `s`.
 // Once per plan, before any launch (and outside stream capture): the
 // persistent kernel's shared-memory attribute for `kernel`.
@@ -134,6 +157,25 @@ cudaError_t batch_prep_combine(const BatchDev& d, double* N, const pbe_batch_cel
 cudaError_t batch_rk45_control(const BatchDev& d, double* N, const double* Y,
                                const StageCombine& err, double* k0, const Rk45Ctl& ctl,
                                cudaStream_t s);
+// GMRES steps (batch_implicit.cu): start (preconditioner at N, v_0 = r/|r|),
+// Arnoldi step j (after W = J(N) Z), finish (x = P^-1 V y, resid = relative
+// least-squares residual per cell, may be null); elementwise helpers.
+cudaError_t batch_gmres_start(const BatchDev& d, const GmresDev& g, const double* N, const double* r,
+                              const pbe_batch_cell_params_t* params, cudaStream_t s);
+cudaError_t batch_gmres_arnoldi(const BatchDev& d, const GmresDev& g, int j, cudaStream_t s);
+cudaError_t batch_gmres_finish(const BatchDev& d, const GmresDev& g, double* x, double* resid,
+                               cudaStream_t s);
+cudaError_t batch_lincomb(double* out, double a, const double* X, double b, const double* Y,
+                          long long total, int num_sms, cudaStream_t s);
+cudaError_t batch_ros_update(double* N, double c1, const double* K1, double c2, const double* K2,
+                             long long total, int num_sms, cudaStream_t s);
+
+// Prep of one Jacobian-vector pass (batch_kernels.cu, batch_jvp_prep_kernel):
+// j side from A, k side from B, breakage (brk) as the product of its Jacobian
+// at the state G with B, else zero. Followed by batch_main with Y = B and a
+// copy of d whose A = A.
+cudaError_t batch_jvp_prep(const BatchDev& d, const double* A, const double* B, const double* G,
+                           const pbe_batch_cell_params_t* params, bool brk, cudaStream_t s);
 // Persistent RHS kernel over the plan's bundles: out (+)= RHS(Y) for every cell.
 cudaError_t batch_main(const BatchDev& d, const double* Y, const pbe_batch_cell_params_t* params,
                        double* out, bool accumulate, cudaStream_t s);

@@ -195,7 +195,7 @@ __device__ double cell_clip(const AggCellView& v, const TileGroup& G)
                 const int mid = (lo + hi) >> 1;
                 if (dbits(xj + v.x[mid]) >= tb) hi = mid; else lo = mid + 1;
             }
-            const double Nj = v.Nk[j], hj = v.Hk[j], aj = v.a[j], iaj = v.ia[j];
+            const double Nj = v.Aj[j], hj = v.AHj[j], aj = v.a[j], iaj = v.ia[j];
             for (int k = lo; k < n; ++k)
                 acc += rate_gen<K>(j == k, v.b0, v.bbr, v.bsh, Nj, hj, aj, iaj, v.Nk[k], v.Hk[k],
                                    v.a[k], v.ia[k]);
@@ -308,6 +308,8 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
         v.x = x;
         v.Nk = (stage == kStageRhs || stage == kStageNext) ? Nc : Yc;
         v.Hk = d.Hk + off;
+        v.Aj = v.Nk;
+        v.AHj = v.Hk;
         v.Nj = d.Nj + off;
         v.Hj = d.Hj + off;
         v.Fs = v.Nk;
@@ -337,6 +339,95 @@ __device__ __forceinline__ void batch_first_done(const BatchDev& d, double* out,
     *o = accumulate ? __ldcg(o) + v : v;
 }
 
+// ---------------------------------------------------------------------------
+// Prep of one Jacobian-vector pass (one CTA per cell). The aggregation RHS is
+// quadratic: R(N) = T(N, N) with T(a, b) = sum over pairs j <= k of
+// c_d beta(j, k) a_j b_k (deposits as the RHS; death b_i sum_k beta_ik a_k),
+// so J(N) v = T(N, v) + T(v, N), two passes of the persistent pair kernel
+// with the j side from a and the k side from b. This prep builds the j-side
+// arrays from a (coefficient-scaled, and unscaled for the generic path), the
+// k-side x b, the moments of a (death b_i sum_k beta_ik a_k), the clipped
+// pairs' sum of T(a, b), and the breakage term: the breakage RHS is linear
+// in N wherever its guard passes, so with brk its Jacobian-vector product
+// S_j b_j deposited as the RHS deposits S_j N_j, for the bins whose G_j (the
+// state) passes the guard S_j != 0 && G_j > 2.2e-308; without brk, zero.
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(256)
+batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __restrict__ Bv,
+                      const double* __restrict__ Gs, const pbe_batch_cell_params_t* __restrict__ params,
+                      int brk)
+{
+    __shared__ double sh[8];
+    const BatchCellDev cd = d.cells[blockIdx.x];
+    const BatchGridDev gd = d.grids[cd.grid];
+    const pbe_batch_cell_params_t P = params[blockIdx.x];
+    const bool agg = d.kernel >= 0;
+    const int F = d.selection;
+    const int off = cd.off, n = cd.n;
+    const double* x = d.gx + gd.off;
+    const double* a = d.ga + gd.off;
+    const double* ia = d.gia + gd.off;
+    const double cN = (K <= 2) ? P.beta0 : P.beta_br;
+    const double cH = (K == 1 || K == 2) ? P.beta0 : P.beta_sh;
+    double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double ya = A[off + i], yb = Bv[off + i];
+        const double xi = x[i];
+        if (agg) {
+            const double ha = xi * ya;
+            if (K != 2 && K != 4) d.Nj[off + i] = cN * ya;
+            if (NeedH<K>::j) d.Hj[off + i] = cH * ha;
+            d.Ha[off + i] = ha;
+            d.Hk[off + i] = xi * yb;
+            m[0] = fma(ia[i], ya, m[0]);
+            m[1] += ya;
+            m[2] = fma(a[i], ya, m[2]);
+            m[3] = fma(a[i] * a[i], ya, m[3]);
+            m[4] += ha;
+        }
+        if (F >= 0) {
+            double sn = 0.0;
+            if (brk) {
+                const double S = sel_value(F, xi, P.S0, P.v_ref, P.alpha, P.v_min);
+                sn = (S != 0.0 && Gs[off + i] > kBreakageNMin) ? S * yb : 0.0;
+            }
+            d.SN[off + i] = sn;
+        }
+    }
+    __syncthreads();                       // the cell's pass arrays are complete
+    if (agg) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const double s_ = block_sum(m[q], sh);
+            if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + q] = s_;
+        }
+        AggCellView v;
+        v.x = x;
+        v.Nk = Bv + off;
+        v.Hk = d.Hk + off;
+        v.Nj = d.Nj + off;
+        v.Hj = d.Hj + off;
+        v.Aj = A + off;
+        v.AHj = d.Ha + off;
+        v.Fs = v.Nk;
+        v.a = a; v.ia = ia; v.inv_dx = d.ginv_dx + gd.off;
+        v.Bd = d.gBd + gd.off; v.Sd = d.gSd + gd.off; v.Ld = d.gLd + gd.off;
+        v.n = n; v.D0 = gd.D0; v.geo = gd.geo != 0;
+        v.b0 = P.beta0; v.bbr = P.beta_br; v.bsh = P.beta_sh;
+        const TileGroup G{0, static_cast<int>(threadIdx.x), static_cast<int>(blockDim.x)};
+        const double clip = block_sum(cell_clip<K>(v, G), sh);
+        if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + 5] = clip;
+    }
+    if (d.nq > 0) {
+        if (brk) {
+            cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
+        } else {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) d.Bk[off + i] = 0.0;
+        }
+    }
+}
+
 template <int K>
 __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                            const pbe_batch_cell_params_t* __restrict__ params, double* out,
@@ -352,6 +443,8 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
     v.x = d.gx + gd.off;
     v.Nk = Yg + cd.off;
     v.Hk = d.Hk + cd.off;
+    v.Aj = d.A ? d.A + cd.off : v.Nk;        // a Jacobian-vector pass: the j-side vector
+    v.AHj = d.A ? d.Ha + cd.off : v.Hk;
     v.Nj = d.Nj + cd.off;
     v.Hj = d.Hj + cd.off;
     v.Fs = (K == 2) ? v.Hk : v.Nk;
@@ -496,6 +589,14 @@ cudaError_t prep_any(const BatchDev& d, double* N, const pbe_batch_cell_params_t
     return cudaGetLastError();
 }
 
+template <int K>
+cudaError_t jvp_prep_k(const BatchDev& d, const double* A, const double* B, const double* G,
+                       const pbe_batch_cell_params_t* params, bool brk, cudaStream_t s)
+{
+    batch_jvp_prep_kernel<K><<<d.n_cells, 256, 0, s>>>(d, A, B, G, params, brk ? 1 : 0);
+    return cudaGetLastError();
+}
+
 __global__ void __launch_bounds__(256)
 rk45_control_kernel(BatchDev d, double* N, const double* __restrict__ Y, StageCombine e,
                     double* k0, Rk45Ctl ctl)
@@ -553,6 +654,21 @@ cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params
 {
     const StageCombine none{};
     return prep_any(d, N, params, stage, c, dt6, none, s);
+}
+
+cudaError_t batch_jvp_prep(const BatchDev& d, const double* A, const double* B, const double* G,
+                          const pbe_batch_cell_params_t* params, bool brk, cudaStream_t s)
+{
+    if (d.n_cells <= 0) return cudaErrorInvalidValue;
+    switch (d.kernel < 0 ? 0 : d.kernel) {
+    case 0: return jvp_prep_k<0>(d, A, B, G, params, brk, s);
+    case 1: return jvp_prep_k<1>(d, A, B, G, params, brk, s);
+    case 2: return jvp_prep_k<2>(d, A, B, G, params, brk, s);
+    case 3: return jvp_prep_k<3>(d, A, B, G, params, brk, s);
+    case 4: return jvp_prep_k<4>(d, A, B, G, params, brk, s);
+    case 5: return jvp_prep_k<5>(d, A, B, G, params, brk, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t batch_prep_combine(const BatchDev& d, double* N, const pbe_batch_cell_params_t* params,

@@ -140,6 +140,23 @@ class BatchPlan:
                                              _ptr(gN, "gN"), _ptr(gparams, "gparams"),
                                              _ptr(params, "params"), _stream(stream))
 
+    def jvp(self, N, v, out, params, stream=None) -> int:
+        """out = J(N) v for every cell (overwritten), J = d RHS / dN."""
+        return _lib.load().pbe_batch_jvp(self._h, _ptr(N, "N"), _ptr(v, "v"),
+                                         _ptr(params, "params"), _ptr(out, "out"),
+                                         _stream(stream))
+
+    def ros2(self, N, params, dt: float, n_steps: int, krylov_dim: int = 16, resid=None,
+             stream=None) -> int:
+        """n_steps linearly implicit ROS2 steps in place on N; each stage's system
+        (I - gamma dt J) k = r solved by GMRES(krylov_dim) with Jacobian-vector
+        products. resid: optional device array [n_cells], the largest relative
+        least-squares residual of the call's solves per cell."""
+        return _lib.load().pbe_batch_ros2(self._h, _ptr(N, "N"), _ptr(params, "params"),
+                                          float(dt), int(n_steps), int(krylov_dim),
+                                          _ptr(resid, "resid") if resid is not None else None,
+                                          _stream(stream))
+
     def tape_forward(self, N, params, dt: float, n_steps: int, checkpoint_every: int,
                      stream=None) -> int:
         """n_steps RK4 steps in place on N with checkpoints for tape_backward."""
