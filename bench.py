@@ -457,6 +457,34 @@ def classes_section(dev, stream):
         torch.cuda.synchronize()
         tape_fwd_ms, tape_bwd_ms = a.elapsed_time(b), b.elapsed_time(c_)
         grad_finite = bool(torch.isfinite(gN0).all()) and bool(torch.isfinite(gP).all())
+        # Jacobian-vector product against the RHS, and the linearly implicit ROS2 step
+        rhs = torch.zeros(plan.total, **f64)
+        vv = dN.flip(0).contiguous()
+        jv = torch.zeros(plan.total, **f64)
+        t_call = {}
+        for name, call in (("rhs", lambda: plan.rhs(dN, rhs, P, stream=stream)),
+                           ("jvp", lambda: plan.jvp(dN, vv, jv, P, stream=stream))):
+            for _ in range(3):
+                pg.check(call(), name)
+            a.record(stream)
+            for _ in range(10):
+                pg.check(call(), name)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_call[name] = a.elapsed_time(b) / 10
+        m_kry, ros_steps = 8, 3
+        resid = torch.zeros(len(cfg["cell_n"]), **f64)
+        Yr = dN.clone()
+        pg.check(plan.ros2(Yr, P, 0.5, 1, m_kry, resid, stream=stream), "ros2 warm-up")
+        Yr = dN.clone()
+        torch.cuda.synchronize()
+        a.record(stream)
+        pg.check(plan.ros2(Yr, P, 0.5, ros_steps, m_kry, resid, stream=stream), "ros2")
+        b.record(stream)
+        torch.cuda.synchronize()
+        ros_ms = a.elapsed_time(b) / ros_steps
+        ros_finite = bool(torch.isfinite(Yr).all())
+        ros_resid = float(resid.max())
     plan.close()
     cn = cfg["cell_n"].astype(np.float64)
     gemm_flops = float((2.0 * cn * cn).sum() * 2)          # two separable components
@@ -475,6 +503,15 @@ def classes_section(dev, stream):
                     "forward_ms": round(tape_fwd_ms, 2), "backward_ms": round(tape_bwd_ms, 2),
                     "backward_forward_ratio": round(tape_bwd_ms / tape_fwd_ms, 4),
                     "gradient_finite": grad_finite},
+        "rhs_ms": round(t_call["rhs"], 4),
+        "jvp_ms": round(t_call["jvp"], 4),
+        "jvp_rhs_ratio": round(t_call["jvp"] / t_call["rhs"], 4),
+        "ros2": {"what": "linearly implicit ROS2 steps of dt = 0.5 s, every stage solved by "
+                         "GMRES(8) with Jacobian-vector products (2 RHS + 16 JVP per step)",
+                 "krylov_dim": m_kry, "ms_per_step": round(ros_ms, 3),
+                 "rhs_equivalents_per_step": round(ros_ms / t_call["rhs"], 2),
+                 "cell_steps_per_s": round(len(cn) / (ros_ms / 1e3), 1),
+                 "max_relative_residual": ros_resid, "finite": ros_finite},
         "death_moments_ms": round(times[pg.DEATH_MOMENTS], 4),
         "death_dmma_ms": round(times[pg.DEATH_DMMA], 4),
         "dmma_over_moments_time": round(times[pg.DEATH_DMMA] / times[pg.DEATH_MOMENTS], 2),

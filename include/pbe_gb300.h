@@ -318,6 +318,16 @@ int pbe_batch_jvp(pbe_batch_t plan, const double* N, const double* v,
 int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,
                    int n_steps, int krylov_dim, double* resid, void* stream);
 
+/* Mesh-field (structure-of-arrays) layout for CFD coupling: soa[i * ld + c]
+ * (device) is bin i of cell c, one field per bin over the cells, ld >=
+ * n_cells; rows i < n_c of every cell are read (from_soa: soa -> packed N)
+ * or written (to_soa: packed N -> soa); entries beyond a cell's n_c are not
+ * touched. A tiled transpose through shared memory, coalesced both ways. The
+ * reference's README names this use (many cells of a CFD mesh) but ships no
+ * layer for it. */
+int pbe_batch_from_soa(pbe_batch_t plan, const double* soa, long long ld, double* N, void* stream);
+int pbe_batch_to_soa(pbe_batch_t plan, const double* N, double* soa, long long ld, void* stream);
+
 /* Schedule in use: group_size[c] (16 entries) = threads per tile task for
  * cells with floor(log2(n)) == c (0 where no cell falls), *n_bundles = the
  * number of bundles in the persistent launch. Either pointer may be NULL. */

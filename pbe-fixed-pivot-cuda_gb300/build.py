@@ -31,7 +31,7 @@ REF_RUNNER_LIB = os.path.join(ORACLE_BUILD, "libref_runner.so")
 
 SOURCES = ["aggregation.cu", "breakage.cu", "vjp.cu", "api.cu", "noalloc.cu",
            "batch_kernels.cu", "batch.cu", "adjoint.cu", "death_gemm.cu",
-           "batch_vjp.cu", "batch_implicit.cu", "daughter.cpp"]
+           "batch_vjp.cu", "batch_implicit.cu", "batch_soa.cu", "daughter.cpp"]
 ARCH = ["-gencode=arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
 

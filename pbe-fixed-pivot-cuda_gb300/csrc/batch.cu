@@ -1123,6 +1123,24 @@ int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* p
     return ros2(plan, N, params, dt, n_steps, krylov_dim, resid, static_cast<cudaStream_t>(stream));
 }
 
+int pbe_batch_from_soa(pbe_batch_t plan, const double* soa, long long ld, double* N, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!soa || !N) return cudaErrorInvalidDevicePointer;
+    if (ld < plan->n_cells) return cudaErrorInvalidValue;
+    return batch_soa(plan->d, soa, N, ld, plan->max_n, true, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_to_soa(pbe_batch_t plan, const double* N, double* soa, long long ld, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!soa || !N) return cudaErrorInvalidDevicePointer;
+    if (ld < plan->n_cells) return cudaErrorInvalidValue;
+    return batch_soa(plan->d, N, soa, ld, plan->max_n, false, static_cast<cudaStream_t>(stream));
+}
+
 int pbe_batch_schedule(pbe_batch_t plan, int* group_size, int* n_bundles)
 {
     if (!plan) return cudaErrorInvalidValue;

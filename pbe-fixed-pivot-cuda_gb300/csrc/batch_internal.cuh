@@ -157,6 +157,11 @@ cudaError_t batch_prep_combine(const BatchDev& d, double* N, const pbe_batch_cel
 cudaError_t batch_rk45_control(const BatchDev& d, double* N, const double* Y,
                                const StageCombine& err, double* k0, const Rk45Ctl& ctl,
                                cudaStream_t s);
+// Mesh-field layout (batch_soa.cu): soa[i ld + c] <-> N[off_c + i] for the
+// bins i < n_c of every cell (to_packed: soa -> N), max_n = the longest cell.
+cudaError_t batch_soa(const BatchDev& d, const double* src, double* dst, long long ld, int max_n,
+                      bool to_packed, cudaStream_t s);
+
 // GMRES steps (batch_implicit.cu): start (preconditioner at N, v_0 = r/|r|),
 // Arnoldi step j (after W = J(N) Z), finish (x = P^-1 V y, resid = relative
 // least-squares residual per cell, may be null); elementwise helpers.

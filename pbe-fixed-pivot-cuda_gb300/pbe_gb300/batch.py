@@ -146,6 +146,17 @@ class BatchPlan:
                                          _ptr(params, "params"), _ptr(out, "out"),
                                          _stream(stream))
 
+    def from_soa(self, soa, ld: int, N, stream=None) -> int:
+        """N[off_c + i] = soa[i * ld + c] for the bins of every cell (mesh fields
+        -> packed state)."""
+        return _lib.load().pbe_batch_from_soa(self._h, _ptr(soa, "soa"), int(ld), _ptr(N, "N"),
+                                              _stream(stream))
+
+    def to_soa(self, N, soa, ld: int, stream=None) -> int:
+        """soa[i * ld + c] = N[off_c + i] for the bins of every cell."""
+        return _lib.load().pbe_batch_to_soa(self._h, _ptr(N, "N"), _ptr(soa, "soa"), int(ld),
+                                            _stream(stream))
+
     def ros2(self, N, params, dt: float, n_steps: int, krylov_dim: int = 16, resid=None,
              stream=None) -> int:
         """n_steps linearly implicit ROS2 steps in place on N; each stage's system
