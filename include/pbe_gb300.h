@@ -318,6 +318,19 @@ int pbe_batch_jvp(pbe_batch_t plan, const double* N, const double* v,
 int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,
                    int n_steps, int krylov_dim, double* resid, void* stream);
 
+/* ROS2 to t_end with a step size per cell: the error of a step is the RMS of
+ * dt (k1 + k2) / 2 -- its difference to the embedded first-order solution
+ * N + dt k1 -- over atol + rtol max(|N|, |N_new|); a step is accepted when it
+ * is <= 1, and the next dt is 0.9 err^(-1/2) dt clamped to [0.2, 5] dt (no
+ * growth after a rejection, never past t_end). Solves as pbe_batch_ros2, with
+ * gamma dt per cell. steps / rejects (host, n_cells) and *attempts as for
+ * pbe_batch_rk45; returns cudaErrorNotReady (600) when some cell has not
+ * reached t_end within max_attempts. */
+int pbe_batch_ros2_adaptive(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                            double t_end, double rtol, double atol, double dt0, int krylov_dim,
+                            int max_attempts, int* steps, int* rejects, int* attempts,
+                            double* resid, void* stream);
+
 /* Mesh-field (structure-of-arrays) layout for CFD coupling: soa[i * ld + c]
  * (device) is bin i of cell c, one field per bin over the cells, ld >=
  * n_cells; rows i < n_c of every cell are read (from_soa: soa -> packed N)

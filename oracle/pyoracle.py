@@ -229,6 +229,43 @@ def ros2_step(N, x, dt, agg=None, brk=None):
     return N + (1.5 * dt * k1 + 0.5 * dt * k2)
 
 
+def ros2_adaptive(N, x, t_end, rtol, atol, dt0, agg=None, brk=None, max_attempts=100000):
+    """ROS2 to t_end with the step control of pbe_batch_ros2_adaptive (dense
+    solves): err = RMS(dt (k1 + k2) / 2 / (atol + rtol max(|N|, |N_new|))),
+    accept when <= 1, dt *= clamp(0.9 err^-1/2, 0.2, 5) (<= 1 after a
+    rejection), never past t_end. Returns (N, steps, rejects, status)."""
+    N, x = _f64(N).copy(), _f64(x)
+    g = 1.0 + 1.0 / np.sqrt(2.0)
+    t, dt = 0.0, min(dt0, t_end)
+    steps = rejects = 0
+    for _ in range(max_attempts):
+        A = np.eye(len(x)) - g * dt * jacobian(N, x, agg, brk)
+        k1 = np.linalg.solve(A, _rhs(N, x, agg, brk))
+        k2 = np.linalg.solve(A, _rhs(N + dt * k1, x, agg, brk) - 2.0 * k1)
+        Nn = N + dt * (1.5 * k1 + 0.5 * k2)
+        sc = atol + rtol * np.maximum(np.abs(N), np.abs(Nn))
+        err = np.sqrt(np.mean((dt * (0.5 * (k1 + k2)) / sc) ** 2))
+        finite = np.isfinite(err)
+        accept = bool(finite and err <= 1.0)
+        fac = 0.2 if not finite else (5.0 if err == 0.0 else min(5.0, max(0.2, 0.9 / np.sqrt(err))))
+        if not accept:
+            fac = min(fac, 1.0)
+        if accept:
+            t += dt
+            N = Nn
+            steps += 1
+        else:
+            rejects += 1
+        rem = t_end - t
+        nd = min(dt * fac, rem)
+        if accept and rem <= 1e-12 * max(abs(t_end), 1.0):
+            return N, steps, rejects, 1
+        if nd <= 1e-14 * max(abs(t_end), 1.0):
+            return N, steps, rejects, 2
+        dt = nd
+    return N, steps, rejects, 0
+
+
 def rk4_step(N, x, dt, agg=None, brk=None):
     """One classical RK4 step; agg = dict(kernel, beta0, beta_br, beta_sh[, log_x0, inv_log_r]),
     brk = dict(t_q, bw_q, selection, S0, v_ref, alpha, v_min). Returns the new N."""

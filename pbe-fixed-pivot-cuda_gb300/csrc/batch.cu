@@ -73,6 +73,8 @@ struct pbe_batch_plan {
     pbe_gb300::GmresDev gm{};
     int gm_cap = 0;                    // Krylov dimension the GMRES buffers hold
     double* ros = nullptr;             // F, K1, K2, Y (4 packed vectors)
+    double* ros_cell = nullptr;        // adaptive: t, dt, gamma dt per cell
+    int* ros_int = nullptr;            // adaptive: status, steps, rejects per cell; done
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -827,6 +829,7 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     p->gm.m = m;
     p->gm.total = static_cast<long long>(C);
     p->gm.gt = (1.0 + 1.0 / std::sqrt(2.0)) * dt;
+    p->gm.gtc = nullptr;
     double* F = p->ros;
     double* K1 = p->ros + C;
     double* K2 = p->ros + 2 * C;
@@ -846,6 +849,84 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
         if (e == cudaSuccess) e = batch_ros_update(N, 1.5 * dt, K1, 0.5 * dt, K2, T, p->num_sms, s);
     }
     return e;
+}
+
+// ROS2 to t_end with a step size per cell (batch_implicit.cu: stage and
+// controller kernels, Rk45Ctl conventions): attempts are enqueued in chunks of
+// 4, then the count of finished cells is read back. A finished cell runs with
+// dt = 0 (its solves are trivial; the pair kernel still covers it).
+cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
+                          double t_end, double rtol, double atol, double dt0, int m,
+                          int max_attempts, int* steps_out, int* rejects_out, int* attempts_out,
+                          double* resid, cudaStream_t s)
+{
+    const size_t C = static_cast<size_t>(p->total), nc = static_cast<size_t>(p->n_cells);
+    cudaError_t e = gmres_alloc(p, m);
+    if (e == cudaSuccess && !p->ros) {
+        e = plan_alloc(p, &p->ros, 4 * C);
+        if (e != cudaSuccess) p->ros = nullptr;
+    }
+    if (e == cudaSuccess && !p->ros_cell) {
+        e = plan_alloc(p, &p->ros_cell, 3 * nc);
+        if (e == cudaSuccess) e = plan_alloc(p, &p->ros_int, 3 * nc + 1);
+        if (e != cudaSuccess) { p->ros_cell = nullptr; p->ros_int = nullptr; }
+    }
+    if (e != cudaSuccess) return e;
+    Rk45Ctl ctl;
+    ctl.t = p->ros_cell;
+    ctl.dt = p->ros_cell + nc;
+    ctl.status = p->ros_int;
+    ctl.steps = p->ros_int + nc;
+    ctl.rejects = p->ros_int + 2 * nc;
+    ctl.done = p->ros_int + 3 * nc;
+    ctl.t_end = t_end;
+    ctl.rtol = rtol;
+    ctl.atol = atol;
+    double* gtc = p->ros_cell + 2 * nc;
+    p->gm.m = m;
+    p->gm.total = static_cast<long long>(C);
+    p->gm.gt = 0.0;
+    p->gm.gtc = gtc;
+    const double gamma = 1.0 + 1.0 / std::sqrt(2.0);
+    std::vector<double> init(3 * nc, 0.0);
+    for (size_t c = 0; c < nc; ++c) init[nc + c] = std::min(dt0, t_end);
+    e = cudaMemcpyAsync(p->ros_cell, init.data(), init.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->ros_int, 0, (3 * nc + 1) * sizeof(int), s);
+    if (e == cudaSuccess && resid) e = cudaMemsetAsync(resid, 0, nc * sizeof(double), s);
+    double* F = p->ros;
+    double* K1 = p->ros + C;
+    double* K2 = p->ros + 2 * C;
+    double* Y = p->ros + 3 * C;
+    const BatchDev& d = p->d;
+    const long long T = static_cast<long long>(C);
+    int attempts = 0, done = 0;
+    while (e == cudaSuccess && attempts < max_attempts && done < p->n_cells) {
+        const int chunk = std::min(4, max_attempts - attempts);
+        for (int a = 0; a < chunk && e == cudaSuccess; ++a) {
+            e = batch_ros2_stage(d, N, K1, Y, gtc, ctl, gamma, s);       // gamma dt per cell
+            if (e == cudaSuccess) e = batch_prep(d, N, prm, kStageRhs, 0.0, 0.0, s);
+            if (e == cudaSuccess) e = batch_main(d, N, prm, F, false, s);
+            if (e == cudaSuccess) e = gmres_solve(p, N, F, K1, prm, resid, s);
+            if (e == cudaSuccess) e = batch_ros2_stage(d, N, K1, Y, gtc, ctl, gamma, s);
+            if (e == cudaSuccess) e = batch_prep(d, Y, prm, kStageRhs, 0.0, 0.0, s);
+            if (e == cudaSuccess) e = batch_main(d, Y, prm, F, false, s);
+            if (e == cudaSuccess) e = batch_lincomb(F, 1.0, F, -2.0, K1, T, p->num_sms, s);
+            if (e == cudaSuccess) e = gmres_solve(p, N, F, K2, prm, resid, s);
+            if (e == cudaSuccess) e = batch_ros2_control(d, N, K1, K2, ctl, s);
+        }
+        attempts += chunk;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&done, ctl.done, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e == cudaSuccess && steps_out)
+        e = cudaMemcpyAsync(steps_out, ctl.steps, nc * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && rejects_out)
+        e = cudaMemcpyAsync(rejects_out, ctl.rejects, nc * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (attempts_out) *attempts_out = attempts;
+    if (e != cudaSuccess) return e;
+    return done == p->n_cells ? cudaSuccess : cudaErrorNotReady;
 }
 
 // Adaptive embedded RK 5(4) for every cell to t_end: attempts are enqueued
@@ -1121,6 +1202,22 @@ int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* p
         return cudaErrorInvalidValue;
     if (n_steps == 0) return cudaSuccess;
     return ros2(plan, N, params, dt, n_steps, krylov_dim, resid, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_ros2_adaptive(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params,
+                            double t_end, double rtol, double atol, double dt0, int krylov_dim,
+                            int max_attempts, int* steps, int* rejects, int* attempts,
+                            double* resid, void* stream)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!N || !params) return cudaErrorInvalidDevicePointer;
+    if (!(t_end > 0.0) || !std::isfinite(t_end) || !(rtol >= 0.0) || !(atol >= 0.0) ||
+        !(rtol > 0.0 || atol > 0.0) || !(dt0 > 0.0) || max_attempts <= 0 || krylov_dim < 1 ||
+        krylov_dim > kGmresMaxDim)
+        return cudaErrorInvalidValue;
+    return ros2_adaptive(plan, N, params, t_end, rtol, atol, dt0, krylov_dim, max_attempts, steps,
+                         rejects, attempts, resid, static_cast<cudaStream_t>(stream));
 }
 
 int pbe_batch_from_soa(pbe_batch_t plan, const double* soa, long long ld, double* N, void* stream)

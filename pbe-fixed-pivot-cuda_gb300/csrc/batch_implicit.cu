@@ -59,6 +59,7 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
     const double* a = d.ga + gd.off;
     const double* ia = d.gia + gd.off;
     const bool agg = d.kernel >= 0;
+    const double gt = g.gtc ? g.gtc[c] : g.gt;
     if (agg) {
         double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -88,7 +89,7 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
             const double S = sel_value_i(d.selection, xi, P.S0, P.v_ref, P.alpha, P.v_min);
             if (S != 0.0 && y > kBreakageNMin) loss += S;
         }
-        const double p = 1.0 + g.gt * fmax(loss, 0.0);
+        const double p = 1.0 + gt * fmax(loss, 0.0);
         g.P[off + i] = (p == p && p < 1.7e308) ? p : 1.0;
         const double ri = r[off + i];
         rr = fma(ri, ri, rr);
@@ -129,9 +130,10 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
         return;
     }
     double* w = g.W + off;
+    const double gt = g.gtc ? g.gtc[c] : g.gt;
     double s0 = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double wi = fma(-g.gt, w[i], g.Z[off + i]);
+        const double wi = fma(-gt, w[i], g.Z[off + i]);
         w[i] = wi;
         s0 = fma(wi, wi, s0);
     }
@@ -238,6 +240,76 @@ ros_update_kernel(double* __restrict__ N, double c1, const double* __restrict__ 
         N[i] = N[i] + fma(c1, K1[i], c2 * K2[i]);
 }
 
+// Adaptive ROS2. The error estimate is the difference to the embedded
+// first-order solution N + dt k1: dt (k1 + k2) / 2. (In this form of the
+// method k2 -> -R for small dt, so a first-order combination b1 k1 + b2 k2
+// needs b1 - b2 = 1; the only one that also damps infinitely stiff
+// components, as ROS2 does, is ROS2's own (3/2, 1/2). The estimate of N + dt k1
+// keeps (1/(2 g^2) - 1/g) N of such a component; in practice the stiff
+// components sit near their quasi-steady state and the steps stay limited by
+// accuracy.)
+
+// Per cell: the second stage's state and gamma dt_c.
+__global__ void __launch_bounds__(256)
+ros2_stage_kernel(BatchDev d, const double* __restrict__ N, const double* __restrict__ K1,
+                  double* __restrict__ Y, double* __restrict__ gtc, Rk45Ctl ctl, double gamma)
+{
+    const int c = blockIdx.x;
+    const BatchCellDev cd = d.cells[c];
+    const double dt = ctl.dt[c];           // 0 for a finished cell: Y = N
+    for (int i = threadIdx.x; i < cd.n; i += blockDim.x)
+        Y[cd.off + i] = fma(dt, K1[cd.off + i], N[cd.off + i]);
+    if (threadIdx.x == 0) gtc[c] = gamma * dt;
+}
+
+__global__ void __launch_bounds__(256)
+ros2_control_kernel(BatchDev d, double* __restrict__ N, const double* __restrict__ K1,
+                    const double* __restrict__ K2, Rk45Ctl ctl)
+{
+    __shared__ double sh[8];
+    __shared__ int accept_s;
+    const int c = blockIdx.x;
+    if (ctl.status[c] != 0) return;                 // whole block
+    const BatchCellDev cd = d.cells[c];
+    const int off = cd.off, n = cd.n;
+    const double dt = ctl.dt[c];
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double k1 = K1[off + i], k2 = K2[off + i], y = N[off + i];
+        const double yn = y + dt * fma(1.5, k1, 0.5 * k2);
+        const double sc = ctl.atol + ctl.rtol * fmax(fabs(y), fabs(yn));
+        const double r = (dt * (0.5 * (k1 + k2))) / sc;
+        s2 = fma(r, r, s2);
+    }
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) {
+        const double err = sqrt(s2 / n);
+        const bool finite = (err == err) && err <= 1.7e308;
+        const bool accept = finite && err <= 1.0;
+        double fac;
+        if (!finite) fac = 0.2;
+        else if (err == 0.0) fac = 5.0;
+        else fac = fmin(5.0, fmax(0.2, 0.9 / sqrt(err)));
+        if (!accept) fac = fmin(fac, 1.0);
+        double t = ctl.t[c];
+        if (accept) { t += dt; ctl.t[c] = t; ctl.steps[c] += 1; }
+        else ctl.rejects[c] += 1;
+        const double rem = ctl.t_end - t;
+        double nd = fmin(dt * fac, rem);
+        int st = 0;
+        if (accept && rem <= 1e-12 * fmax(fabs(ctl.t_end), 1.0)) { st = 1; nd = 0.0; }
+        else if (nd <= 1e-14 * fmax(fabs(ctl.t_end), 1.0)) { st = 2; nd = 0.0; }
+        ctl.dt[c] = nd;
+        if (st != 0) { ctl.status[c] = st; atomicAdd(ctl.done, 1); }
+        accept_s = accept ? 1 : 0;
+    }
+    __syncthreads();
+    if (accept_s) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            N[off + i] = N[off + i] + dt * fma(1.5, K1[off + i], 0.5 * K2[off + i]);
+    }
+}
+
 template <int K>
 cudaError_t start_k(const BatchDev& d, const GmresDev& g, const double* N, const double* r,
                     const pbe_batch_cell_params_t* params, cudaStream_t s)
@@ -286,6 +358,20 @@ cudaError_t batch_lincomb(double* out, double a, const double* X, double b, cons
                           long long total, int num_sms, cudaStream_t s)
 {
     lincomb_kernel<<<elementwise_grid(total, num_sms), 256, 0, s>>>(out, a, X, b, Y, total);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_ros2_stage(const BatchDev& d, const double* N, const double* K1, double* Y,
+                             double* gtc, const Rk45Ctl& ctl, double gamma, cudaStream_t s)
+{
+    ros2_stage_kernel<<<d.n_cells, 256, 0, s>>>(d, N, K1, Y, gtc, ctl, gamma);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_ros2_control(const BatchDev& d, double* N, const double* K1, const double* K2,
+                               const Rk45Ctl& ctl, cudaStream_t s)
+{
+    ros2_control_kernel<<<d.n_cells, 256, 0, s>>>(d, N, K1, K2, ctl);
     return cudaGetLastError();
 }
 

@@ -132,6 +132,7 @@ struct GmresDev {
     double* beta0;   // [n_cells] |r|
     int* kval;       // [n_cells] Arnoldi steps taken
     int* done;       // [n_cells] solve ended (converged, breakdown or m steps)
+    const double* gtc;   // [n_cells] gamma dt per cell (adaptive steps), or null: gt
     long long total;
     int m;
     double gt;       // gamma dt
@@ -174,6 +175,16 @@ cudaError_t batch_lincomb(double* out, double a, const double* X, double b, cons
                           long long total, int num_sms, cudaStream_t s);
 cudaError_t batch_ros_update(double* N, double c1, const double* K1, double c2, const double* K2,
                              long long total, int num_sms, cudaStream_t s);
+// Adaptive ROS2 (per-cell dt in ctl.dt, Rk45Ctl conventions): Y = N + dt_c K1
+// and gtc[c] = gamma dt_c for every cell; then, after the second stage, the
+// controller: err = RMS of dt_c (K1 + K2) / 2 (the difference to the embedded
+// first-order solution N + dt_c K1) over atol + rtol max(|N|, |N_new|),
+// accept when <= 1 (N = N + dt_c (3/2 K1 + 1/2 K2)), next dt from
+// 0.9 err^(-1/2) clamped to [0.2, 5].
+cudaError_t batch_ros2_stage(const BatchDev& d, const double* N, const double* K1, double* Y,
+                             double* gtc, const Rk45Ctl& ctl, double gamma, cudaStream_t s);
+cudaError_t batch_ros2_control(const BatchDev& d, double* N, const double* K1, const double* K2,
+                               const Rk45Ctl& ctl, cudaStream_t s);
 
 // Prep of one Jacobian-vector pass (batch_kernels.cu, batch_jvp_prep_kernel):
 // j side from A, k side from B, breakage (brk) as the product of its Jacobian

@@ -116,6 +116,9 @@ _SIGNATURES = {
                             ctypes.c_double, _I, _P, _P, _P, _P]),
     "pbe_batch_jvp": (_I, [_P, _P, _P, _P, _P, _P]),
     "pbe_batch_from_soa": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
+    "pbe_batch_ros2_adaptive": (_I, [_P, _P, _P, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P, _P,
+                                     _P]),
     "pbe_batch_to_soa": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
     "pbe_batch_ros2": (_I, [_P, _P, _P, ctypes.c_double, _I, _I, _P, _P]),
     "pbe_daughter_table": (_I, [_I, _I, ctypes.c_double, ctypes.c_double, _P, _P, _I, _P]),

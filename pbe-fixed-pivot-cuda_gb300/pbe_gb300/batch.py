@@ -146,6 +146,21 @@ class BatchPlan:
                                          _ptr(params, "params"), _ptr(out, "out"),
                                          _stream(stream))
 
+    def ros2_adaptive(self, N, params, t_end: float, rtol: float = 1e-6, atol: float = 0.0,
+                      dt0: float = 1e-3, krylov_dim: int = 16, max_attempts: int = 10000,
+                      resid=None, stream=None):
+        """ROS2 to t_end with a step size per cell. Returns (code, accepted steps
+        per cell, rejected steps per cell, attempts); code 600 (ERR_NOT_READY)
+        if max_attempts ran out."""
+        steps = np.zeros(self.n_cells, dtype=np.int32)
+        rejects = np.zeros(self.n_cells, dtype=np.int32)
+        att = ctypes.c_int()
+        code = _lib.load().pbe_batch_ros2_adaptive(
+            self._h, _ptr(N, "N"), _ptr(params, "params"), float(t_end), float(rtol),
+            float(atol), float(dt0), int(krylov_dim), int(max_attempts), steps.ctypes.data,
+            rejects.ctypes.data, ctypes.byref(att), _ptr(resid, "resid"), _stream(stream))
+        return code, steps, rejects, att.value
+
     def from_soa(self, soa, ld: int, N, stream=None) -> int:
         """N[off_c + i] = soa[i * ld + c] for the bins of every cell (mesh fields
         -> packed state)."""

@@ -166,3 +166,67 @@ def test_ros2_argument_errors():
         assert plan.ros2(dN, dp, 0.1, -1) == pg.ERR_INVALID_VALUE
         assert plan.ros2(dN, dp, 0.1, 0) == 0
         assert plan.jvp(0, dN, dN, dp) == pg.ERR_INVALID_DEVICE_POINTER
+
+
+def test_ros2_adaptive_matches_dense_oracle_controller():
+    """Exact solves (krylov_dim >= n): the per-cell step sequence (accepted and
+    rejected steps) equals the oracle's controller run with dense solves."""
+    torch = _torch()
+    rng = np.random.default_rng(4242)
+    grids, cell_n, cell_grid, N, params = mixed_batch(rng, 5, 2, n_cells=8, n_max=32,
+                                                      kinds=("geo_fine", "geo_coarse"))
+    N = [np.abs(Nc) for Nc in N]
+    t_q, bw_q = DAUGHTER
+    t_end, rtol, atol, dt0 = 4.0, 1e-4, 1e-6 * max(Nc.max() for Nc in N), 0.1
+    with pg.BatchPlan(grids, cell_n, cell_grid, 5, 2, t_q, bw_q) as plan:
+        dN = t(np.concatenate(N))
+        code, steps, rejects, att = plan.ros2_adaptive(dN, t(params), t_end, rtol, atol, dt0,
+                                                       krylov_dim=40)
+        assert code == 0, pg.error_string(code)
+        torch.cuda.synchronize()
+        got = dN.cpu().numpy()
+    for c in range(len(cell_n)):
+        x = grids[cell_grid[c]][:cell_n[c]]
+        agg, brk = _dicts(5, 2, params[c], t_q, bw_q)
+        ref, st, rj, status = pyoracle.ros2_adaptive(N[c], x, t_end, rtol, atol, dt0, agg, brk)
+        assert status == 1
+        # the step sizes agree to round-off (GMRES vs dense LU): the counts may
+        # differ by the last, shortest step
+        assert abs(int(steps[c]) - st) <= 1 and rejects[c] == rj, (c, steps[c], rejects[c], st, rj)
+        o = plan.offsets[c]
+        sc = np.abs(ref).max() + 1e-300
+        assert np.abs(got[o:o + cell_n[c]] - ref).max() <= 1e-8 * sc, c
+
+
+def test_ros2_adaptive_on_a_persistently_stiff_cell():
+    """Aggregation (G = 200 s^-1) against power-law breakage S ~ (x/v_ref)^2:
+    the largest bins keep breaking at up to ~2.5e7 s^-1 while aggregation
+    refills them, so an explicit method stays stability-limited throughout
+    (RK45 does not reach t_end within 20000 attempts), while ROS2's steps are
+    limited by accuracy only. Exact solves (krylov_dim >= n): the run follows
+    the oracle's dense-solve controller."""
+    torch = _torch()
+    n = 40
+    x = 1e-18 * 2.0 ** (np.arange(n) / 2)
+    N0 = pg.grids.lognormal_ic(x, 8, 1.0, 1e14)
+    t_q, bw_q = pg.quadrature.uniform(4)
+    prm = pg.batch.cell_params(1, beta_br=6.73e-18, beta_sh=4 * 200 / 3, S0=1.0,
+                               v_ref=float(x[14]), alpha=2.0)
+    agg = dict(kernel=5, beta_br=6.73e-18, beta_sh=4 * 200 / 3)
+    brk = dict(t_q=t_q, bw_q=bw_q, selection=2, S0=1.0, v_ref=float(x[14]), alpha=2.0)
+    t_end, rtol, atol, dt0 = 20.0, 1e-3, 1e-6 * N0.max(), 1e-3
+    ref, st, rj, status = pyoracle.ros2_adaptive(N0, x, t_end, rtol, atol, dt0, agg, brk)
+    assert status == 1
+    with pg.BatchPlan([x], [n], [0], 5, 2, t_q, bw_q) as plan:
+        a, b = t(N0.copy()), t(N0.copy())
+        code, steps, rejects, att = plan.ros2_adaptive(a, t(prm), t_end, rtol, atol, dt0,
+                                                       krylov_dim=n)
+        assert code == 0, pg.error_string(code)
+        code_rk, s_rk, _, att_rk = plan.rk45(b, t(prm), t_end, rtol, atol, dt0,
+                                             max_attempts=20000)
+        torch.cuda.synchronize()
+        A = a.cpu().numpy()
+    assert code_rk == pg.ERR_NOT_READY and att_rk == 20000
+    assert abs(int(steps[0]) - st) <= 1 and rejects[0] == rj, (steps, rejects, st, rj)
+    assert att < 20000 // 4
+    assert np.abs(A - ref).max() <= 1e-8 * np.abs(ref).max()
