@@ -405,6 +405,7 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     if (e == cudaSuccess) e = plan_alloc(p, &d.gBd, G);
     if (e == cudaSuccess) e = plan_alloc(p, &d.gSd, G);
     if (e == cudaSuccess) e = plan_alloc(p, &d.gLd, G);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.gSl, G);
     if (e == cudaSuccess) e = plan_alloc(p, &d.bfirst, static_cast<size_t>(foff));
     if (e == cudaSuccess) e = plan_alloc(p, &d.bwlo, static_cast<size_t>(woff));
     if (e == cudaSuccess) e = plan_alloc(p, &d.bwhi, static_cast<size_t>(woff));

@@ -43,6 +43,7 @@ struct BatchDev {
     int nq;            // quadrature points (0 = no breakage)
     // per grid bin (packed by BatchGridDev::off)
     double* gx; double* ga; double* gia; double* ginv_dx; double* gBd; double* gSd; int* gLd;
+    double* gSl;    // shear factor of lag d seen from the larger member: (1 + rho)^3 x_0 / x_d
     // breakage fragment tables: bfirst[foff + q (n+2) + m + 1] = first j with
     // lo(q, j) >= m; bwlo / bwhi[woff + q n + j] = bw_q times the shares of the
     // fragment x_j t_q at lo and lo + 1 (all of bw_q at lo when clipped)

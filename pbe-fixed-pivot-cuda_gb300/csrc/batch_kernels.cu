@@ -62,6 +62,7 @@ batch_grid_kernel(BatchDev d)
         const double s = 1.0 + rho;
         d.gBd[gd->off + i] = brownian_like ? c * (rho + 1.0 / rho + 2.0) : c;
         d.gSd[gd->off + i] = c * (s * s) * s;
+        d.gSl[gd->off + i] = (s * s) * s * (x0 / xi);
         const double v = x0 + xi;
         const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         d.gLd[gd->off + i] = L;

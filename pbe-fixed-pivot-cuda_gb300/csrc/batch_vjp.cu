@@ -127,7 +127,7 @@ __device__ void batch_vjp_task(const BatchDev& d, const BatchVjpDev& vd, const d
     v.lam = lam + cd.off;
     v.D = vd.D + cd.off;
     v.a = d.ga + gd.off; v.ia = d.gia + gd.off;
-    v.Bf = d.gBd + gd.off; v.Sf = d.gSd + gd.off; v.Ld = d.gLd + gd.off;
+    v.Bf = d.gBd + gd.off; v.Sf = d.gSd + gd.off; v.Sl = d.gSl + gd.off; v.Ld = d.gLd + gd.off;
     v.lag0_scale = 2.0;
     v.n = n;
     v.geo = gd.geo != 0;

@@ -277,6 +277,7 @@ struct VjpWs {
     double* D;         // [n]  (lambda_{i+1} - lambda_i) / (x_{i+1} - x_i)
     double* Bf;        // [n]  Brownian factor of lag d (rho + 1/rho + 2), no beta, no 1/2
     double* Sf;        // [n]  shear factor of lag d (1 + rho)^3 (times x of the smaller member)
+    double* Sl;        // [n]  the same times x_0 / x_d: times x of the larger member
     int*    Ld;        // [n]  bracket offset of lag d (as AggWs)
     double* mom_part;  // [nb_prep * 16] moments of N and lambda*N, max deviation
     double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
@@ -299,6 +300,7 @@ inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
     w.D        = reinterpret_cast<double*>(take(dn));
     w.Bf       = reinterpret_cast<double*>(take(dn));
     w.Sf       = reinterpret_cast<double*>(take(dn));
+    w.Sl       = reinterpret_cast<double*>(take(dn));
     w.Ld       = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(n)));
     w.mom_part = reinterpret_cast<double*>(take(sizeof(double) * 16 * static_cast<size_t>(agg_prep_blocks(n))));
     w.mom      = reinterpret_cast<double*>(take(sizeof(double) * 16));

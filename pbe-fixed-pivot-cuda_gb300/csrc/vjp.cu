@@ -39,8 +39,10 @@ constexpr int VW = kVW;                 // rows per task
 //   K=1: R0 = sum P N_k, R1 = sum P h_k       f N_k = x_m N_k + h_k
 //   K=2: R0 = sum P h_k                       f N_k = x_m h_k
 //   K=3: R0 = sum P N_k Bf                    Brownian factor per lag
-//   K=4: R1 = sum_upper P N_k Sf, R2 = sum_lower P h_k Sf   (shear f = x_min Sf)
-//   K=5: R0, R1, R2 as K=3 and K=4
+//   K=4: R1 = sum_upper P N_k Sf + sum_lower P N_k Sl (shear f = x_min Sf;
+//        on a geometric grid x_min = x_k = x_m x_0/x_d for a lower partner, so
+//        f = x_m Sl with Sl = Sf x_0/x_d and both visits sum into R1, times x_m)
+//   K=5: R0, R1 as K=3 and K=4
 // The generic (non-geometric) path accumulates sum P N_k f directly: R0 for
 // K=0..3 (f = f_0 or Bf), R1 for the shear part.
 
@@ -84,6 +86,7 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
         ws.Bf[i] = rho + 1.0 / rho + 2.0;
         const double s = 1.0 + rho;
         ws.Sf[i] = (s * s) * s;
+        ws.Sl[i] = (s * s) * s * (x0 / xi);
         const double v = x0 + xi;
         ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         if (n >= 2) {
@@ -147,7 +150,7 @@ vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     const int tid = threadIdx.x;
     VjpCellView v;
     v.x = x; v.N = N; v.h = ws.h; v.lam = lam; v.D = ws.D; v.a = ws.a; v.ia = ws.ia;
-    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Ld = ws.Ld; v.lag0_scale = 1.0;
+    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Sl = ws.Sl; v.Ld = ws.Ld; v.lag0_scale = 1.0;
     v.n = n;
     v.geo = ws.mom[10] != 0.0;
     const TileGroup G{0, tid, kMainThreads};
@@ -187,7 +190,7 @@ vjp_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     __syncwarp();
     VjpCellView v;
     v.x = x; v.N = N; v.h = ws.h; v.lam = lam; v.D = ws.D; v.a = ws.a; v.ia = ws.ia;
-    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Ld = ws.Ld; v.lag0_scale = 1.0;
+    v.Bf = ws.Bf; v.Sf = ws.Sf; v.Sl = ws.Sl; v.Ld = ws.Ld; v.lag0_scale = 1.0;
     v.n = n;
     v.geo = ws.mom[10] != 0.0;
     const int I = tile * VW;

@@ -40,6 +40,7 @@ struct VjpCellView {
     const double* ia;      // x^(-1/3)
     const double* Bf;      // Brownian lag factor (rho + 1/rho + 2) ...
     const double* Sf;      // shear lag factor (1 + rho)^3 ...
+    const double* Sl;      // ... the same times x_0 / x_d (lower partners: f = x_m Sl)
     const int*    Ld;      // bracket offset of lag d
     double lag0_scale;     // ... times lag0_scale at d = 0 (tables that carry the pair 1/2 use 2)
     int n;
@@ -120,7 +121,7 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
             // is clipped (L = kLagClipAll) gives lo >= n - 1 -> P = lambda_{n-1}
             if (d == 0) continue;
             const int L = __ldg(v.Ld + d);
-            const double Bf = __ldg(v.Bf + d), Sf = __ldg(v.Sf + d);
+            const double Bf = __ldg(v.Bf + d), Sl = __ldg(v.Sl + d);
             const int e = L - d;
 #pragma unroll
             for (int t = 0; t < VW; ++t) {
@@ -141,8 +142,11 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
                         const double Nk = __ldg(N + k);
                         if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
                         if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(h + k), R1[t]); }
-                        if constexpr (K == 3 || K == 5) R0[t] = fma(P * Nk, Bf, R0[t]);
-                        if constexpr (K == 4 || K == 5) R2[t] = fma(P * __ldg(h + k), Sf, R2[t]);
+                        if constexpr (K >= 3) {
+                            const double t1 = P * Nk;
+                            if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
+                            if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sl, R1[t]);
+                        }
                     }
                 }
             }
@@ -233,7 +237,7 @@ __device__ __forceinline__ void vjp_tile_row(const VjpCellView& v, int m, int t,
     if constexpr (K == 3 || K == 5)
         AX0 = fin[t] - fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
     if constexpr (K == 4 || K == 5) {
-        const double Tv = v.geo ? fma(xm, fin[VW + t], fin[2 * VW + t]) : fin[VW + t];
+        const double Tv = v.geo ? xm * fin[VW + t] : fin[VW + t];
         AX1 = Tv - fma(lm, moment_factor<K, 1>(xm, am, iam, M), moment_factor<K, 1>(xm, am, iam, Lm));
     }
     if constexpr (K <= 2) g = b0 * AX0;
