@@ -282,7 +282,7 @@ struct VjpWs {
     double* mom_part;  // [nb_prep * 16] moments of N and lambda*N, max deviation
     double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
     double* gpart;     // [max(ntile, nb_brk) * 4] per-task parameter partials
-    double* vpart;     // [ntile * kVjpMaxChunks * 3 kTileW] row sums per (tile, partner chunk)
+    double* vpart;     // [ntile * kVjpMaxChunks * 2 kTileW] row sums per (tile, partner chunk)
     int*    counter;   // [8]
 };
 
@@ -305,7 +305,7 @@ inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
     w.mom_part = reinterpret_cast<double*>(take(sizeof(double) * 16 * static_cast<size_t>(agg_prep_blocks(n))));
     w.mom      = reinterpret_cast<double*>(take(sizeof(double) * 16));
     w.gpart    = reinterpret_cast<double*>(take(sizeof(double) * 4 * static_cast<size_t>(ntile > nbb ? ntile : nbb)));
-    w.vpart    = reinterpret_cast<double*>(take(sizeof(double) * 3 * kTileW * kVjpMaxChunks *
+    w.vpart    = reinterpret_cast<double*>(take(sizeof(double) * 2 * kTileW * kVjpMaxChunks *
                                                 static_cast<size_t>(ntile)));
     w.counter  = reinterpret_cast<int*>(take(sizeof(int) * 8));
     if (ws) *ws = w;

@@ -34,7 +34,7 @@ namespace {
 
 constexpr int VW = kVW;                 // rows per task
 
-// dL/dN needs, per kernel type K, up to three row sums (see vjp_main_kernel):
+// dL/dN needs, per kernel type K, up to two row sums (see vjp_main_kernel):
 //   K=0: R0 = sum P N_k                       f = 1
 //   K=1: R0 = sum P N_k, R1 = sum P h_k       f N_k = x_m N_k + h_k
 //   K=2: R0 = sum P h_k                       f N_k = x_m h_k
@@ -136,7 +136,7 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
 }
 
 // Pair sums: task = (row tile, partner chunk); the whole CTA is one group.
-// Each task stores its rows' three sums per chunk; vjp_rows_kernel adds the
+// Each task stores its rows' two sums per chunk; vjp_rows_kernel adds the
 // chunks in order and finishes the rows.
 template <int K>
 __global__ void __launch_bounds__(kMainThreads, 2)

@@ -3,7 +3,7 @@
 // single-instance kernel (vjp.cu) and the batched-cell kernel (batch_vjp.cu).
 //
 // A task owns the VW = kTileW rows [I, I + VW) of one cell and accumulates,
-// per row m, up to three partner sums of P (the lambda interpolated at the
+// per row m, up to two partner sums of P (the lambda interpolated at the
 // pair's birth volume) times N_k (or x_k N_k) times the lag factor (see
 // vjp.cu for the derivation). It runs on a group of T threads (runtime
 // value, named barrier, like agg_tile.cuh); the T partials of every row are
@@ -16,7 +16,7 @@
 namespace pbe_gb300 {
 
 constexpr int kVW = kTileW;              // rows per task
-constexpr int kVRows = 3 * kVW;          // three accumulators per row
+constexpr int kVRows = 2 * kVW;          // two accumulators per row
 
 // sum_k f(m,k) N_k (or lambda_k N_k) from the moments mo[0..4].
 template <int K, int X>   // X: 0 = beta0 / Brownian part, 1 = shear part
@@ -51,7 +51,7 @@ constexpr int kVMaxGroups = kMainThreads / 32;
 
 struct VjpShared {
     double part[kVMaxGroups][kVRows];     // 32-column chunk partials (chunk g*T/32 + c)
-    double fin[kVMaxGroups][kVRows];      // R0[0..VW), R1[0..VW), R2[0..VW) of the task
+    double fin[kVMaxGroups][kVRows];      // R0[0..VW), R1[0..VW) of the task
     double gsh[kVMaxGroups][kVW][2];      // per-row parameter partials
     double cinfo[kVMaxGroups][16];        // per-task cell values (batched)
 };
@@ -77,9 +77,9 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
     const double* __restrict__ lam = v.lam;
     const double* __restrict__ D = v.D;
 
-    double R0[VW], R1[VW], R2[VW];
+    double R0[VW], R1[VW];
 #pragma unroll
-    for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; R2[t] = 0.0; }
+    for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; }
 
     if (v.geo) {
         // two passes over the lags (upper visits, then lower visits), so each
@@ -191,7 +191,6 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
     for (int t = 0; t < VW; ++t) {
         red[t * RS + lane] = R0[t];
         red[(VW + t) * RS + lane] = R1[t];
-        red[(2 * VW + t) * RS + lane] = R2[t];
     }
     G.sync();
     // fixed-order reduction: 32-column chunks (bank-rotated), then the chunks
