@@ -135,26 +135,29 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     // counters of the main kernel. No block waits for another.
     __threadfence();
     const int nb = gridDim.x;
-    // warps 0-4: one moment each; warp 5: largest deviation; warp 6: smallest
-    // D0 candidate (lanes stride over the blocks, fixed butterflies)
+    // seven reductions over the blocks' partials, spread over the warps: r < 5
+    // one moment each, r = 5 the largest deviation, r = 6 the smallest D0
+    // candidate (lanes stride over the blocks, fixed butterflies)
     const int wq = threadIdx.x >> 5, lq = threadIdx.x & 31;
-    if (wq < 5) {
-        double t = 0.0;
-        for (int b = lq; b < nb; b += 32) t += __ldcg(ws.mom_part + b * 8 + wq);
-        t = warp_sum(t);
-        if (lq == 0) ws.mom[wq] = t;
-    } else if (wq == 5) {
-        double m5 = 0.0;
-        for (int b = lq; b < nb; b += 32) m5 = fmax(m5, __ldcg(ws.mom_part + b * 8 + 5));
-        m5 = warp_max(m5);
-        if (lq == 0) sh[0] = m5;
-    } else if (wq == 6) {
-        int dmin = n;
-        for (int b = lq; b < nb; b += 32)
-            dmin = min(dmin, static_cast<int>(__ldcg(ws.mom_part + b * 8 + 6)));
+    for (int r = wq; r < 7; r += kPrepThreads / 32) {
+        if (r < 5) {
+            double t = 0.0;
+            for (int b = lq; b < nb; b += 32) t += __ldcg(ws.mom_part + b * 8 + r);
+            t = warp_sum(t);
+            if (lq == 0) ws.mom[r] = t;
+        } else if (r == 5) {
+            double m5 = 0.0;
+            for (int b = lq; b < nb; b += 32) m5 = fmax(m5, __ldcg(ws.mom_part + b * 8 + 5));
+            m5 = warp_max(m5);
+            if (lq == 0) sh[0] = m5;
+        } else {
+            int dmin = n;
+            for (int b = lq; b < nb; b += 32)
+                dmin = min(dmin, static_cast<int>(__ldcg(ws.mom_part + b * 8 + 6)));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) dmin = min(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
-        if (lq == 0) d0_s = dmin;
+            for (int o = 16; o > 0; o >>= 1) dmin = min(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+            if (lq == 0) d0_s = dmin;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -21,7 +21,8 @@ namespace pbe_gb300 {
 // ---- launch geometry --------------------------------------------------------
 constexpr int kTileW        = 12;    // output bins owned by one task (125 regs, no spill)
 constexpr int kMainThreads  = 256;   // threads per aggregation task CTA
-constexpr int kPrepThreads  = 256;
+constexpr int kPrepThreads  = 64;    // per-bin prep kernels: small blocks spread the
+                                     // cube roots and divisions over every SM
 constexpr int kMaxClipTasks = 32;    // tasks summing the pairs clipped at x[n-1]
 constexpr int kScatterChunk = 2048;  // lags per task in scatter mode
 constexpr int kRedRows      = 2 * (kTileW + 1);   // R[0..W], TH[0..W]
