@@ -282,7 +282,7 @@ struct VjpWs {
     int*    Ld;        // [n]  bracket offset of lag d (as AggWs)
     double* mom_part;  // [nb_prep * 16] moments of N and lambda*N, max deviation
     double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
-    double* gpart;     // [max(ntile, nb_brk) * 4] per-task parameter partials
+    double* gpart;     // [max(ntile, n / 8) * 4] per-task / per-block parameter partials
     double* vpart;     // [ntile * kVjpMaxChunks * 2 kTileW] row sums per (tile, partner chunk)
     int*    counter;   // [8]
 };
@@ -293,7 +293,7 @@ inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
     auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align256(bytes); return p; };
     const size_t dn = sizeof(double) * static_cast<size_t>(n);
     const int ntile = (n + kTileW - 1) / kTileW;
-    const int nbb = (n + 255) / 256;
+    const int nbb = (n + 7) / 8;          // breakage VJP blocks: 256 / 32 parents at least
     VjpWs w{};
     w.h        = reinterpret_cast<double*>(take(dn));
     w.a        = reinterpret_cast<double*>(take(dn));

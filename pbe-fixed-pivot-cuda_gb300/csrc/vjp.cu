@@ -110,27 +110,30 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     }
 }
 
+// One block: the eleven reductions over the prep blocks' partials, one per
+// warp and round (lanes stride over the blocks, fixed butterflies).
 __global__ void __launch_bounds__(256)
 vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
 {
-    __shared__ double sh[8];
+    __shared__ double mx_s;
     const int nb = (n + kPrepThreads - 1) / kPrepThreads;
-    for (int q = 0; q < 10; ++q) {
-        double s = 0.0;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ws.mom_part[b * 16 + q];
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) ws.mom[q] = s;
+    const int wq = threadIdx.x >> 5, lq = threadIdx.x & 31;
+    for (int r = wq; r < 11; r += 8) {
+        double t = 0.0;
+        if (r < 10) {
+            for (int b = lq; b < nb; b += 32) t += ws.mom_part[b * 16 + r];
+            t = warp_sum(t);
+            if (lq == 0) ws.mom[r] = t;
+        } else {
+            for (int b = lq; b < nb; b += 32) t = fmax(t, ws.mom_part[b * 16 + 10]);
+            t = warp_max(t);
+            if (lq == 0) mx_s = t;
+        }
     }
-    double mx = 0.0;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) mx = fmax(mx, ws.mom_part[b * 16 + 10]);
-    mx = warp_max(mx);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 0; w < 8; ++w) mx = fmax(mx, sh[w]);
         const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
-        ws.mom[10] = (n >= 2 && mx <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
+        ws.mom[10] = (n >= 2 && mx_s <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
         ws.counter[0] = 0;
     }
 }
@@ -214,36 +217,45 @@ vjp_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
 }
 
 // gp[0..2] += fixed-order sums of the per-tile partials
-__global__ void __launch_bounds__(256) vjp_gfin_kernel(int ntile, VjpWs ws, double* gp, int nslots)
+// One block: parameter slot q (< nslots <= 4) summed by warp q over the
+// tasks' partials in a fixed order.
+__global__ void __launch_bounds__(128) vjp_gfin_kernel(int ntile, VjpWs ws, double* gp, int nslots)
 {
-    __shared__ double sh[8];
-    for (int q = 0; q < nslots; ++q) {
-        double s = 0.0;
-        for (int b = threadIdx.x; b < ntile; b += blockDim.x) s += ws.gpart[b * 4 + q];
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) gp[q] += s;
-    }
+    const int q = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (q >= nslots) return;
+    double s = 0.0;
+    for (int b = l; b < ntile; b += 32) s += ws.gpart[b * 4 + q];
+    s = warp_sum(s);
+    if (l == 0) gp[q] += s;
 }
 
 // -------------------------------------------------------------------------
-// breakage VJP: one thread per parent j; block partials of the parameter sums
+// breakage VJP: nqp lanes per parent j (nqp = n_quad rounded up to a power of
+// two, <= 32), each lane the fragments q = l % nqp, + nqp, ... (their bracket
+// searches run side by side), summed over the lanes by a fixed butterfly;
+// block partials of the parameter sums.
 // -------------------------------------------------------------------------
 template <int F>
 __global__ void __launch_bounds__(256)
 brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
                const double* __restrict__ t_q, const double* __restrict__ bw_q,
                const double* __restrict__ lam, double* __restrict__ gN, double* part, int n,
-               int nq, double S0, double v_ref, double alpha, double v_min)
+               int nq, int nqp, double S0, double v_ref, double alpha, double v_min)
 {
     __shared__ double sh[8];
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int l = threadIdx.x % nqp;
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) / nqp;
     double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    double S = 0.0, Nj = 0.0, xj = 1.0;
+    bool on = false;
+    double acc = 0.0;
     if (j < n) {
-        const double xj = x[j], Nj = N[j];
-        const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
-        if ((S != 0.0) && (Nj > kBreakageNMin)) {
-            double Q = -lam[j];
-            for (int q = 0; q < nq; ++q) {
+        xj = x[j];
+        Nj = N[j];
+        S = selection<F>(xj, S0, v_ref, alpha, v_min);
+        on = (S != 0.0) && (Nj > kBreakageNMin);
+        if (on) {
+            for (int q = l; q < nq; q += nqp) {
                 const double v = xj * t_q[q];
                 const int lo = frag_bracket(x, n, v);
                 double P;
@@ -254,16 +266,20 @@ brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
                     const double eta = (v - xl) / (xh - xl);
                     P = fma(1.0 - eta, lam[lo], eta * lam[lo + 1]);
                 }
-                Q = fma(bw_q[q], P, Q);
+                acc = fma(bw_q[q], P, acc);
             }
-            gN[j] += S * Q;
-            const double NQ = Nj * Q;
-            p0 = (S / S0) * NQ;
-            if constexpr (F == 1) p1 = -(S / v_ref) * NQ;
-            if constexpr (F == 2) {
-                p1 = -(alpha * S / v_ref) * NQ;
-                p2 = S * log(xj / v_ref) * NQ;
-            }
+        }
+    }
+    for (int o = nqp >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (on && l == 0) {
+        const double Q = acc - lam[j];
+        gN[j] += S * Q;
+        const double NQ = Nj * Q;
+        p0 = (S / S0) * NQ;
+        if constexpr (F == 1) p1 = -(S / v_ref) * NQ;
+        if constexpr (F == 2) {
+            p1 = -(alpha * S / v_ref) * NQ;
+            p2 = S * log(xj / v_ref) * NQ;
         }
     }
     const double s0 = block_sum(p0, sh);
@@ -313,17 +329,19 @@ cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStr
     vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, ws, n, ntile, nch);
     vjp_rows_kernel<K><<<(ntile + 7) / 8, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, nch,
                                                        a.beta0, a.beta_br, a.beta_sh);
-    vjp_gfin_kernel<<<1, 256, 0, s>>>(ntile, ws, a.gp, 3);
+    vjp_gfin_kernel<<<1, 128, 0, s>>>(ntile, ws, a.gp, 3);
     return cudaGetLastError();
 }
 
 template <int F>
 cudaError_t brk_vjp_f(const BrkVjpArgs& a, const VjpWs& ws, cudaStream_t s)
 {
-    const int nb = (a.n + 255) / 256;
+    int nqp = 1;
+    while (nqp < a.n_quad && nqp < 32) nqp <<= 1;
+    const int nb = static_cast<int>((static_cast<long long>(a.n) * nqp + 255) / 256);
     brk_vjp_kernel<F><<<nb, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.lam, a.gN, ws.gpart, a.n,
-                                         a.n_quad, a.S0, a.v_ref, a.alpha, a.v_min);
-    vjp_gfin_kernel<<<1, 256, 0, s>>>(nb, ws, a.gp, 4);
+                                         a.n_quad, nqp, a.S0, a.v_ref, a.alpha, a.v_min);
+    vjp_gfin_kernel<<<1, 128, 0, s>>>(nb, ws, a.gp, 4);
     return cudaGetLastError();
 }
 
