@@ -724,8 +724,8 @@ def main():
         rhs.zero_()
         pg.check(pg.aggregation_rhs(n_dev, dx, rhs, ap, stream=stream, mode=mode), "aggregation")
         pg.check(pg.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream=stream, mode=mode), "breakage")
-    # aggregation: prep, clip, pair kernel; breakage: prep + gather (gather
-    # mode) or one scatter kernel
+    # aggregation: counter reset (memset), prep, pair kernel; breakage: prep +
+    # gather (gather mode) or one scatter kernel
     launches_per_step = 3 + (2 if mode == pg.MODE_GATHER else 1)
 
     clocks = ClockSampler(local)

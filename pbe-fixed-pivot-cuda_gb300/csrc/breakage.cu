@@ -70,7 +70,7 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (live) {
         // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
         int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-        const int lo_prev = (j == 0) ? -2 : (lane > 0 ? lo_left : frag_bracket(x, n, x[j - 1] * tq));
+        const int lo_prev = (j == 0) ? -2 : (lane > 0 ? lo_left : frag_bracket_below(x, n, x[j - 1] * tq, lo));
         for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
         if (j == n - 1)
             for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;

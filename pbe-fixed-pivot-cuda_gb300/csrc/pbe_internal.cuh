@@ -152,6 +152,24 @@ __device__ __forceinline__ int bracket_from(const double* __restrict__ x, int n,
     return lo;
 }
 
+// Same bracket, for a v known to satisfy x[0] < v < x[start+1]: gallops down
+// from start (1, 2, 4, ... pivots), then bisects the last step.
+__device__ __forceinline__ int bracket_down(const double* __restrict__ x, double v, int start)
+{
+    const long long vb = dbits(v);
+    int hi = start + 1, step = 1;            // x[hi] > v
+    while (hi - step > 0 && dbits(__ldg(x + hi - step)) > vb) {
+        hi -= step;
+        step <<= 1;
+    }
+    int lo = hi - step > 0 ? hi - step : 0;  // x[lo] <= v
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (dbits(__ldg(x + mid)) <= vb) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 // Selection function S(v) (reference src/breakage_kernels.cuh:51-65).
 template <int F>
 __device__ __forceinline__ double selection(double v, double S0, double v_ref, double alpha,
@@ -170,6 +188,15 @@ __device__ __forceinline__ int frag_bracket(const double* __restrict__ x, int n,
     if (dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
     if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
     return bracket_lo(x, n, v);
+}
+
+// frag_bracket of a v at or below a volume whose frag_bracket is `above`.
+__device__ __forceinline__ int frag_bracket_below(const double* __restrict__ x, int n, double v,
+                                                  int above)
+{
+    if (above < 0 || dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
+    if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
+    return bracket_down(x, v, above < n - 2 ? above : n - 2);
 }
 
 // ---- aggregation scratch ----------------------------------------------------
