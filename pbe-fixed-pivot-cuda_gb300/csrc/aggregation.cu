@@ -103,7 +103,7 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
         ws.Ld[i] = L;
         if (L == i) d0 = i;
-        if (i < agg_tiles(n)) ws.tticket[i] = 0;
+        if (i < agg_tiles(n)) { ws.tticket[i] = 0; ws.cticket[i] = 0; }
         if (n >= 2) {
             dev = geo_dev(fit_s, xi, i);
             if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
@@ -254,11 +254,12 @@ template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile, int nchunk,
-                int ntasks, int nclip, double b0, double bbr, double bsh, int T)
+                int ntasks, int nclip, double b0, double bbr, double bsh, int T, int Cg)
 {
     extern __shared__ double red[];               // [2 W][kMainThreads]
     __shared__ TileShared sm;
     __shared__ int s_task[kMaxGroups];
+    __shared__ int s_last[kMaxGroups];
 
     const int tid = threadIdx.x;
     AggCellView v;
@@ -301,13 +302,34 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         task -= nclip;
 
         int tile, chunk = 0;     // tile 0 is the top one (largest first)
-        if (SCATTER && v.geo) { tile = task / nchunk; chunk = task % nchunk; }
-        else { if (task >= ntile) continue; tile = task; }
+        int nct = 1;             // gather: lag chunks of this tile
+        if constexpr (SCATTER) {
+            if (v.geo) { tile = task / nchunk; chunk = task % nchunk; }
+            else { if (task >= ntile) continue; tile = task; }
+        } else {
+            // chunk-major: chunk c of every tile that reaches lag c Cg (tile t
+            // spans the lags below n - W t), tiles top first within a chunk
+            int c = 0;
+            for (;;) {
+                const int cnt = (c * Cg < n) ? min(ntile, (n - c * Cg + W - 1) / W) : 0;
+                if (cnt == 0 || task < cnt) break;
+                task -= cnt;
+                ++c;
+            }
+            tile = task;
+            chunk = c;
+            if (tile >= ntile) continue;
+            // generic grids walk rows, not lags: one task per tile there
+            nct = v.geo ? (n - W * tile + Cg - 1) / Cg : 1;
+            if (chunk >= nct) continue;
+        }
 
         const int I = n - W * (tile + 1);
         const int smax = min(I + W - 1, n - 2);
-        const int d_begin = (SCATTER && v.geo) ? chunk * kScatterChunk : 0;
-        const int d_end = (SCATTER && v.geo) ? min(n, d_begin + kScatterChunk) : n;
+        const int csize = SCATTER ? kScatterChunk : Cg;
+        const bool chunked = SCATTER ? v.geo : nct > 1;
+        const int d_begin = chunked ? chunk * csize : 0;
+        const int d_end = chunked ? min(n, d_begin + csize) : n;
         // skip empty lag chunks (uniform: every thread reads the same entry)
         if (SCATTER && v.geo && chunk > 0 && (d_begin >= n || ws.Ld[d_begin] > smax)) continue;
 
@@ -316,6 +338,28 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         // the reference's w*rate even on grids spanning hundreds of octaves.
         const int St = -ilogb(x[max(I, 0)]);
         agg_tile_accumulate<K, true>(v, I, d_begin, d_end, St, red + g * T, sm, G);
+
+        if (!SCATTER && nct > 1) {
+            // store this chunk's slot sums; the tile's last chunk task adds all
+            // of them in chunk order and runs the epilogue (nobody waits)
+            constexpr int R2 = TileSlots<true>::rows;
+            double* cp = ws.cpart + static_cast<size_t>(tile) * agg_chunk_bound(n) * R2;
+            if (lane < R2) cp[chunk * R2 + lane] = sm.fin[g][lane];
+            G.sync();
+            if (lane == 0) {
+                __threadfence();
+                s_last[g] = (atomicAdd(ws.cticket + tile, 1) == nct - 1);
+            }
+            G.sync();
+            if (!s_last[g]) continue;
+            __threadfence();
+            if (lane < R2) {
+                double acc = 0.0;
+                for (int c = 0; c < nct; ++c) acc += __ldcg(cp + c * R2 + lane);
+                sm.fin[g][lane] = acc;
+            }
+            G.sync();
+        }
 
         if (lane < W) {
             const int i = I + lane;
@@ -366,6 +410,18 @@ int agg_group_size(long long ntasks, int num_sms)
     return 256;
 }
 
+// Group size of chunked gather launches (PBE_GB300_AGG_GROUP overrides as for
+// agg_group_size): 32.
+int agg_group_size_chunked()
+{
+    static const int forced = []() {
+        const char* e = std::getenv("PBE_GB300_AGG_GROUP");
+        const int v = e ? std::atoi(e) : 0;
+        return (v == 32 || v == 64 || v == 128 || v == 256) ? v : 0;
+    }();
+    return forced ? forced : 32;
+}
+
 // Tasks that sum the clipped pairs (about n + q^2 pairs on a grid with q bins
 // per octave, more on generic grids), spread over parts of ~1024 lags or rows.
 int agg_clip_tasks(int n)
@@ -382,10 +438,36 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const int ntile = (n + W - 1) / W;
     const int nchunk = SC ? (n + kScatterChunk - 1) / kScatterChunk : 1;
     const int nclip = agg_clip_tasks(n);
-    const long long ntasks_ll = static_cast<long long>(ntile) * nchunk + nclip;
+    // gather: cut the tiles' lags into chunks when the tiles alone leave the
+    // CTA slots with fewer than 4 tasks each (their costs fall linearly from
+    // the top tile down, so the largest would set the kernel's time)
+    int Cg = n;
+    long long ngather = ntile;
+    if (!SC && n >= 2 && ntile < 4 * 2 * num_sms) {
+        const long long lags = static_cast<long long>(ntile) * n -
+                               static_cast<long long>(W) * ntile * (ntile - 1) / 2;
+        const long long target = static_cast<long long>(kChunkTasks) * 2 *
+                                 (num_sms < kChunkMaxSms ? num_sms : kChunkMaxSms);
+        long long cg = (lags + target - 1) / target;
+        cg = ((cg + 31) / 32) * 32;
+        if (cg < kChunkMinLags) cg = kChunkMinLags;
+        const long long floor_bound = (n + agg_chunk_bound(n) - 1) / agg_chunk_bound(n);
+        if (cg < floor_bound) cg = floor_bound;
+        if (cg < n) {
+            Cg = static_cast<int>(cg);
+            ngather = 0;
+            for (int c = 0; static_cast<long long>(c) * Cg < n; ++c) {
+                const int cnt = (n - c * Cg + W - 1) / W;
+                ngather += cnt < ntile ? cnt : ntile;
+            }
+        }
+    }
+    const long long ntasks_ll = (SC ? static_cast<long long>(ntile) * nchunk : ngather) + nclip;
     if (ntasks_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int ntasks = static_cast<int>(ntasks_ll);
-    const int T = agg_group_size(ntasks, num_sms);
+    // chunked gather: many tasks of few lags; single warps keep the fixed-order
+    // reduction (2 W T adds per task) small next to a chunk's pairs
+    const int T = (!SC && Cg < n) ? agg_group_size_chunked() : agg_group_size(ntasks, num_sms);
     const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
     const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
     const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
@@ -400,7 +482,7 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     if (prof) cudaEventRecord(g_prof_start, s);
     agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, nchunk,
                                                             ntasks, nclip, a.beta0, a.beta_br,
-                                                            a.beta_sh, T);
+                                                            a.beta_sh, T, Cg);
     if (prof) cudaEventRecord(g_prof_stop, s);
     return cudaGetLastError();
 }

@@ -219,12 +219,29 @@ struct AggWs {
     double* tfirst;    // [ntile] gather mode: tile's own value of its first bin
     double* tcarry;    // [ntile] gather mode: the lower neighbour's carry into that bin
     int*    tticket;   // [ntile] contributors to the tile's first bin done (0, 1, 2)
+    double* cpart;     // [ntile * agg_chunk_bound(n) * 2 kTileW] lag-chunk partials of R, TH
+    int*    cticket;   // [ntile] lag-chunk tasks of the tile done
     int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d,
                        //      [2] prep blocks done, [3] bin n-1 contributors done
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
 __host__ __device__ constexpr int agg_tiles(int n) { return (n + kTileW - 1) / kTileW; }
+
+// Gather mode with few tiles per CTA slot (small n): each tile's lags are cut
+// into chunks of at least kChunkMinLags lags, about kChunkTasks tasks per CTA
+// slot in all, on GPUs of up to kChunkMaxSms SMs; agg_chunk_bound(n) chunks per
+// tile at most (the scratch is sized for it whatever the GPU).
+constexpr int kChunkTasks = 8;
+constexpr int kChunkMaxSms = 256;
+constexpr int kChunkMinLags = 256;
+__host__ __device__ constexpr int agg_chunk_bound(int n)
+{
+    const int a = (n + kChunkMinLags - 1) / kChunkMinLags;
+    const int b = n > 0 ? (2 * kTileW * kChunkTasks * 2 * kChunkMaxSms + n - 1) / n + 1 : 1;
+    const int m = a < b ? a : b;
+    return m < 1 ? 1 : m;
+}
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -238,6 +255,9 @@ constexpr size_t agg_ws_bytes(int n)
          + align256(sizeof(double) * 8)
          + align256(sizeof(double) * kMaxClipTasks)
          + 2 * align256(sizeof(double) * static_cast<size_t>(agg_tiles(n)))
+         + align256(sizeof(int) * static_cast<size_t>(agg_tiles(n)))
+         + align256(sizeof(double) * 2 * kTileW * static_cast<size_t>(agg_tiles(n)) *
+                    static_cast<size_t>(agg_chunk_bound(n)))
          + align256(sizeof(int) * static_cast<size_t>(agg_tiles(n)))
          + align256(sizeof(int) * 8);
 }
@@ -263,6 +283,9 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.tfirst    = reinterpret_cast<double*>(take(sizeof(double) * nt));
     w.tcarry    = reinterpret_cast<double*>(take(sizeof(double) * nt));
     w.tticket   = reinterpret_cast<int*>(take(sizeof(int) * nt));
+    w.cpart     = reinterpret_cast<double*>(take(sizeof(double) * 2 * kTileW * nt *
+                                                 static_cast<size_t>(agg_chunk_bound(n))));
+    w.cticket   = reinterpret_cast<int*>(take(sizeof(int) * nt));
     w.counter   = reinterpret_cast<int*>(take(sizeof(int) * 8));
     if (ws) *ws = w;
     return off;
