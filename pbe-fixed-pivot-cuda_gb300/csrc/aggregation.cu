@@ -33,10 +33,10 @@
 //
 // Kernels per call: prep (per-bin values, lag tables, moment partials,
 // geometric check; its last block finishes moments, flag and counters) ->
-// main (persistent CTAs pulling target tiles from an atomic counter, largest
-// first). GATHER mode: one CTA owns each output bin and reduces it in a fixed
-// order -> bitwise reproducible. SCATTER mode: geometric tasks are (tile, lag
-// chunk) and flush with FP64 atomicAdd.
+// main (persistent CTAs pulling target tiles, or for small n their lag
+// chunks, from an atomic counter, largest first). GATHER mode: each output
+// bin is written once, from sums reduced in a fixed order -> bitwise
+// reproducible. SCATTER mode: every task flushes its bins with FP64 atomicAdd.
 // =============================================================================
 #include <cstdlib>
 
@@ -253,7 +253,7 @@ __device__ __forceinline__ void first_bin_done(double* rhs, int I, const AggWs& 
 template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
-                double* __restrict__ rhs, AggWs ws, int n, int ntile, int nchunk,
+                double* __restrict__ rhs, AggWs ws, int n, int ntile,
                 int ntasks, int nclip, double b0, double bbr, double bsh, int T, int Cg)
 {
     extern __shared__ double red[];               // [2 W][kMainThreads]
@@ -301,37 +301,28 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
         }
         task -= nclip;
 
-        int tile, chunk = 0;     // tile 0 is the top one (largest first)
-        int nct = 1;             // gather: lag chunks of this tile
-        if constexpr (SCATTER) {
-            if (v.geo) { tile = task / nchunk; chunk = task % nchunk; }
-            else { if (task >= ntile) continue; tile = task; }
-        } else {
-            // chunk-major: chunk c of every tile that reaches lag c Cg (tile t
-            // spans the lags below n - W t), tiles top first within a chunk
-            int c = 0;
-            for (;;) {
-                const int cnt = (c * Cg < n) ? min(ntile, (n - c * Cg + W - 1) / W) : 0;
-                if (cnt == 0 || task < cnt) break;
-                task -= cnt;
-                ++c;
-            }
-            tile = task;
-            chunk = c;
-            if (tile >= ntile) continue;
-            // generic grids walk rows, not lags: one task per tile there
-            nct = v.geo ? (n - W * tile + Cg - 1) / Cg : 1;
-            if (chunk >= nct) continue;
+        // chunk-major: chunk c of every tile that reaches lag c Cg (tile t
+        // spans the lags below n - W t), tiles top first within a chunk
+        // (Cg = n: one task per tile)
+        int c = 0;
+        for (;;) {
+            const int cnt = (c * Cg < n) ? min(ntile, (n - c * Cg + W - 1) / W) : 0;
+            if (cnt == 0 || task < cnt) break;
+            task -= cnt;
+            ++c;
         }
+        const int tile = task, chunk = c;      // tile 0 is the top one (largest first)
+        if (tile >= ntile) continue;
+        // generic grids walk rows, not lags: one task per tile there
+        const int nct = v.geo ? (n - W * tile + Cg - 1) / Cg : 1;
+        if (chunk >= nct) continue;
 
         const int I = n - W * (tile + 1);
         const int smax = min(I + W - 1, n - 2);
-        const int csize = SCATTER ? kScatterChunk : Cg;
-        const bool chunked = SCATTER ? v.geo : nct > 1;
-        const int d_begin = chunked ? chunk * csize : 0;
-        const int d_end = chunked ? min(n, d_begin + csize) : n;
-        // skip empty lag chunks (uniform: every thread reads the same entry)
-        if (SCATTER && v.geo && chunk > 0 && (d_begin >= n || ws.Ld[d_begin] > smax)) continue;
+        const int d_begin = nct > 1 ? chunk * Cg : 0;
+        const int d_end = nct > 1 ? min(n, d_begin + Cg) : n;
+        // scatter: skip empty lag chunks (uniform: every thread reads the same entry)
+        if (SCATTER && chunk > 0 && ws.Ld[d_begin] > smax) continue;
 
         // Per-task exponent shift of the weight numerators: th ~ x_I (r-1) is
         // carried as th 2^St ~ (r-1), so sum rate*th keeps the dynamic range of
@@ -365,7 +356,7 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
             const int i = I + lane;
             if (i >= 0) {
                 const double birth = agg_tile_birth<true>(v, I, lane, St, sm.fin[g]);
-                const bool first = !(SCATTER && v.geo) || chunk == 0;
+                const bool first = !SCATTER || chunk == 0;
                 const double death = first ? agg_death<K>(v, i) : 0.0;
                 const double val = birth - death;
                 if constexpr (SCATTER) {
@@ -436,14 +427,14 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const int n = a.n;
     const int nb = agg_prep_blocks(n);
     const int ntile = (n + W - 1) / W;
-    const int nchunk = SC ? (n + kScatterChunk - 1) / kScatterChunk : 1;
     const int nclip = agg_clip_tasks(n);
-    // gather: cut the tiles' lags into chunks when the tiles alone leave the
-    // CTA slots with fewer than 4 tasks each (their costs fall linearly from
-    // the top tile down, so the largest would set the kernel's time)
+    // cut the tiles' lags into chunks when the tiles alone leave the CTA slots
+    // with fewer than 4 tasks each (their costs fall linearly from the top
+    // tile down, so the largest would set the kernel's time). Gather adds a
+    // tile's chunk sums in order; scatter flushes each chunk with atomics.
     int Cg = n;
     long long ngather = ntile;
-    if (!SC && n >= 2 && ntile < 4 * 2 * num_sms) {
+    if (n >= 2 && ntile < 4 * 2 * num_sms) {
         const long long lags = static_cast<long long>(ntile) * n -
                                static_cast<long long>(W) * ntile * (ntile - 1) / 2;
         const long long target = static_cast<long long>(kChunkTasks) * 2 *
@@ -462,12 +453,12 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
             }
         }
     }
-    const long long ntasks_ll = (SC ? static_cast<long long>(ntile) * nchunk : ngather) + nclip;
+    const long long ntasks_ll = ngather + nclip;
     if (ntasks_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int ntasks = static_cast<int>(ntasks_ll);
     // chunked gather: many tasks of few lags; single warps keep the fixed-order
     // reduction (2 W T adds per task) small next to a chunk's pairs
-    const int T = (!SC && Cg < n) ? agg_group_size_chunked() : agg_group_size(ntasks, num_sms);
+    const int T = (Cg < n) ? agg_group_size_chunked() : agg_group_size(ntasks, num_sms);
     const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
     const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
     const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
@@ -480,7 +471,7 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
-    agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, nchunk,
+    agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile,
                                                             ntasks, nclip, a.beta0, a.beta_br,
                                                             a.beta_sh, T, Cg);
     if (prof) cudaEventRecord(g_prof_stop, s);

@@ -24,7 +24,6 @@ constexpr int kMainThreads  = 256;   // threads per aggregation task CTA
 constexpr int kPrepThreads  = 64;    // per-bin prep kernels: small blocks spread the
                                      // cube roots and divisions over every SM
 constexpr int kMaxClipTasks = 32;    // tasks summing the pairs clipped at x[n-1]
-constexpr int kScatterChunk = 2048;  // lags per task in scatter mode
 constexpr int kRedRows      = 2 * (kTileW + 1);   // R[0..W], TH[0..W]
 
 // A grid is treated as geometric when |log(x_i/x_0) - i*log(r)| <= kGeoTol for
