@@ -798,6 +798,25 @@ def main():
             b_.record(stream)
         torch.cuda.synchronize()
         vjp_ms = sum(a_.elapsed_time(b_) for a_, b_ in v_evs) / len(v_evs)
+
+        # ---- the other accumulation mode on the same step ------------------
+        other = pg.MODE_SCATTER if mode == pg.MODE_GATHER else pg.MODE_GATHER
+
+        def other_step():
+            rhs.zero_()
+            pg.check(pg.aggregation_rhs(dN, dx, rhs, ap, stream=stream, mode=other), "aggregation")
+            pg.check(pg.breakage_rhs(dN, dx, dt, db, rhs, bp, stream=stream, mode=other), "breakage")
+        for _ in range(3):
+            other_step()
+        o_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(max(args.steps // 4, 5))]
+        for a_, b_ in o_evs:
+            flush.zero_()
+            a_.record(stream)
+            other_step()
+            b_.record(stream)
+        torch.cuda.synchronize()
+        other_ms = sum(a_.elapsed_time(b_) for a_, b_ in o_evs) / len(o_evs)
         time.sleep(0.2)
         clk = clocks.stop()
 
@@ -841,6 +860,11 @@ def main():
         "clocks": clk,
     }
     if vjp_ms is not None:
+        out["other_mode"] = {"mode": "scatter" if other == pg.MODE_SCATTER else "gather",
+                             "evals_per_s": round(1e3 / other_ms, 3),
+                             "ms_per_step": round(other_ms, 5),
+                             "what": "the same step in the other accumulation mode, device-resident, "
+                                     "L2 flushed"}
         out["vjp"] = {"ms_per_eval": round(vjp_ms, 5),
                       "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
                       "what": "aggregation + breakage VJP (dL/dN and parameter gradients) of "
