@@ -140,6 +140,7 @@ struct TileShared {
     double wsum[kMaxGroups];              // per-warp partials of group sums
     double extra[kMaxGroups][kTileW];     // per-bin additions (batched breakage)
     double cinfo[kMaxGroups][8];          // per-task cell values for the epilogue (batched)
+    int last[kMaxGroups];                 // this group ran a tile's last lag chunk (batched)
 };
 
 // A group of T threads (T a multiple of 32, T <= kMainThreads) working on one

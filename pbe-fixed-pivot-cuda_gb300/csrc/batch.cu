@@ -45,7 +45,8 @@ struct pbe_batch_plan {
     std::vector<void*> allocs;
     int group_size[16] = {0};
     int4* d_bundles = nullptr;
-    int2* d_tasks = nullptr;
+    int4* d_tasks = nullptr;
+    std::vector<char> grid_geo;        // grids verified geometric (lag chunks apply)
     std::vector<double> t_q, bw_q;
     double* d_tq = nullptr;
     double* d_bw = nullptr;
@@ -145,7 +146,7 @@ void tune_cache_store_locked(const TuneKey& k, int t)
 }
 
 // ---- schedule ------------------------------------------------------------------
-struct HostTask { int cell, I; long long cost; };
+struct HostTask { int cell, I, chunk, nct; long long cost; };
 
 long long task_cost(int n, int I, int T)
 {
@@ -159,18 +160,29 @@ long long task_cost(int n, int I, int T)
 // vjp: row tiles of the VJP, whose work does not depend on the first row (every
 // row meets all n partners).
 void build_schedule(const pbe_batch_plan& p, const int* gs, const bool* want,
-                    std::vector<int4>& bundles, std::vector<int2>& tasks, bool vjp = false)
+                    std::vector<int4>& bundles, std::vector<int4>& tasks, bool vjp = false)
 {
     std::vector<std::vector<HostTask>> per(kClasses);
+    const int Cg = p.d.Cg;
     for (int c = 0; c < p.n_cells; ++c) {
         const int n = p.cell_n[c];
         const int cls = n_class(n);
         if (want && !want[cls]) continue;
         if (vjp) {
-            for (int I = 0; I < n; I += W) per[cls].push_back({c, I, task_cost(n, n, gs[cls])});
+            for (int I = 0; I < n; I += W) per[cls].push_back({c, I, 0, 1, task_cost(n, n, gs[cls])});
         } else {
-            // forward tiles aligned to the top: the lowest may start below bin 0
-            for (int I = n - W; I > -W; I -= W) per[cls].push_back({c, I, task_cost(n, I, gs[cls])});
+            // forward tiles aligned to the top: the lowest may start below bin 0;
+            // tile t spans the lags below n - W t, cut into chunks of Cg lags
+            // when the plan has few tiles (chunk_setup)
+            const bool chunks = Cg > 0 && p.grid_geo[p.cell_grid[c]];
+            for (int I = n - W; I > -W; I -= W) {
+                const int span = I + W;
+                const int nct = chunks ? (span + Cg - 1) / Cg : 1;
+                for (int k = 0; k < nct; ++k) {
+                    const int lags = nct > 1 ? std::min(Cg, span - k * Cg) : span;
+                    per[cls].push_back({c, I, k, nct, task_cost(n, lags - W, gs[cls])});
+                }
+            }
         }
     }
     struct B { long long cost; int cls; int first; int cnt; };
@@ -197,7 +209,7 @@ void build_schedule(const pbe_batch_plan& p, const int* gs, const bool* want,
         bundles.push_back(make_int4(static_cast<int>(tasks.size()), b.cnt, gs[b.cls], 0));
         for (int k = 0; k < b.cnt; ++k) {
             const HostTask& t = sorted[b.cls][b.first + k];
-            tasks.push_back(make_int2(t.cell, t.I));
+            tasks.push_back(make_int4(t.cell, t.I, t.chunk, t.nct));
         }
     }
 }
@@ -214,14 +226,14 @@ cudaError_t plan_alloc(pbe_batch_plan* p, T** out, size_t count)
 }
 
 cudaError_t upload_schedule(pbe_batch_plan* p, const std::vector<int4>& b,
-                            const std::vector<int2>& t, int4** db, int2** dt, cudaStream_t s)
+                            const std::vector<int4>& t, int4** db, int4** dt, cudaStream_t s)
 {
     cudaError_t e = plan_alloc(p, db, b.size());
     if (e == cudaSuccess) e = plan_alloc(p, dt, t.size());
     if (e == cudaSuccess && !b.empty())
         e = cudaMemcpyAsync(*db, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && !t.empty())
-        e = cudaMemcpyAsync(*dt, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, s);
+        e = cudaMemcpyAsync(*dt, t.data(), t.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return e;
 }
@@ -252,10 +264,10 @@ cudaError_t tune_class(pbe_batch_plan* p, int cls, const pbe_batch_cell_params_t
         int gs[kClasses];
         for (int c = 0; c < kClasses; ++c) gs[c] = cand[ci];
         std::vector<int4> b;
-        std::vector<int2> t;
+        std::vector<int4> t;
         build_schedule(*p, gs, want, b, t);
         int4* db = nullptr;
-        int2* dt = nullptr;
+        int4* dt = nullptr;
         e = upload_schedule(p, b, t, &db, &dt, s);
         if (e != cudaSuccess) break;
         const int nb = static_cast<int>(b.size());
@@ -303,7 +315,7 @@ cudaError_t autotune(pbe_batch_plan* p, bool retune, cudaStream_t s)
     }
     for (int cls = 0; cls < kClasses && e == cudaSuccess; ++cls) {
         if (!present[cls]) continue;
-        const TuneKey key(p->num_sms, p->kernel, p->nq > 0 ? 1 : 0, cls);
+        const TuneKey key(p->num_sms, p->kernel, (p->nq > 0 ? 1 : 0) | (p->d.Cg > 0 ? 2 : 0), cls);
         auto it = g_tune.find(key);
         if (!retune && it != g_tune.end()) { p->group_size[cls] = it->second; continue; }
         int T = rule_group_size(cls);
@@ -315,6 +327,51 @@ cudaError_t autotune(pbe_batch_plan* p, bool retune, cudaStream_t s)
     }
     free_last(p, 3);
     return e;
+}
+
+// Plans with few tiles (a handful of small cells) cut each tile of a cell on a
+// geometric grid into chunks of Cg lags, about kChunkTasks tasks per CTA slot
+// in all; the tile's last chunk task adds the chunk sums in chunk order and runs
+// the epilogue. Cg is fixed for the plan, so a tile has the same chunks in every
+// schedule built from it (tuning, class subsets, the Jacobian-vector pass).
+cudaError_t chunk_setup(pbe_batch_plan* p, long long tiles, cudaStream_t s)
+{
+    BatchDev& d = p->d;
+    d.Cg = 0;
+    d.cbound = 1;
+    std::vector<BatchGridDev> hg(static_cast<size_t>(p->n_grids));
+    cudaError_t e = cudaMemcpyAsync(hg.data(), d.grids, hg.size() * sizeof(BatchGridDev),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    p->grid_geo.assign(static_cast<size_t>(p->n_grids), 0);
+    for (int g = 0; g < p->n_grids; ++g) p->grid_geo[g] = hg[g].geo != 0;
+    if (p->kernel < 0 || tiles >= 4LL * 2 * p->num_sms) return cudaSuccess;
+    long long lags = 0;
+    int max_geo_n = 0;
+    for (int c = 0; c < p->n_cells; ++c) {
+        if (!p->grid_geo[p->cell_grid[c]]) continue;
+        const long long n = p->cell_n[c], nt = (n + W - 1) / W;
+        lags += nt * n - static_cast<long long>(W) * nt * (nt - 1) / 2;
+        max_geo_n = std::max(max_geo_n, p->cell_n[c]);
+    }
+    if (lags == 0) return cudaSuccess;
+    const long long target = static_cast<long long>(kChunkTasks) * 2 *
+                             std::min(p->num_sms, kChunkMaxSms);
+    long long cg = (lags + target - 1) / target;
+    cg = std::max<long long>(((cg + 31) / 32) * 32, kChunkMinLags);
+    if (cg >= max_geo_n) return cudaSuccess;
+    const int Cg = static_cast<int>(cg);
+    const int cbound = (max_geo_n + Cg - 1) / Cg;      // the top tile spans n lags
+    const size_t nt = static_cast<size_t>(tiles);
+    e = plan_alloc(p, &d.cpart, nt * static_cast<size_t>(cbound) * 2 * W);
+    if (e == cudaSuccess) e = plan_alloc(p, &d.cticket, nt);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.cticket, 0, nt * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    d.Cg = Cg;
+    d.cbound = cbound;
+    return cudaSuccess;
 }
 
 cudaError_t validate(int n_grids, const int* grid_n, const double* grid_x, int n_cells,
@@ -451,15 +508,19 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     if (e == cudaSuccess) e = batch_kernel_setup(kernel);
     if (e == cudaSuccess) e = batch_grid_tables(d, p->d_tq, p->d_bw, 0, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = chunk_setup(p, tiles, s);
     if (e != cudaSuccess) return e;
 
-    for (int cls = 0; cls < kClasses; ++cls) p->group_size[cls] = rule_group_size(cls);
+    // lag chunks: single-warp groups keep the fixed-order reduction (2 W T adds
+    // per task) small next to a chunk's pairs
+    for (int cls = 0; cls < kClasses; ++cls)
+        p->group_size[cls] = d.Cg > 0 ? 32 : rule_group_size(cls);
     if (flags & (PBE_BATCH_TUNE | PBE_BATCH_RETUNE)) {
         e = autotune(p, (flags & PBE_BATCH_RETUNE) != 0, s);
         if (e != cudaSuccess) return e;
     }
     std::vector<int4> b;
-    std::vector<int2> t;
+    std::vector<int4> t;
     build_schedule(*p, p->group_size, nullptr, b, t);
     e = upload_schedule(p, b, t, &p->d_bundles, &p->d_tasks, s);
     if (e != cudaSuccess) return e;
@@ -604,11 +665,11 @@ cudaError_t vjp_setup(pbe_batch_plan* p, cudaStream_t s)
     std::vector<int> tile_off(static_cast<size_t>(p->n_cells) + 1, 0);
     for (int c = 0; c < p->n_cells; ++c) tile_off[c + 1] = tile_off[c] + (p->cell_n[c] + W - 1) / W;
     std::vector<int4> b;
-    std::vector<int2> t;
+    std::vector<int4> t;
     build_schedule(*p, p->group_size, nullptr, b, t, true);
     int* dto = nullptr;
     int4* db = nullptr;
-    int2* dt = nullptr;
+    int4* dt = nullptr;
     cudaError_t e = plan_alloc(p, &vd.h, C);
     if (e == cudaSuccess) e = plan_alloc(p, &vd.D, C);
     if (e == cudaSuccess) e = plan_alloc(p, &vd.mom, static_cast<size_t>(p->n_cells) * 16);

@@ -70,7 +70,15 @@ struct BatchDev {
     double* tfirst; double* tcarry; int* tticket;   // [sum of the cells' tiles]
     // schedule
     const int4* bundles;   // {first task, tasks, group size, 0}
-    const int2* tasks;     // {cell, first bin}
+    const int4* tasks;     // {cell, first bin, lag chunk, chunks of the tile}
+    // lag chunks of the tiles (plans with few tiles: see build_schedule):
+    // chunk c of a tile covers the lags [c Cg, (c + 1) Cg); the tile's last
+    // chunk task (ticket count a multiple of its chunk count: no reset needed)
+    // adds the chunks' slot sums in order and runs the epilogue
+    int Cg;                // lags per chunk (0: no chunks)
+    int cbound;            // most chunks of a tile
+    double* cpart;         // [tiles * cbound * 2 kTileW]
+    unsigned* cticket;     // [tiles] lag-chunk tasks of the tile done (wraps at nct)
     int n_bundles;
     int num_sms;
 };
@@ -83,7 +91,7 @@ struct BatchVjpDev {
     double* tpart;         // [2 * tiles]: parameter partials per row tile
     const int* tile_off;   // [n_cells + 1]: first row-tile slot of each cell
     const int4* bundles;   // row-tile bundles {first task, tasks, group size, 0}
-    const int2* tasks;     // {cell, first row}
+    const int4* tasks;     // {cell, first row, 0, 1}
     int n_bundles;
     int* counter;
 };
@@ -199,7 +207,7 @@ cudaError_t batch_main(const BatchDev& d, const double* Y, const pbe_batch_cell_
 // Same over an explicit bundle list (the autotuner's candidate schedules).
 cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
                                const pbe_batch_cell_params_t* params, double* out,
-                               bool accumulate, const int4* bundles, const int2* tasks,
+                               bool accumulate, const int4* bundles, const int4* tasks,
                                int n_bundles, cudaStream_t s);
 // Death term N_i sum_k beta(x_i, x_k) N_k of every cell (death_gemm.cu):
 // method 0 = per-cell moments, 1 = FP64 tensor-core GEMM over the work items

@@ -432,10 +432,10 @@ batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __
 template <int K>
 __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                            const pbe_batch_cell_params_t* __restrict__ params, double* out,
-                           bool accumulate, int2 tk, double* red, TileShared& sm,
+                           bool accumulate, int4 tk, double* red, TileShared& sm,
                            const TileGroup& G)
 {
-    const int c = tk.x, I = tk.y;
+    const int c = tk.x, I = tk.y, chunk = tk.z, nct = tk.w;
     const BatchCellDev cd = d.cells[c];
     const BatchGridDev gd = d.grids[cd.grid];
     const int n = cd.n;
@@ -468,7 +468,34 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
     const int tile = (n - I) / W - 1;
     const int St = -ilogb(v.x[max(I, 0)]);
     if (agg) {
-        agg_tile_accumulate<K, true>(v, I, 0, n, St, red, sm, G);    // syncs the group first
+        const int d_begin = nct > 1 ? chunk * d.Cg : 0;
+        const int d_end = nct > 1 ? min(n, d_begin + d.Cg) : n;
+        agg_tile_accumulate<K, true>(v, I, d_begin, d_end, St, red, sm, G);   // syncs the group first
+        if (nct > 1) {
+            // this chunk's slot sums; the tile's last chunk task adds all of
+            // them in chunk order and runs the epilogue (nobody waits)
+            constexpr int R2 = TileSlots<true>::rows;
+            const int slot = cd.tile_off + tile;
+            double* cp = d.cpart + static_cast<size_t>(slot) * d.cbound * R2;
+            if (G.lane < R2) cp[chunk * R2 + G.lane] = sm.fin[G.g][G.lane];
+            G.sync();
+            if (G.lane == 0) {
+                __threadfence();
+                // the ticket counts 0 .. nct-1 and wraps to 0 on the last chunk
+                // task, so it is ready for the next launch without a reset
+                sm.last[G.g] = atomicInc(d.cticket + slot, static_cast<unsigned>(nct - 1))
+                               == static_cast<unsigned>(nct - 1);
+            }
+            G.sync();
+            if (!sm.last[G.g]) return;
+            __threadfence();
+            if (G.lane < R2) {
+                double acc = 0.0;
+                for (int q = 0; q < nct; ++q) acc += __ldcg(cp + q * R2 + G.lane);
+                sm.fin[G.g][G.lane] = acc;
+            }
+            G.sync();
+        }
 #pragma unroll
         for (int q = 0; q < 5; ++q) v.M[q] = sm.cinfo[G.g][q];
         v.b0 = sm.cinfo[G.g][5]; v.bbr = sm.cinfo[G.g][6]; v.bsh = sm.cinfo[G.g][7];
@@ -503,7 +530,7 @@ template <int K>
 __global__ void __launch_bounds__(kMainThreads, 2)
 batch_main_kernel(BatchDev d, const double* __restrict__ Y,
                   const pbe_batch_cell_params_t* __restrict__ params, double* out, int accumulate,
-                  const int4* __restrict__ bundles, const int2* __restrict__ tasks, int n_bundles)
+                  const int4* __restrict__ bundles, const int4* __restrict__ tasks, int n_bundles)
 {
     extern __shared__ double red[];     // [2 W][kMainThreads]
     __shared__ TileShared sm;
@@ -528,7 +555,7 @@ batch_main_kernel(BatchDev d, const double* __restrict__ Y,
 
 template <int K>
 cudaError_t main_k(const BatchDev& d, const double* Y, const pbe_batch_cell_params_t* params,
-                   double* out, bool accumulate, const int4* bundles, const int2* tasks,
+                   double* out, bool accumulate, const int4* bundles, const int4* tasks,
                    int n_bundles, cudaStream_t s)
 {
     const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
@@ -688,7 +715,7 @@ cudaError_t batch_rk45_control(const BatchDev& d, double* N, const double* Y,
 
 cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
                                const pbe_batch_cell_params_t* params, double* out,
-                               bool accumulate, const int4* bundles, const int2* tasks,
+                               bool accumulate, const int4* bundles, const int4* tasks,
                                int n_bundles, cudaStream_t s)
 {
     switch (d.kernel < 0 ? 0 : d.kernel) {

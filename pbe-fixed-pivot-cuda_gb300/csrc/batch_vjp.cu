@@ -113,7 +113,7 @@ batch_vjp_prep_kernel(BatchDev d, BatchVjpDev vd, const double* __restrict__ N,
 template <int K>
 __device__ void batch_vjp_task(const BatchDev& d, const BatchVjpDev& vd, const double* N,
                                const double* lam, double* gN,
-                               const pbe_batch_cell_params_t* __restrict__ params, int2 tk,
+                               const pbe_batch_cell_params_t* __restrict__ params, int4 tk,
                                double* red, VjpShared& sm, const TileGroup& G)
 {
     const int c = tk.x, I = tk.y;
