@@ -331,6 +331,13 @@ int pbe_batch_ros2_adaptive(pbe_batch_t plan, double* N, const pbe_batch_cell_pa
                             int max_attempts, int* steps, int* rejects, int* attempts,
                             double* resid, void* stream);
 
+/* Krylov tolerance of the plan's Rosenbrock solves (default 0): a cell's
+ * GMRES ends once its least-squares residual |r - A x| <= tol |r|, before
+ * krylov_dim steps; the cell is then left out of the remaining
+ * Jacobian-vector products of that solve. 0 runs every solve for krylov_dim
+ * steps (or to an exact breakdown). tol in [0, 1), else cudaErrorInvalidValue. */
+int pbe_batch_set_krylov_tol(pbe_batch_t plan, double tol);
+
 /* Mesh-field (structure-of-arrays) layout for CFD coupling: soa[i * ld + c]
  * (device) is bin i of cell c, one field per bin over the cells, ld >=
  * n_cells; rows i < n_c of every cell are read (from_soa: soa -> packed N)

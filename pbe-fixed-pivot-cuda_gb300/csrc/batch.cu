@@ -73,6 +73,7 @@ struct pbe_batch_plan {
     // linearly implicit (Rosenbrock) integrator: GMRES state and stage vectors
     pbe_gb300::GmresDev gm{};
     int gm_cap = 0;                    // Krylov dimension the GMRES buffers hold
+    double krylov_tol = 0.0;           // relative residual that ends a solve early (0: never)
     double* ros = nullptr;             // F, K1, K2, Y (4 packed vectors)
     double* ros_cell = nullptr;        // adaptive: t, dt, gamma dt per cell
     int* ros_int = nullptr;            // adaptive: status, steps, rejects per cell; done
@@ -814,14 +815,18 @@ const double kDPErr[7] = {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0,
 // J(N) v = T(N, v) + T(v, N) for the aggregation part (two passes of the pair
 // kernel with the j side from the first vector, batch_kernels.cu) plus the
 // breakage Jacobian at N applied to v (first pass).
+// skip (device, n_cells, or null): cells left out of both passes (their
+// out entries keep their old values).
 cudaError_t jvp(pbe_batch_plan* p, const double* N, const double* v,
-                const pbe_batch_cell_params_t* prm, double* out, cudaStream_t s)
+                const pbe_batch_cell_params_t* prm, double* out, cudaStream_t s,
+                const int* skip = nullptr)
 {
     if (!p->d.Ha) {
         cudaError_t e = plan_alloc(p, &p->d.Ha, static_cast<size_t>(p->total));
         if (e != cudaSuccess) { p->d.Ha = nullptr; return e; }
     }
-    const BatchDev& d = p->d;
+    BatchDev d = p->d;
+    d.skip = skip;
     BatchDev d1 = d;
     d1.A = N;
     cudaError_t e = batch_jvp_prep(d, N, v, N, prm, true, s);
@@ -866,7 +871,8 @@ cudaError_t gmres_solve(pbe_batch_plan* p, const double* N, const double* r, dou
     const GmresDev& g = p->gm;
     cudaError_t e = batch_gmres_start(d, g, N, r, prm, s);
     for (int j = 0; j < g.m && e == cudaSuccess; ++j) {
-        e = jvp(p, N, g.Z, prm, g.W, s);
+        // cells whose solve has ended (or never started) are left out
+        e = jvp(p, N, g.Z, prm, g.W, s, g.done);
         if (e == cudaSuccess) e = batch_gmres_arnoldi(d, g, j, s);
     }
     if (e == cudaSuccess) e = batch_gmres_finish(d, g, x, resid, s);
@@ -892,6 +898,8 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     p->gm.total = static_cast<long long>(C);
     p->gm.gt = (1.0 + 1.0 / std::sqrt(2.0)) * dt;
     p->gm.gtc = nullptr;
+    p->gm.skip = nullptr;
+    p->gm.tol = p->krylov_tol;
     double* F = p->ros;
     double* K1 = p->ros + C;
     double* K2 = p->ros + 2 * C;
@@ -916,7 +924,7 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
 // ROS2 to t_end with a step size per cell (batch_implicit.cu: stage and
 // controller kernels, Rk45Ctl conventions): attempts are enqueued in chunks of
 // 4, then the count of finished cells is read back. A finished cell runs with
-// dt = 0 (its solves are trivial; the pair kernel still covers it).
+// dt = 0 and is left out of the RHS, Jacobian-vector and solve launches.
 cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
                           double t_end, double rtol, double atol, double dt0, int m,
                           int max_attempts, int* steps_out, int* rejects_out, int* attempts_out,
@@ -949,6 +957,8 @@ cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_par
     p->gm.total = static_cast<long long>(C);
     p->gm.gt = 0.0;
     p->gm.gtc = gtc;
+    p->gm.skip = ctl.status;               // finished cells: no solve
+    p->gm.tol = p->krylov_tol;
     const double gamma = 1.0 + 1.0 / std::sqrt(2.0);
     std::vector<double> init(3 * nc, 0.0);
     for (size_t c = 0; c < nc; ++c) init[nc + c] = std::min(dt0, t_end);
@@ -960,7 +970,8 @@ cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_par
     double* K1 = p->ros + C;
     double* K2 = p->ros + 2 * C;
     double* Y = p->ros + 3 * C;
-    const BatchDev& d = p->d;
+    BatchDev d = p->d;
+    d.skip = ctl.status;                   // finished cells: no RHS work
     const long long T = static_cast<long long>(C);
     int attempts = 0, done = 0;
     while (e == cudaSuccess && attempts < max_attempts && done < p->n_cells) {
@@ -993,12 +1004,12 @@ cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_par
 
 // Adaptive embedded RK 5(4) for every cell to t_end: attempts are enqueued
 // in chunks of 8 (6 RHS evaluations and one control launch each), then the
-// count of finished cells is read back.
+// count of finished cells is read back. Finished cells are left out of the
+// RHS launches.
 cudaError_t rk45(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double t_end,
                  double rtol, double atol, double dt0, int max_attempts, int* steps_out,
                  int* rejects_out, int* attempts_out, cudaStream_t s)
 {
-    const BatchDev& d = p->d;
     const size_t C = static_cast<size_t>(p->total), nc = static_cast<size_t>(p->n_cells);
     cudaError_t e = cudaSuccess;
     if (!p->rk_k) {
@@ -1017,6 +1028,8 @@ cudaError_t rk45(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     ctl.t_end = t_end;
     ctl.rtol = rtol;
     ctl.atol = atol;
+    BatchDev d = p->d;
+    d.skip = ctl.status;                   // finished cells: no RHS work
     std::vector<double> init(2 * nc, 0.0);
     for (size_t c = 0; c < nc; ++c) init[nc + c] = std::min(dt0, t_end);
     e = cudaMemcpyAsync(p->rk_cell, init.data(), init.size() * sizeof(double),
@@ -1280,6 +1293,15 @@ int pbe_batch_ros2_adaptive(pbe_batch_t plan, double* N, const pbe_batch_cell_pa
         return cudaErrorInvalidValue;
     return ros2_adaptive(plan, N, params, t_end, rtol, atol, dt0, krylov_dim, max_attempts, steps,
                          rejects, attempts, resid, static_cast<cudaStream_t>(stream));
+}
+
+int pbe_batch_set_krylov_tol(pbe_batch_t plan, double tol)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (!(tol >= 0.0) || !(tol < 1.0)) return cudaErrorInvalidValue;
+    plan->krylov_tol = tol;
+    return cudaSuccess;
 }
 
 int pbe_batch_from_soa(pbe_batch_t plan, const double* soa, long long ld, double* N, void* stream)

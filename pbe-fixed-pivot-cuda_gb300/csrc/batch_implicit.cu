@@ -96,10 +96,10 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
     }
     rr = block_sum(rr, sh);
     const double b0 = sqrt(rr);
-    const bool live = b0 > 0.0 && b0 < 1.7e308;
+    const bool live = b0 > 0.0 && b0 < 1.7e308 && !(g.skip && g.skip[c]);
     const double inv = live ? 1.0 / b0 : 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double v0 = r[off + i] * inv;
+        const double v0 = live ? r[off + i] * inv : 0.0;
         g.V[off + i] = v0;
         g.Z[off + i] = v0 / g.P[off + i];
     }
@@ -121,6 +121,7 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
 {
     __shared__ double sh[8];
     __shared__ double h_s[kGmresMaxDim + 1];
+    __shared__ int more_s;
     const int c = blockIdx.x;
     const BatchCellDev cd = d.cells[c];
     const int off = cd.off, n = cd.n;
@@ -150,16 +151,6 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
     double s2 = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s2 = fma(w[i], w[i], s2);
     const double hn = sqrt(block_sum(s2, sh));
-    // a new direction lost to round-off (an invariant Krylov space: the
-    // solution is exact) or the last allowed step ends the cell's solve
-    const bool more = hn > 1e-13 * wn0 && j + 1 < g.m;
-    const double inv = hn > 0.0 ? 1.0 / hn : 0.0;
-    double* v1 = g.V + static_cast<size_t>(j + 1) * T + off;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double v = more ? w[i] * inv : 0.0;
-        v1[i] = v;
-        g.Z[off + i] = v / g.P[off + i];
-    }
     if (threadIdx.x == 0) {
         const int m = g.m, m1 = m + 1;
         double* H = g.H + static_cast<size_t>(c) * m1 * m;   // column-major, column j at H + j*m1
@@ -184,7 +175,22 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
         gg[j + 1] = -sj * gg[j];
         gg[j] = cj * gg[j];
         g.kval[c] = j + 1;
+        // a new direction lost to round-off (an invariant Krylov space: the
+        // solution is exact), the last allowed step, or a residual |g_{j+1}|
+        // within the tolerance ends the cell's solve
+        const bool conv = g.tol > 0.0 && fabs(gg[j + 1]) <= g.tol * g.beta0[c];
+        const bool more = hn > 1e-13 * wn0 && j + 1 < g.m && !conv;
         if (!more) g.done[c] = 1;
+        more_s = more ? 1 : 0;
+    }
+    __syncthreads();
+    const bool more = more_s != 0;
+    const double inv = hn > 0.0 ? 1.0 / hn : 0.0;
+    double* v1 = g.V + static_cast<size_t>(j + 1) * T + off;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = more ? w[i] * inv : 0.0;
+        v1[i] = v;
+        g.Z[off + i] = v / g.P[off + i];
     }
 }
 

@@ -73,14 +73,19 @@ struct BatchDev {
     const int4* tasks;     // {cell, first bin, lag chunk, chunks of the tile}
     // lag chunks of the tiles (plans with few tiles: see build_schedule):
     // chunk c of a tile covers the lags [c Cg, (c + 1) Cg); the tile's last
-    // chunk task (ticket count a multiple of its chunk count: no reset needed)
-    // adds the chunks' slot sums in order and runs the epilogue
+    // chunk task (a ticket that wraps to 0 with it: no reset needed) adds the
+    // chunks' slot sums in order and runs the epilogue
     int Cg;                // lags per chunk (0: no chunks)
     int cbound;            // most chunks of a tile
     double* cpart;         // [tiles * cbound * 2 kTileW]
     unsigned* cticket;     // [tiles] lag-chunk tasks of the tile done (wraps at nct)
     int n_bundles;
     int num_sms;
+    // [n_cells] or null: a cell with a nonzero entry is left out of the prep
+    // and pair launches (its outputs keep their old values): the finished
+    // cells of an adaptive run, the ended solves of a GMRES. The entries do not
+    // change during a launch, so all tasks of a cell agree.
+    const int* skip;
 };
 
 // Scratch of the batched VJP (batch_vjp.cu).
@@ -142,9 +147,11 @@ struct GmresDev {
     int* kval;       // [n_cells] Arnoldi steps taken
     int* done;       // [n_cells] solve ended (converged, breakdown or m steps)
     const double* gtc;   // [n_cells] gamma dt per cell (adaptive steps), or null: gt
+    const int* skip;     // [n_cells] or null: cells whose solve is not run (x = 0)
     long long total;
     int m;
     double gt;       // gamma dt
+    double tol;      // a solve ends once |r - A x| <= tol |r| (0: after m steps or breakdown)
 };
 
 // Launchers (batch_kernels.cu). All are asynchronous on `s`.

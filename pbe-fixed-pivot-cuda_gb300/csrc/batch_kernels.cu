@@ -251,6 +251,7 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
                   int stage, double c, double dt6, StageCombine sc)
 {
     __shared__ double sh[8];
+    if (d.skip && d.skip[blockIdx.x]) return;       // whole block
     const BatchCellDev cd = d.cells[blockIdx.x];
     const BatchGridDev gd = d.grids[cd.grid];
     const pbe_batch_cell_params_t P = params[blockIdx.x];
@@ -360,6 +361,7 @@ batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __
                       int brk)
 {
     __shared__ double sh[8];
+    if (d.skip && d.skip[blockIdx.x]) return;       // whole block
     const BatchCellDev cd = d.cells[blockIdx.x];
     const BatchGridDev gd = d.grids[cd.grid];
     const pbe_batch_cell_params_t P = params[blockIdx.x];
@@ -436,6 +438,7 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                            const TileGroup& G)
 {
     const int c = tk.x, I = tk.y, chunk = tk.z, nct = tk.w;
+    if (d.skip && d.skip[c]) return;                // the whole group
     const BatchCellDev cd = d.cells[c];
     const BatchGridDev gd = d.grids[cd.grid];
     const int n = cd.n;

@@ -161,6 +161,11 @@ class BatchPlan:
             rejects.ctypes.data, ctypes.byref(att), _ptr(resid, "resid"), _stream(stream))
         return code, steps, rejects, att.value
 
+    def set_krylov_tol(self, tol: float) -> int:
+        """Relative residual that ends a cell's GMRES solve early in ros2 and
+        ros2_adaptive (0, the default: krylov_dim steps or an exact breakdown)."""
+        return _lib.load().pbe_batch_set_krylov_tol(self._h, float(tol))
+
     def from_soa(self, soa, ld: int, N, stream=None) -> int:
         """N[off_c + i] = soa[i * ld + c] for the bins of every cell (mesh fields
         -> packed state)."""

@@ -230,3 +230,59 @@ def test_ros2_adaptive_on_a_persistently_stiff_cell():
     assert abs(int(steps[0]) - st) <= 1 and rejects[0] == rj, (steps, rejects, st, rj)
     assert att < 20000 // 4
     assert np.abs(A - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+def test_krylov_tolerance_ends_solves_early_within_tolerance():
+    """pbe_batch_set_krylov_tol: with tol = 1e-9 every solve stops once its
+    relative least-squares residual is <= tol (the reported residuals are),
+    the steps stay on the oracle's dense-solve ROS2 (relative 1e-6) but are
+    not the full-dimension solves bit for bit (some solve stopped early); the
+    adaptive controller with tol = 1e-9 takes the dense controller's steps.
+    Tolerances outside [0, 1) are rejected."""
+    torch = _torch()
+    rng = np.random.default_rng(905)
+    grids, cell_n, cell_grid, N, params = mixed_batch(rng, 5, 2, n_cells=12, n_max=40)
+    N = [np.abs(Nc) for Nc in N]
+    t_q, bw_q = DAUGHTER
+    dt, steps = 0.5, 3
+    with pg.BatchPlan(grids, cell_n, cell_grid, 5, 2, t_q, bw_q) as plan:
+        for bad in (-1e-3, 1.0, float("nan")):
+            assert plan.set_krylov_tol(bad) == pg.ERR_INVALID_VALUE
+        outs, rs = [], []
+        for tol in (0.0, 1e-9):
+            assert plan.set_krylov_tol(tol) == 0
+            dN = t(np.concatenate(N))
+            resid = t(np.zeros(len(cell_n)))
+            code = plan.ros2(dN, t(params), dt, steps, krylov_dim=48, resid=resid)
+            assert code == 0, pg.error_string(code)
+            torch.cuda.synchronize()
+            outs.append(dN.cpu().numpy())
+            rs.append(resid.cpu().numpy())
+        assert np.all(rs[1] <= 1e-9), rs[1]
+        assert not np.array_equal(outs[0].view(np.int64), outs[1].view(np.int64))
+        for c in range(len(cell_n)):
+            x = grids[cell_grid[c]][:cell_n[c]]
+            agg, brk = _dicts(5, 2, params[c], t_q, bw_q)
+            ref = N[c].copy()
+            for _ in range(steps):
+                ref = pyoracle.ros2_step(ref, x, dt, agg, brk)
+            o = plan.offsets[c]
+            sc = np.abs(ref).max() + np.abs(N[c]).max() + 1e-300
+            assert np.abs(outs[1][o:o + cell_n[c]] - ref).max() / sc < 1e-6, c
+        # adaptive
+        t_end, rtol, dt0 = 4.0, 1e-4, 0.1
+        atol = 1e-6 * max(Nc.max() for Nc in N)
+        dN = t(np.concatenate(N))
+        code, st, rj, att = plan.ros2_adaptive(dN, t(params), t_end, rtol, atol, dt0,
+                                               krylov_dim=40)
+        assert code == 0, pg.error_string(code)
+        torch.cuda.synchronize()
+        got = dN.cpu().numpy()
+    for c in range(len(cell_n)):
+        x = grids[cell_grid[c]][:cell_n[c]]
+        agg, brk = _dicts(5, 2, params[c], t_q, bw_q)
+        ref, s_o, r_o, status = pyoracle.ros2_adaptive(N[c], x, t_end, rtol, atol, dt0, agg, brk)
+        assert status == 1
+        assert abs(int(st[c]) - s_o) <= 1 and abs(int(rj[c]) - r_o) <= 1, (c, st[c], rj[c], s_o, r_o)
+        o = plan.offsets[c]
+        assert np.abs(got[o:o + cell_n[c]] - ref).max() <= 1e-6 * (np.abs(ref).max() + 1e-300), c
