@@ -552,6 +552,7 @@ def profile_case(name: str) -> None:
       batched : 1024 cells of the batched workload (seed 2026), 4 batched RHS
       death   : the 512-cell size-class workload, 3 DMMA and 3 moment death calls
       vjp     : the n = 16384 workload, 3 aggregation + breakage VJPs
+      breakage: the n = 16384 workload, 3 breakage RHS calls in each mode
       adjoint : the n = 3840 flocculation tape, 10 steps forward + backward"""
     import torch
 
@@ -586,6 +587,13 @@ def profile_case(name: str) -> None:
         for _ in range(3):
             pg.check(pg.aggregation_rhs_vjp(dN, dx, lam, gN, ga, ap), "agg vjp")
             pg.check(pg.breakage_rhs_vjp(dN, dx, dt, db, lam, gN, gb, bp), "brk vjp")
+    elif name == "breakage":
+        x, N, t_q, bw_q, ap, bp = workload()
+        dN, dx = torch.tensor(N, **f64), torch.tensor(x, **f64)
+        dt, db = torch.tensor(t_q, **f64), torch.tensor(bw_q, **f64)
+        rhs = torch.zeros(N_BINS, **f64)
+        for mode in (pg.MODE_GATHER,) * 3 + (pg.MODE_SCATTER,) * 3:
+            pg.check(pg.breakage_rhs(dN, dx, dt, db, rhs, bp, mode=mode), "brk")
     elif name == "adjoint":
         cfg = pg.grids.config_flocculation_adjoint(n_steps=10, switch_step=5)
         dx, dtq, dbw = (torch.tensor(cfg[k], **f64) for k in ("x", "t_q", "bw_q"))
@@ -695,7 +703,7 @@ def reference_kernels_section(dev, stream, dN, dx, dt, db, rhs, ap, bp, flush, s
 
 def main():
     ap_ = argparse.ArgumentParser()
-    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint", "vjp"],
+    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint", "vjp", "breakage"],
                      help="run a few launches of one kernel family (for ncu) and exit")
     ap_.add_argument("--gpus", type=int, default=1)
     ap_.add_argument("--steps", type=int, default=200)
