@@ -77,6 +77,9 @@ struct pbe_batch_plan {
     double* ros = nullptr;             // F, K1, K2, Y (4 packed vectors)
     double* ros_cell = nullptr;        // adaptive: t, dt, gamma dt per cell
     int* ros_int = nullptr;            // adaptive: status, steps, rejects per cell; done
+    // selection function per cell bin for one multi-stage call (sel_cache);
+    // allocated with the plan, so that a call under stream capture allocates nothing
+    double* sx = nullptr;
     // per-cell launch loop scratch (allocated on first use)
     void* cell_agg_ws = nullptr;
     void* cell_brk_ws = nullptr;
@@ -481,6 +484,7 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     if (e == cudaSuccess) e = plan_alloc(p, &d.tfirst, static_cast<size_t>(tiles));
     if (e == cudaSuccess) e = plan_alloc(p, &d.tcarry, static_cast<size_t>(tiles));
     if (e == cudaSuccess) e = plan_alloc(p, &d.tticket, static_cast<size_t>(tiles));
+    if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->sx, C);
     if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_tq, static_cast<size_t>(p->nq));
     if (e == cudaSuccess && p->nq > 0) e = plan_alloc(p, &p->d_bw, static_cast<size_t>(p->nq));
     if (e != cudaSuccess) return e;
@@ -548,10 +552,34 @@ cudaError_t check_plan(pbe_batch_plan* p)
     return dev == p->device ? cudaSuccess : cudaErrorInvalidDevice;
 }
 
-// One RK4 step sequence (or a plain RHS) enqueued on s.
+// Selection function of every cell bin for the parameters of one
+// multi-stage call, computed once on s at the call's start (for the power law
+// one pow per bin instead of one per bin and stage): the plan's kernels read it
+// while the SelScope of the call is alive. Plans without breakage: nothing.
+struct SelScope {
+    pbe_batch_plan* p;
+    explicit SelScope(pbe_batch_plan* q) : p(q) {}
+    ~SelScope() { p->d.Sx = nullptr; }
+    SelScope(const SelScope&) = delete;
+    SelScope& operator=(const SelScope&) = delete;
+};
+
+cudaError_t sel_cache(pbe_batch_plan* p, const pbe_batch_cell_params_t* prm, cudaStream_t s)
+{
+    p->d.Sx = nullptr;
+    if (p->selection < 0 || p->nq <= 0 || !p->sx) return cudaSuccess;
+    cudaError_t e = batch_sel(p->d, prm, p->sx, s);   // (sx: allocated with the plan)
+    if (e == cudaSuccess) p->d.Sx = p->sx;
+    return e;
+}
+
+// One RK4 step sequence enqueued on s.
 cudaError_t enqueue_rk4(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm,
                         double dt, int n_steps, cudaStream_t s)
 {
+    SelScope scope(p);
+    cudaError_t e0 = sel_cache(p, prm, s);
+    if (e0 != cudaSuccess) return e0;
     const BatchDev& d = p->d;
     const double h = 0.5 * dt, dt6 = dt / 6.0;
     cudaError_t e = cudaSuccess;
@@ -696,6 +724,7 @@ cudaError_t vjp_setup(pbe_batch_plan* p, cudaStream_t s)
 // previous step). ckpt: N at every step multiple of `every` is copied to
 // ckpt[step / every]. Ys: the stage states of every step are copied to
 // Ys[((step - s0) * 4 + q) * total]. finish: close the last step.
+// (The caller holds a SelScope with the selection of prm cached.)
 cudaError_t run_steps(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* prm, double dt,
                       int s0, int s1, bool first, double* ckpt, int every, double* Ys,
                       bool finish, cudaStream_t s)
@@ -748,6 +777,9 @@ cudaError_t tape_forward(pbe_batch_plan* p, double* N, const pbe_batch_cell_para
         p->t_seg_cap = 4 * seg * C;
     }
     p->t_recorded = false;
+    SelScope scope(p);
+    e = sel_cache(p, prm, s);
+    if (e != cudaSuccess) return e;
     e = run_steps(p, N, prm, dt, 0, n_steps, true, p->t_ckpt, every, nullptr, true, s);
     if (e != cudaSuccess) return e;
     p->t_recorded = true;
@@ -771,7 +803,9 @@ cudaError_t tape_backward(pbe_batch_plan* p, const double* lamT, double* gN0, do
     const double dt = p->t_dt, h = 0.5 * dt, c6 = dt / 6.0;
     const double cs[3] = {h, h, dt};
     const pbe_batch_cell_params_t* prm = p->t_params;
-    cudaError_t e = cudaMemcpyAsync(lam, lamT, bytes, cudaMemcpyDeviceToDevice, s);
+    SelScope scope(p);
+    cudaError_t e = sel_cache(p, prm, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lam, lamT, bytes, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(gp, 0, sizeof(double) * 8 * static_cast<size_t>(p->n_cells), s);
     const int every = p->t_every;
@@ -900,6 +934,9 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     p->gm.gtc = nullptr;
     p->gm.skip = nullptr;
     p->gm.tol = p->krylov_tol;
+    SelScope scope(p);
+    e = sel_cache(p, prm, s);
+    if (e != cudaSuccess) return e;
     double* F = p->ros;
     double* K1 = p->ros + C;
     double* K2 = p->ros + 2 * C;
@@ -966,6 +1003,9 @@ cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_par
                         cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->ros_int, 0, (3 * nc + 1) * sizeof(int), s);
     if (e == cudaSuccess && resid) e = cudaMemsetAsync(resid, 0, nc * sizeof(double), s);
+    SelScope scope(p);
+    if (e == cudaSuccess) e = sel_cache(p, prm, s);
+    if (e != cudaSuccess) return e;
     double* F = p->ros;
     double* K1 = p->ros + C;
     double* K2 = p->ros + 2 * C;
@@ -1028,6 +1068,9 @@ cudaError_t rk45(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     ctl.t_end = t_end;
     ctl.rtol = rtol;
     ctl.atol = atol;
+    SelScope scope(p);
+    e = sel_cache(p, prm, s);
+    if (e != cudaSuccess) return e;
     BatchDev d = p->d;
     d.skip = ctl.status;                   // finished cells: no RHS work
     std::vector<double> init(2 * nc, 0.0);

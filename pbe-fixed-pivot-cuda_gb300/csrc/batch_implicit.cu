@@ -86,7 +86,8 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
                  + beta_self<K>(xi, P.beta0, P.beta_br, P.beta_sh) * y;
         }
         if (d.selection >= 0 && d.nq > 0) {
-            const double S = sel_value_i(d.selection, xi, P.S0, P.v_ref, P.alpha, P.v_min);
+            const double S = d.Sx ? d.Sx[off + i]
+                                  : sel_value_i(d.selection, xi, P.S0, P.v_ref, P.alpha, P.v_min);
             if (S != 0.0 && y > kBreakageNMin) loss += S;
         }
         const double p = 1.0 + gt * fmax(loss, 0.0);

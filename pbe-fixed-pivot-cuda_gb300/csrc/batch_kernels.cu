@@ -165,6 +165,19 @@ cell_stage_kernel(double* N, const double* k, double* kacc, double* Y, int n, in
     if (i < n) stage_update(stage, N, k, kacc, Y, i, c, dt6);
 }
 
+// Selection function of every cell bin for the given parameters (one CTA per
+// cell): evaluated once per multi-stage call instead of once per stage.
+__global__ void __launch_bounds__(256)
+batch_sel_kernel(BatchDev d, const pbe_batch_cell_params_t* __restrict__ params,
+                 double* __restrict__ Sx)
+{
+    const BatchCellDev cd = d.cells[blockIdx.x];
+    const pbe_batch_cell_params_t P = params[blockIdx.x];
+    const double* x = d.gx + d.grids[cd.grid].off;
+    for (int i = threadIdx.x; i < cd.n; i += blockDim.x)
+        Sx[cd.off + i] = sel_value(d.selection, x[i], P.S0, P.v_ref, P.alpha, P.v_min);
+}
+
 // ---------------------------------------------------------------------------
 // Clipped pairs of a cell (v >= x[n-1], all deposited on bin n-1), summed by
 // the group of the task that owns bin n-1: per lag on a geometric grid (the
@@ -294,7 +307,7 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
             m[4] += h;
         }
         if (F >= 0) {
-            const double S = sel_value(F, xi, P.S0, P.v_ref, P.alpha, P.v_min);
+            const double S = d.Sx ? d.Sx[off + i] : sel_value(F, xi, P.S0, P.v_ref, P.alpha, P.v_min);
             d.SN[off + i] = (S != 0.0 && y > kBreakageNMin) ? S * y : 0.0;
         }
     }
@@ -392,7 +405,8 @@ batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __
         if (F >= 0) {
             double sn = 0.0;
             if (brk) {
-                const double S = sel_value(F, xi, P.S0, P.v_ref, P.alpha, P.v_min);
+                const double S = d.Sx ? d.Sx[off + i]
+                                      : sel_value(F, xi, P.S0, P.v_ref, P.alpha, P.v_min);
                 sn = (S != 0.0 && Gs[off + i] > kBreakageNMin) ? S * yb : 0.0;
             }
             d.SN[off + i] = sn;
@@ -685,6 +699,14 @@ cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params
 {
     const StageCombine none{};
     return prep_any(d, N, params, stage, c, dt6, none, s);
+}
+
+cudaError_t batch_sel(const BatchDev& d, const pbe_batch_cell_params_t* params, double* Sx,
+                      cudaStream_t s)
+{
+    if (d.n_cells <= 0 || d.selection < 0) return cudaErrorInvalidValue;
+    batch_sel_kernel<<<d.n_cells, 256, 0, s>>>(d, params, Sx);
+    return cudaGetLastError();
 }
 
 cudaError_t batch_jvp_prep(const BatchDev& d, const double* A, const double* B, const double* G,
