@@ -80,7 +80,8 @@ batch_vjp_prep_kernel(BatchDev d, BatchVjpDev vd, const double* __restrict__ N,
         double p0 = 0.0, p1 = 0.0, p2 = 0.0;
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
             const double xj = x[j], Nj = Nc[j];
-            const double S = sel_value_v(F, xj, P.S0, P.v_ref, P.alpha, P.v_min);
+            const double S = d.Sx ? d.Sx[off + j]
+                                  : sel_value_v(F, xj, P.S0, P.v_ref, P.alpha, P.v_min);
             if (!((S != 0.0) && (Nj > kBreakageNMin))) continue;
             double Q = -lc[j];
             for (int q = 0; q < d.nq; ++q) {
