@@ -881,6 +881,7 @@ def main():
                    "l2": "flushed before every timed step (512 MiB write)",
                    "parallelism": "replicas" if n_gpus > 1 else "single GPU"},
         "pair_interactions_per_s": round(value * PAIRS, 1),
+        "fragments_per_s": round(value * N_BINS * N_QUAD, 1),
         "wall_s_timed_loop": round(wall, 4),
         "e2e": {"value": round(e2e_value, 3), "unit": "evals/s",
                 "h2d_bytes_per_step": N_BINS * 8, "d2h_bytes_per_step": N_BINS * 8},
