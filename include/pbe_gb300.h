@@ -338,6 +338,15 @@ int pbe_batch_ros2_adaptive(pbe_batch_t plan, double* N, const pbe_batch_cell_pa
  * steps (or to an exact breakdown). tol in [0, 1), else cudaErrorInvalidValue. */
 int pbe_batch_set_krylov_tol(pbe_batch_t plan, double tol);
 
+/* Restarts of the plan's Rosenbrock solves (default 0): a cell whose relative
+ * residual after krylov_dim steps is above the Krylov tolerance runs another
+ * cycle on r - A x, up to `restarts` more (each one Jacobian-vector product for
+ * the residual plus up to krylov_dim steps; cells within the tolerance are
+ * left out). With tol 0 every cell runs every cycle. The reported resid is
+ * the residual after the cell's last cycle. restarts in [0, 1000], else
+ * cudaErrorInvalidValue. */
+int pbe_batch_set_krylov_restarts(pbe_batch_t plan, int restarts);
+
 /* Mesh-field (structure-of-arrays) layout for CFD coupling: soa[i * ld + c]
  * (device) is bin i of cell c, one field per bin over the cells, ld >=
  * n_cells; rows i < n_c of every cell are read (from_soa: soa -> packed N)

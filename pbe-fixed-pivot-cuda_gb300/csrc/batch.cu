@@ -74,6 +74,7 @@ struct pbe_batch_plan {
     pbe_gb300::GmresDev gm{};
     int gm_cap = 0;                    // Krylov dimension the GMRES buffers hold
     double krylov_tol = 0.0;           // relative residual that ends a solve early (0: never)
+    int krylov_restarts = 0;           // further GMRES cycles for cells above krylov_tol
     double* ros = nullptr;             // F, K1, K2, Y (4 packed vectors)
     double* ros_cell = nullptr;        // adaptive: t, dt, gamma dt per cell
     int* ros_int = nullptr;            // adaptive: status, steps, rejects per cell; done
@@ -889,27 +890,48 @@ cudaError_t gmres_alloc(pbe_batch_plan* p, int m)
     if (e == cudaSuccess) e = plan_alloc(p, &g.beta0, nc);
     if (e == cudaSuccess) e = plan_alloc(p, &g.kval, nc);
     if (e == cudaSuccess) e = plan_alloc(p, &g.done, nc);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.R, C);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.rnorm, nc);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.last, nc);
+    if (e == cudaSuccess) e = plan_alloc(p, &g.conv, nc);
     if (e != cudaSuccess) return e;
     p->gm = g;
     p->gm_cap = m;
     return cudaSuccess;
 }
 
-// x = (I - gt J(N))^-1 r for every cell: GMRES(m) without restart, right
-// preconditioned (batch_implicit.cu); resid[c] = max(resid[c], relative
-// least-squares residual).
-cudaError_t gmres_solve(pbe_batch_plan* p, const double* N, const double* r, double* x,
-                        const pbe_batch_cell_params_t* prm, double* resid, cudaStream_t s)
+// One GMRES cycle of every cell that needs it (gmres_solve).
+cudaError_t gmres_cycle(pbe_batch_plan* p, const double* N, const double* r, double* x,
+                        const pbe_batch_cell_params_t* prm, double* resid, bool first, bool final,
+                        cudaStream_t s)
 {
     const BatchDev& d = p->d;
     const GmresDev& g = p->gm;
-    cudaError_t e = batch_gmres_start(d, g, N, r, prm, s);
+    cudaError_t e = batch_gmres_start(d, g, N, r, prm, first, s);
     for (int j = 0; j < g.m && e == cudaSuccess; ++j) {
-        // cells whose solve has ended (or never started) are left out
+        // cells whose cycle has ended (or never started) are left out
         e = jvp(p, N, g.Z, prm, g.W, s, g.done);
         if (e == cudaSuccess) e = batch_gmres_arnoldi(d, g, j, s);
     }
-    if (e == cudaSuccess) e = batch_gmres_finish(d, g, x, resid, s);
+    if (e == cudaSuccess) e = batch_gmres_finish(d, g, x, resid, !first, final, s);
+    return e;
+}
+
+// x = (I - gt J(N))^-1 r for every cell: GMRES(m), right preconditioned
+// (batch_implicit.cu), then up to g.restarts more cycles on r - A x for the
+// cells above the tolerance (one Jacobian-vector product each to form the
+// residual); resid[c] = max(resid[c], relative residual of the solve).
+cudaError_t gmres_solve(pbe_batch_plan* p, const double* N, const double* r, double* x,
+                        const pbe_batch_cell_params_t* prm, double* resid, cudaStream_t s)
+{
+    const GmresDev& g = p->gm;
+    const int R = g.restarts;
+    cudaError_t e = gmres_cycle(p, N, r, x, prm, resid, true, R == 0, s);
+    for (int k = 1; k <= R && e == cudaSuccess; ++k) {
+        e = jvp(p, N, x, prm, g.W, s, g.conv);
+        if (e == cudaSuccess) e = batch_gmres_restart(p->d, g, r, x, s);
+        if (e == cudaSuccess) e = gmres_cycle(p, N, g.R, x, prm, resid, false, k == R, s);
+    }
     return e;
 }
 
@@ -934,6 +956,7 @@ cudaError_t ros2(pbe_batch_plan* p, double* N, const pbe_batch_cell_params_t* pr
     p->gm.gtc = nullptr;
     p->gm.skip = nullptr;
     p->gm.tol = p->krylov_tol;
+    p->gm.restarts = p->krylov_restarts;
     SelScope scope(p);
     e = sel_cache(p, prm, s);
     if (e != cudaSuccess) return e;
@@ -996,6 +1019,7 @@ cudaError_t ros2_adaptive(pbe_batch_plan* p, double* N, const pbe_batch_cell_par
     p->gm.gtc = gtc;
     p->gm.skip = ctl.status;               // finished cells: no solve
     p->gm.tol = p->krylov_tol;
+    p->gm.restarts = p->krylov_restarts;
     const double gamma = 1.0 + 1.0 / std::sqrt(2.0);
     std::vector<double> init(3 * nc, 0.0);
     for (size_t c = 0; c < nc; ++c) init[nc + c] = std::min(dt0, t_end);
@@ -1344,6 +1368,15 @@ int pbe_batch_set_krylov_tol(pbe_batch_t plan, double tol)
     if (e != cudaSuccess) return e;
     if (!(tol >= 0.0) || !(tol < 1.0)) return cudaErrorInvalidValue;
     plan->krylov_tol = tol;
+    return cudaSuccess;
+}
+
+int pbe_batch_set_krylov_restarts(pbe_batch_t plan, int restarts)
+{
+    cudaError_t e = check_plan(plan);
+    if (e != cudaSuccess) return e;
+    if (restarts < 0 || restarts > 1000) return cudaErrorInvalidValue;
+    plan->krylov_restarts = restarts;
     return cudaSuccess;
 }
 

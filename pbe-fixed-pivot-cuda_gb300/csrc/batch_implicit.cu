@@ -42,11 +42,14 @@ __device__ __forceinline__ double sel_value_i(int F, double v, double S0, double
     }
 }
 
-// Start of a solve: preconditioner, |r|, v_0 = r / |r|, z = P^-1 v_0.
+// Start of a cycle: preconditioner, |r|, v_0 = r / |r|, z = P^-1 v_0. The
+// first cycle of a solve records |r| and clears the cell's conv flag; a later
+// cycle (r = the restart residual) runs only cells without conv.
 template <int K>
 __global__ void __launch_bounds__(256)
 gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
-                   const double* __restrict__ r, const pbe_batch_cell_params_t* __restrict__ params)
+                   const double* __restrict__ r, const pbe_batch_cell_params_t* __restrict__ params,
+                   int first)
 {
     __shared__ double sh[8];
     __shared__ double m_s[5];
@@ -97,7 +100,8 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
     }
     rr = block_sum(rr, sh);
     const double b0 = sqrt(rr);
-    const bool live = b0 > 0.0 && b0 < 1.7e308 && !(g.skip && g.skip[c]);
+    const bool skipped = (g.skip && g.skip[c]) || (!first && g.conv[c]);
+    const bool live = b0 > 0.0 && b0 < 1.7e308 && !skipped;
     const double inv = live ? 1.0 / b0 : 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const double v0 = live ? r[off + i] * inv : 0.0;
@@ -111,6 +115,11 @@ gmres_start_kernel(BatchDev d, GmresDev g, const double* __restrict__ N,
         g.beta0[c] = live ? b0 : 0.0;
         g.kval[c] = 0;
         g.done[c] = live ? 0 : 1;
+        if (first) {
+            g.rnorm[c] = live ? b0 : 0.0;
+            g.conv[c] = live ? 0 : 1;
+            g.last[c] = 0.0;
+        }
     }
 }
 
@@ -179,7 +188,7 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
         // a new direction lost to round-off (an invariant Krylov space: the
         // solution is exact), the last allowed step, or a residual |g_{j+1}|
         // within the tolerance ends the cell's solve
-        const bool conv = g.tol > 0.0 && fabs(gg[j + 1]) <= g.tol * g.beta0[c];
+        const bool conv = g.tol > 0.0 && fabs(gg[j + 1]) <= g.tol * g.rnorm[c];
         const bool more = hn > 1e-13 * wn0 && j + 1 < g.m && !conv;
         if (!more) g.done[c] = 1;
         more_s = more ? 1 : 0;
@@ -195,11 +204,13 @@ gmres_arnoldi_kernel(BatchDev d, GmresDev g, int j)
     }
 }
 
-// End of a solve: y = R^-1 g (the kval valid columns), x = P^-1 V y,
-// resid[c] = max(resid[c], |g_k| / |r|) (the relative residual of the
-// least-squares problem).
+// End of a cycle: y = R^-1 g (the kval valid columns), x = P^-1 V y (acc:
+// x += P^-1 V y, a restart cycle). A cell that ran this cycle records its
+// relative residual |g_k| / |r| (r the system's right-hand side) and, within
+// the tolerance, its conv flag; final: resid[c] = max(resid[c], that residual).
 __global__ void __launch_bounds__(256)
-gmres_finish_kernel(BatchDev d, GmresDev g, double* __restrict__ xo, double* __restrict__ resid)
+gmres_finish_kernel(BatchDev d, GmresDev g, double* __restrict__ xo, double* __restrict__ resid,
+                    int acc, int final)
 {
     __shared__ double y_s[kGmresMaxDim];
     const int c = blockIdx.x;
@@ -216,14 +227,37 @@ gmres_finish_kernel(BatchDev d, GmresDev g, double* __restrict__ xo, double* __r
             const double dq = H[static_cast<size_t>(q) * m1 + q];
             y_s[q] = dq != 0.0 ? s_ / dq : 0.0;
         }
-        if (resid) resid[c] = fmax(resid[c], g.beta0[c] > 0.0 ? fabs(gg[k]) / g.beta0[c] : 0.0);
+        if (g.beta0[c] > 0.0) {                // the cell ran this cycle
+            const double rel = g.rnorm[c] > 0.0 ? fabs(gg[k]) / g.rnorm[c] : 0.0;
+            g.last[c] = rel;
+            if (g.tol > 0.0 && rel <= g.tol) g.conv[c] = 1;
+        }
+        if (final && resid) resid[c] = fmax(resid[c], g.last[c]);
     }
     __syncthreads();
+    if (acc && k == 0) return;                 // nothing to add
     const size_t T = static_cast<size_t>(g.total);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double s_ = 0.0;
         for (int q = 0; q < k; ++q) s_ = fma(y_s[q], g.V[static_cast<size_t>(q) * T + off + i], s_);
-        xo[off + i] = s_ / g.P[off + i];
+        const double v = s_ / g.P[off + i];
+        xo[off + i] = acc ? xo[off + i] + v : v;
+    }
+}
+
+// Restart residual of every cell without conv: R = r - (x - gamma dt W),
+// W = J x on entry.
+__global__ void __launch_bounds__(256)
+gmres_restart_kernel(BatchDev d, GmresDev g, const double* __restrict__ r,
+                     const double* __restrict__ x)
+{
+    const int c = blockIdx.x;
+    if (g.conv[c] || (g.skip && g.skip[c])) return;      // whole block
+    const BatchCellDev cd = d.cells[c];
+    const double gt = g.gtc ? g.gtc[c] : g.gt;
+    for (int i = threadIdx.x; i < cd.n; i += blockDim.x) {
+        const int e = cd.off + i;
+        g.R[e] = r[e] - fma(-gt, g.W[e], x[e]);
     }
 }
 
@@ -319,9 +353,9 @@ ros2_control_kernel(BatchDev d, double* __restrict__ N, const double* __restrict
 
 template <int K>
 cudaError_t start_k(const BatchDev& d, const GmresDev& g, const double* N, const double* r,
-                    const pbe_batch_cell_params_t* params, cudaStream_t s)
+                    const pbe_batch_cell_params_t* params, bool first, cudaStream_t s)
 {
-    gmres_start_kernel<K><<<d.n_cells, 256, 0, s>>>(d, g, N, r, params);
+    gmres_start_kernel<K><<<d.n_cells, 256, 0, s>>>(d, g, N, r, params, first ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -335,15 +369,15 @@ int elementwise_grid(long long total, int num_sms)
 } // namespace
 
 cudaError_t batch_gmres_start(const BatchDev& d, const GmresDev& g, const double* N, const double* r,
-                              const pbe_batch_cell_params_t* params, cudaStream_t s)
+                              const pbe_batch_cell_params_t* params, bool first, cudaStream_t s)
 {
     switch (d.kernel < 0 ? 0 : d.kernel) {
-    case 0: return start_k<0>(d, g, N, r, params, s);
-    case 1: return start_k<1>(d, g, N, r, params, s);
-    case 2: return start_k<2>(d, g, N, r, params, s);
-    case 3: return start_k<3>(d, g, N, r, params, s);
-    case 4: return start_k<4>(d, g, N, r, params, s);
-    case 5: return start_k<5>(d, g, N, r, params, s);
+    case 0: return start_k<0>(d, g, N, r, params, first, s);
+    case 1: return start_k<1>(d, g, N, r, params, first, s);
+    case 2: return start_k<2>(d, g, N, r, params, first, s);
+    case 3: return start_k<3>(d, g, N, r, params, first, s);
+    case 4: return start_k<4>(d, g, N, r, params, first, s);
+    case 5: return start_k<5>(d, g, N, r, params, first, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -355,9 +389,16 @@ cudaError_t batch_gmres_arnoldi(const BatchDev& d, const GmresDev& g, int j, cud
 }
 
 cudaError_t batch_gmres_finish(const BatchDev& d, const GmresDev& g, double* x, double* resid,
-                               cudaStream_t s)
+                               bool acc, bool final, cudaStream_t s)
 {
-    gmres_finish_kernel<<<d.n_cells, 256, 0, s>>>(d, g, x, resid);
+    gmres_finish_kernel<<<d.n_cells, 256, 0, s>>>(d, g, x, resid, acc ? 1 : 0, final ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_gmres_restart(const BatchDev& d, const GmresDev& g, const double* r,
+                                const double* x, cudaStream_t s)
+{
+    gmres_restart_kernel<<<d.n_cells, 256, 0, s>>>(d, g, r, x);
     return cudaGetLastError();
 }
 

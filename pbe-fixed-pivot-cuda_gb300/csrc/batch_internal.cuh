@@ -153,8 +153,15 @@ struct GmresDev {
     int* done;       // [n_cells] solve ended (converged, breakdown or m steps)
     const double* gtc;   // [n_cells] gamma dt per cell (adaptive steps), or null: gt
     const int* skip;     // [n_cells] or null: cells whose solve is not run (x = 0)
+    // restarted solves: a cell whose residual after a cycle of m steps is above
+    // tol |r| starts another cycle on r - A x (up to `restarts` more)
+    double* R;       // [total] residual r - A x of the current solution
+    double* rnorm;   // [n_cells] |r| of the system (tol is relative to it)
+    double* last;    // [n_cells] |r - A x| / |r| after the cell's last cycle
+    int* conv;       // [n_cells] 1: no further cycle (within tol, r = 0, or skipped)
     long long total;
     int m;
+    int restarts;
     double gt;       // gamma dt
     double tol;      // a solve ends once |r - A x| <= tol |r| (0: after m steps or breakdown)
 };
@@ -187,11 +194,17 @@ cudaError_t batch_soa(const BatchDev& d, const double* src, double* dst, long lo
 // GMRES steps (batch_implicit.cu): start (preconditioner at N, v_0 = r/|r|),
 // Arnoldi step j (after W = J(N) Z), finish (x = P^-1 V y, resid = relative
 // least-squares residual per cell, may be null); elementwise helpers.
+// first: the first cycle of a solve (records |r|, clears conv); later cycles
+// run only the cells without conv. finish: acc adds to x (later cycles);
+// final folds each cell's last relative residual into resid (max).
+// restart: R = r - A x (W = J x on entry) for the cells without conv.
+cudaError_t batch_gmres_restart(const BatchDev& d, const GmresDev& g, const double* r,
+                                const double* x, cudaStream_t s);
 cudaError_t batch_gmres_start(const BatchDev& d, const GmresDev& g, const double* N, const double* r,
-                              const pbe_batch_cell_params_t* params, cudaStream_t s);
+                              const pbe_batch_cell_params_t* params, bool first, cudaStream_t s);
 cudaError_t batch_gmres_arnoldi(const BatchDev& d, const GmresDev& g, int j, cudaStream_t s);
 cudaError_t batch_gmres_finish(const BatchDev& d, const GmresDev& g, double* x, double* resid,
-                               cudaStream_t s);
+                               bool acc, bool final, cudaStream_t s);
 cudaError_t batch_lincomb(double* out, double a, const double* X, double b, const double* Y,
                           long long total, int num_sms, cudaStream_t s);
 cudaError_t batch_ros_update(double* N, double c1, const double* K1, double c2, const double* K2,

@@ -122,6 +122,7 @@ _SIGNATURES = {
     "pbe_batch_to_soa": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
     "pbe_batch_ros2": (_I, [_P, _P, _P, ctypes.c_double, _I, _I, _P, _P]),
     "pbe_batch_set_krylov_tol": (_I, [_P, ctypes.c_double]),
+    "pbe_batch_set_krylov_restarts": (_I, [_P, _I]),
     "pbe_daughter_table": (_I, [_I, _I, ctypes.c_double, ctypes.c_double, _P, _P, _I, _P]),
     "pbe_batch_tape_forward": (_I, [_P, _P, _P, ctypes.c_double, _I, _I, _P]),
     "pbe_batch_tape_backward": (_I, [_P, _P, _P, _P, _P]),

@@ -166,6 +166,11 @@ class BatchPlan:
         ros2_adaptive (0, the default: krylov_dim steps or an exact breakdown)."""
         return _lib.load().pbe_batch_set_krylov_tol(self._h, float(tol))
 
+    def set_krylov_restarts(self, restarts: int) -> int:
+        """Further GMRES cycles (on r - A x) for cells whose residual is above
+        the Krylov tolerance after krylov_dim steps (default 0)."""
+        return _lib.load().pbe_batch_set_krylov_restarts(self._h, int(restarts))
+
     def from_soa(self, soa, ld: int, N, stream=None) -> int:
         """N[off_c + i] = soa[i * ld + c] for the bins of every cell (mesh fields
         -> packed state)."""

@@ -249,3 +249,34 @@ def test_batch_rk4_single_term_plans_match_oracle(kernel, selection):
             ref = pyoracle.rk4_step(ref, x, dt, agg=agg, brk=brk)
         np.testing.assert_allclose(got[c], ref, rtol=1e-11, atol=1e-11 * np.abs(N[c]).max(),
                                    err_msg="k=%d sel=%d cell %d" % (kernel, selection, c))
+
+
+def test_config1_constant_kernel_rk4_follows_scott_and_the_oracle():
+    """The reference's CPU-runnable case: constant kernel beta0 = 1e-15 on
+    x_i = 1e-18 2^i (n = 256), N_i = N0 (x_i/x_m) e^(-x_i/x_m) dx_i/x_m,
+    1000 RK4 steps of dt = 1 s as one graph. Total number follows
+    Smoluchowski/Scott M0(t) = M0(0) / (1 + beta0 M0(0) t / 2)
+    (pbe_examples_utils.hpp:207-221) to 1e-9, and every bin follows the
+    oracle's 1000 rk4_step calls (1e-10 of the largest N)."""
+    import torch
+
+    n = 256
+    x = 1e-18 * np.power(2.0, np.arange(n, dtype=np.float64))
+    xm, N0, b0 = 4e-18, 1e12, 1e-15
+    dx = x * np.sqrt(2.0) - x / np.sqrt(2.0)
+    N = N0 * (x / xm) * np.exp(-x / xm) * dx / xm
+    params = pg.batch.cell_params(1, beta0=b0)
+    steps = 1000
+    with pg.BatchPlan([x], [n], [0], 0) as plan:
+        dN = t(N.copy())
+        assert plan.rk4(dN, t(params), 1.0, steps) == 0
+        torch.cuda.synchronize()
+        got = dN.cpu().numpy()
+    M0 = N.sum()
+    expect = M0 / (1.0 + b0 * M0 * steps / 2.0)
+    assert abs(got.sum() - expect) / expect < 1e-9
+    ref = N.copy()
+    agg = dict(kernel=0, beta0=b0)
+    for _ in range(steps):
+        ref = pyoracle.rk4_step(ref, x, 1.0, agg=agg)
+    np.testing.assert_allclose(got, ref, rtol=1e-9, atol=1e-10 * np.abs(ref).max())

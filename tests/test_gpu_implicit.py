@@ -286,3 +286,44 @@ def test_krylov_tolerance_ends_solves_early_within_tolerance():
         assert abs(int(st[c]) - s_o) <= 1 and abs(int(rj[c]) - r_o) <= 1, (c, st[c], rj[c], s_o, r_o)
         o = plan.offsets[c]
         assert np.abs(got[o:o + cell_n[c]] - ref).max() <= 1e-6 * (np.abs(ref).max() + 1e-300), c
+
+
+def test_krylov_restarts_reach_the_tolerance_with_a_small_dimension():
+    """Restarted GMRES: a ROS2 step (dt = 1 s, Brownian+shear + linear
+    breakage, n = 64) solved with a Krylov dimension too small for one cycle
+    (S0 = 1 s^-1 with m = 4: relative residual ~4e-4; S0 = 50 s^-1 with
+    m = 12: ~4e-6) reaches tol = 1e-12 within 10 restarts, and the step then
+    equals the oracle's dense-solve ROS2 step (relative 1e-11 and 1e-8). (With
+    m <= 8 at S0 = 50 restarted GMRES stagnates, as it may on non-normal
+    operators.) Both cells of the plan agree bit for bit; restart counts
+    outside [0, 1000] are rejected."""
+    torch = _torch()
+    n = 64
+    x = 1e-18 * 2.0 ** (np.arange(n) / 4)
+    N0 = pg.grids.lognormal_ic(x, 20, 1.0, 1e12)
+    t_q, bw_q = pg.quadrature.uniform(4)
+    dt = 1.0
+    for S0, m, bound in ((1.0, 4, 1e-11), (50.0, 12, 1e-8)):
+        prm = pg.batch.cell_params(2, beta_br=6.73e-18, beta_sh=66.67, S0=S0,
+                                   v_ref=float(x[n // 2]), alpha=1.0)
+        agg = dict(kernel=5, beta_br=6.73e-18, beta_sh=66.67)
+        brk = dict(t_q=t_q, bw_q=bw_q, selection=1, S0=S0, v_ref=float(x[n // 2]), alpha=1.0)
+        dense = pyoracle.ros2_step(N0.copy(), x, dt, agg, brk)
+        errs, res = [], []
+        with pg.BatchPlan([x], [n, n], [0, 0], 5, 1, t_q, bw_q) as plan:
+            assert plan.set_krylov_restarts(-1) == pg.ERR_INVALID_VALUE
+            assert plan.set_krylov_restarts(1001) == pg.ERR_INVALID_VALUE
+            for tol, restarts in ((0.0, 0), (1e-12, 10)):
+                assert plan.set_krylov_tol(tol) == 0
+                assert plan.set_krylov_restarts(restarts) == 0
+                dN = t(np.concatenate([N0, N0]))
+                resid = t(np.zeros(2))
+                assert plan.ros2(dN, t(prm), dt, 1, krylov_dim=m, resid=resid) == 0
+                torch.cuda.synchronize()
+                a = dN.cpu().numpy()
+                np.testing.assert_array_equal(a[:n].view(np.int64), a[n:].view(np.int64))
+                errs.append(np.abs(a[:n] - dense).max() / np.abs(dense).max())
+                res.append(float(resid.cpu().numpy().max()))
+        assert res[0] > 1e-7 and errs[0] > 1e-4 * bound, (S0, errs, res)   # one cycle is not enough
+        assert res[1] <= 1e-12, (S0, res)
+        assert errs[1] < bound, (S0, errs)
