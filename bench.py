@@ -752,9 +752,10 @@ def main():
         rhs.zero_()
         pg.check(pg.aggregation_rhs(n_dev, dx, rhs, ap, stream=stream, mode=mode), "aggregation")
         pg.check(pg.breakage_rhs(n_dev, dx, dt, db, rhs, bp, stream=stream, mode=mode), "breakage")
-    # aggregation: counter reset (memset), prep, pair kernel; breakage: prep +
-    # gather (gather mode) or one scatter kernel
-    launches_per_step = 3 + (2 if mode == pg.MODE_GATHER else 1)
+    # our kernels per step: aggregation prep + pair kernel; breakage prep +
+    # gather (gather mode) or one scatter kernel. (The aggregation call also
+    # enqueues one 32-byte cudaMemsetAsync of its counters, not counted.)
+    launches_per_step = 2 + (2 if mode == pg.MODE_GATHER else 1)
 
     clocks = ClockSampler(local)
     with torch.cuda.stream(stream):
@@ -886,6 +887,7 @@ def main():
         "e2e": {"value": round(e2e_value, 3), "unit": "evals/s",
                 "h2d_bytes_per_step": N_BINS * 8, "d2h_bytes_per_step": N_BINS * 8},
         "gpu_launches": launches_per_step * args.steps,
+        "memsets_per_step": 1,
         "clocks": clk,
     }
     if vjp_ms is not None:
