@@ -201,7 +201,12 @@ enum {
     PBE_BATCH_TUNE   = 1,  /* pick the tile group size per section-count class by timing
                               candidates on the device (results cached per process, and
                               in the file named by PBE_GB300_TUNE_CACHE when set)        */
-    PBE_BATCH_RETUNE = 2   /* like TUNE, ignoring cached results                          */
+    PBE_BATCH_RETUNE = 2,  /* like TUNE, ignoring cached results                          */
+    /* where the breakage term is gathered (bitwise the same result either way);
+     * default: by the pair tasks for plans of at most 2 x SM-count cells, by a
+     * per-cell prep CTA otherwise */
+    PBE_BATCH_BRK_PREP  = 4,   /* always by the per-cell prep CTA                        */
+    PBE_BATCH_BRK_TASKS = 8    /* always by the pair tasks, each for its own bins         */
 };
 
 /* Builds a plan. Returns 1 (InvalidValue) for inconsistent sizes, a cell with

@@ -456,6 +456,12 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     BatchDev& d = p->d;
     d.n_grids = n_grids; d.n_cells = n_cells; d.kernel = kernel; d.selection = selection;
     d.nq = p->nq; d.num_sms = p->num_sms;
+    // breakage gather in the pair tasks for plans of at most one wave of prep
+    // CTAs (measured: one n = 3840 cell 358 -> 233 us per RHS, 64 cells
+    // 1540 -> 1435 us; 1024 cells 20.84 -> 21.12 ms, so those keep the prep)
+    d.brk_tasks = (p->nq > 0 && n_cells <= 2 * p->num_sms) ? 1 : 0;
+    if (flags & PBE_BATCH_BRK_PREP) d.brk_tasks = 0;
+    if ((flags & PBE_BATCH_BRK_TASKS) && p->nq > 0) d.brk_tasks = 1;
     const size_t G = static_cast<size_t>(goff), C = static_cast<size_t>(off);
     BatchCellDev* dcells = nullptr;
     e = plan_alloc(p, &d.grids, static_cast<size_t>(n_grids));
@@ -868,6 +874,7 @@ cudaError_t jvp(pbe_batch_plan* p, const double* N, const double* v,
     if (e == cudaSuccess) e = batch_main(d1, v, prm, out, false, s);
     BatchDev d2 = d;
     d2.A = v;
+    d2.nobrk = 1;                          // breakage is linear: first pass only
     if (e == cudaSuccess) e = batch_jvp_prep(d, v, N, N, prm, false, s);
     if (e == cudaSuccess) e = batch_main(d2, N, prm, out, true, s);
     return e;
@@ -1192,6 +1199,9 @@ int pbe_batch_create(pbe_batch_t* plan, int n_grids, const int* grid_n, const do
 {
     if (!plan) return cudaErrorInvalidValue;
     *plan = nullptr;
+    if ((flags & ~(PBE_BATCH_TUNE | PBE_BATCH_RETUNE | PBE_BATCH_BRK_PREP | PBE_BATCH_BRK_TASKS)) ||
+        ((flags & PBE_BATCH_BRK_PREP) && (flags & PBE_BATCH_BRK_TASKS)))
+        return cudaErrorInvalidValue;
     cudaError_t e = validate(n_grids, grid_n, grid_x, n_cells, cell_n, cell_grid, kernel_type,
                              selection, n_quad, t_q, bw_q);
     if (e != cudaSuccess) return e;

@@ -55,7 +55,7 @@ struct BatchDev {
     double* Hj;     // j-side x N factor: beta x N (beta0, beta_sh)
     double* Hk;     // x N (Sum, Product)
     double* SN;     // S(x) N, 0 where the breakage guard skips the bin
-    double* Bk;     // breakage term of the stage (gathered by the prep kernel)
+    double* Bk;     // breakage term of the stage (gathered by the prep kernel unless brk_tasks)
     double* k;      // stage derivative (RK4)
     double* kacc;   // k1 + 2 k2 + 2 k3 (+ k4)
     // Jacobian-vector passes (batch_jvp.cu): the j-side vector of the pass,
@@ -91,6 +91,14 @@ struct BatchDev {
     // computed once at its start by batch_sel; null: the kernels evaluate the
     // selection function per bin
     const double* Sx;
+    // where the breakage term is gathered from SN: 0 by the prep kernel (one
+    // CTA per cell, into Bk), 1 by the pair tasks in their epilogues (their
+    // own bins). Plans of few cells take 1, so that one large cell's prep
+    // does not hold up the launch; many cells balance the prep CTAs anyway.
+    int brk_tasks;
+    // 1: no breakage term in this pass (the second pass of a Jacobian-vector
+    // product)
+    int nobrk;
 };
 
 // Scratch of the batched VJP (batch_vjp.cu).

@@ -8,17 +8,18 @@
 // Per RHS evaluation (two launches):
 //  * batch_prep_kernel, one CTA per cell: the RK4 stage update of the cell's
 //    state, the stage arrays (j-side factors carrying the cell's kernel
-//    coefficients, S(x) N for breakage), the five death moments, the sum of
-//    the cell's clipped pairs and the whole breakage term (a gather per bin).
+//    coefficients, S(x) N for breakage), the five death moments and the sum
+//    of the cell's clipped pairs.
 //  * batch_main_kernel, persistent: CTAs pull "bundles" from an atomic
 //    counter, largest first. A bundle holds 256/T tile tasks (cell, first bin)
 //    that run side by side on groups of T threads; T is chosen per section
 //    count class by the plan (autotuned or by rule), so a 64-section cell is
 //    not spread over 256 threads. A task runs the shared tile body
-//    (agg_tile.cuh), adds the prep kernel's clip and breakage terms and writes
-//    its bins once: no atomics, and a fixed summation order for a fixed
-//    schedule. Keeping the latency-bound gathers out of this kernel leaves its
-//    CTAs on the FP64 pipe.
+//    (agg_tile.cuh), gathers the breakage term of its bins from S N (a few
+//    fragments per bin and quadrature point), adds the prep kernel's clip sum
+//    and writes its bins once: no atomics, and a fixed summation order for a
+//    fixed schedule. The gather is spread over all tasks instead of one CTA
+//    per cell, so a large cell's prep does not hold up the launch.
 // =============================================================================
 #include "batch_internal.cuh"
 #include "agg_tile.cuh"
@@ -218,11 +219,11 @@ __device__ double cell_clip(const AggCellView& v, const TileGroup& G)
     return acc;
 }
 
-// Breakage of every bin of a cell (one CTA): bin i takes the hi-shares of the
-// fragments bracketed at i-1 and the lo-shares of those at i (bin 0 also the
-// fragments clipped below x[0]), minus S_i N_i. A warp covers 32/nqp bins,
-// nqp = the quadrature points rounded up to a power of two (<= 32) lanes per
-// bin, summed in a fixed butterfly.
+// Breakage of every bin of a cell (one CTA, prep kernels when !brk_tasks): bin
+// i takes the hi-shares of the fragments bracketed at i-1 and the lo-shares of
+// those at i (bin 0 also the fragments clipped below x[0]), minus S_i N_i. A
+// warp covers 32/nqp bins, nqp = the quadrature points rounded up to a power
+// of two (<= 32) lanes per bin, summed in a fixed butterfly.
 __device__ void cell_breakage(const BatchDev& d, const BatchGridDev& gd, const double* SN,
                               double* Bk, int n)
 {
@@ -252,11 +253,46 @@ __device__ void cell_breakage(const BatchDev& d, const BatchGridDev& gd, const d
     }
 }
 
+// The same breakage term for the bins I .. I+W-1 of a cell (those in
+// [0, n)), gathered by a task's group into out[0 .. W) (brk_tasks), with the
+// same lanes per bin, loops and butterfly, so the sums are bitwise those of
+// cell_breakage.
+__device__ void tile_breakage(const BatchDev& d, const BatchGridDev& gd, const double* SN, int n,
+                              int I, double* out, const TileGroup& G)
+{
+    int nqp = 1;
+    while (nqp < d.nq && nqp < 32) nqp <<= 1;
+    const int per_warp = 32 / nqp;
+    const int nw = G.T >> 5, w = G.lane >> 5, l = G.lane & 31;
+    const int ng = gd.n;
+    for (int base = w * per_warp; base < W; base += nw * per_warp) {   // uniform per warp
+        const int t = base + l / nqp;
+        const int i = I + t;
+        const bool in = t < W && i >= 0 && i < n;
+        double acc = 0.0;
+        if (in) {
+            for (int q = l % nqp; q < d.nq; q += nqp) {
+                const int* fq = d.bfirst + gd.foff + q * (ng + 2);
+                const double* wl = d.bwlo + gd.woff + q * ng;
+                const double* wh = d.bwhi + gd.woff + q * ng;
+                const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
+                const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
+                const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
+                if (i == 0) { for (int j = 0; j < fb; ++j) acc = fma(SN[j], wl[j], acc); }
+                else        { for (int j = fa; j < fb; ++j) acc = fma(SN[j], wh[j], acc); }
+                for (int j = fb; j < fc; ++j) acc = fma(SN[j], wl[j], acc);
+            }
+        }
+        for (int o = nqp >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (t < W && (l % nqp) == 0) out[t] = in ? acc - SN[i] : 0.0;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Stage prep: one CTA per cell. Pass 1 (per bin): the stage update, the stage
-// arrays and the moment partials. Pass 2 (after a block barrier, so the whole
-// cell's arrays are visible): the moments, the cell's clipped-pair sum
-// (mom[5]) and its breakage term (Bk), which the persistent kernel then adds.
+// arrays (S N for the breakage gather of the pair tasks) and the moment
+// partials. Pass 2 (after a block barrier, so the whole cell's arrays are
+// visible): the moments and the cell's clipped-pair sum (mom[5]).
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
@@ -336,7 +372,7 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
         const double clip = block_sum(cell_clip<K>(v, G), sh);
         if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + 5] = clip;
     }
-    if (d.nq > 0) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
+    if (d.nq > 0 && !d.brk_tasks) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
 }
 
 // Hand-over of bin `bin` of a cell (the first bin of tile slot `slot`): its
@@ -362,10 +398,12 @@ __device__ __forceinline__ void batch_first_done(const BatchDev& d, double* out,
 // with the j side from a and the k side from b. This prep builds the j-side
 // arrays from a (coefficient-scaled, and unscaled for the generic path), the
 // k-side x b, the moments of a (death b_i sum_k beta_ik a_k), the clipped
-// pairs' sum of T(a, b), and the breakage term: the breakage RHS is linear
+// pairs' sum of T(a, b), and the breakage input: the breakage RHS is linear
 // in N wherever its guard passes, so with brk its Jacobian-vector product
-// S_j b_j deposited as the RHS deposits S_j N_j, for the bins whose G_j (the
-// state) passes the guard S_j != 0 && G_j > 2.2e-308; without brk, zero.
+// deposits S_j b_j as the RHS deposits S_j N_j, for the bins whose G_j (the
+// state) passes the guard S_j != 0 && G_j > 2.2e-308 (SN = S b there, 0
+// elsewhere; gathered here or by the pair tasks, as for the RHS); the pass
+// without brk runs its pair kernel with nobrk.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
@@ -436,13 +474,8 @@ batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __
         const double clip = block_sum(cell_clip<K>(v, G), sh);
         if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + 5] = clip;
     }
-    if (d.nq > 0) {
-        if (brk) {
-            cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
-        } else {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) d.Bk[off + i] = 0.0;
-        }
-    }
+    // first pass only (the second runs with nobrk)
+    if (d.nq > 0 && !d.brk_tasks && brk) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
 }
 
 template <int K>
@@ -517,6 +550,11 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
         for (int q = 0; q < 5; ++q) v.M[q] = sm.cinfo[G.g][q];
         v.b0 = sm.cinfo[G.g][5]; v.bbr = sm.cinfo[G.g][6]; v.bsh = sm.cinfo[G.g][7];
     }
+    const bool brk = d.nq > 0 && !d.nobrk;
+    if (brk && d.brk_tasks) {
+        tile_breakage(d, gd, d.SN + cd.off, n, I, sm.extra[G.g], G);
+        G.sync();
+    }
     if (G.lane < W) {
         const int i = I + G.lane;
         if (i >= 0) {
@@ -526,7 +564,7 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                 if (i == n - 1) birth += d.mom[c * 8 + 5];     // clipped pairs (prep)
                 val = birth - agg_death<K>(v, i);
             }
-            if (d.nq > 0) val += d.Bk[cd.off + i];             // breakage (prep)
+            if (brk) val += d.brk_tasks ? sm.extra[G.g][G.lane] : d.Bk[cd.off + i];   // breakage
             if (agg && G.lane == 0 && I >= 1) {
                 // the w-part of slot I-1 comes from the tile below
                 d.tfirst[cd.tile_off + tile] = val;

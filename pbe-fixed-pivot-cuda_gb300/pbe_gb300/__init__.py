@@ -23,6 +23,8 @@ from ._lib import (  # noqa: F401
     SEL_LINEAR,
     SEL_POWERLAW,
     SEL_THRESHOLD,
+    BATCH_BRK_PREP,
+    BATCH_BRK_TASKS,
     BATCH_RETUNE,
     BATCH_TUNE,
     DEATH_DMMA,

@@ -80,6 +80,7 @@ class BatchCellParams(ctypes.Structure):
 
 
 BATCH_TUNE, BATCH_RETUNE = 1, 2
+BATCH_BRK_PREP, BATCH_BRK_TASKS = 4, 8
 DEATH_MOMENTS, DEATH_DMMA = 0, 1
 DAUGHTER_SYMMETRIC, DAUGHTER_EROSION, DAUGHTER_UNIFORM, DAUGHTER_POWERLAW = range(4)
 

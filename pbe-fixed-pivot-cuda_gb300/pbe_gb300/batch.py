@@ -16,7 +16,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import BATCH_RETUNE, BATCH_TUNE, PbeError
+from ._lib import BATCH_BRK_PREP, BATCH_BRK_TASKS, BATCH_RETUNE, BATCH_TUNE, PbeError
 from .rhs import _ptr, _stream
 
 PARAM_FIELDS = ("beta0", "beta_br", "beta_sh", "S0", "v_ref", "alpha", "v_min", "reserved")
@@ -63,7 +63,8 @@ class BatchPlan:
     def __init__(self, grids: Sequence[np.ndarray], cell_n: Sequence[int],
                  cell_grid: Sequence[int], kernel: int, selection: int = -1,
                  t_q: Optional[np.ndarray] = None, bw_q: Optional[np.ndarray] = None,
-                 tune: bool = False, retune: bool = False, stream=None):
+                 tune: bool = False, retune: bool = False, stream=None,
+                 breakage_gather: Optional[str] = None):
         lib = _lib.load()
         grid_n = np.ascontiguousarray([len(g) for g in grids], dtype=np.int32)
         grid_x = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float64) for g in grids]))
@@ -76,6 +77,10 @@ class BatchPlan:
             bw = np.ascontiguousarray(bw_q, dtype=np.float64)
             nq = len(tq)
         flags = (BATCH_TUNE if tune else 0) | (BATCH_RETUNE if retune else 0)
+        if breakage_gather is not None:
+            # "prep" or "tasks": where the breakage term is gathered (the plan
+            # picks by its cell count when None)
+            flags |= {"prep": BATCH_BRK_PREP, "tasks": BATCH_BRK_TASKS}[breakage_gather]
         h = ctypes.c_void_p()
         code = lib.pbe_batch_create(
             ctypes.byref(h), len(grid_n), grid_n.ctypes.data, grid_x.ctypes.data, len(cn),

@@ -280,3 +280,46 @@ def test_config1_constant_kernel_rk4_follows_scott_and_the_oracle():
     for _ in range(steps):
         ref = pyoracle.rk4_step(ref, x, 1.0, agg=agg)
     np.testing.assert_allclose(got, ref, rtol=1e-9, atol=1e-10 * np.abs(ref).max())
+
+
+def test_breakage_gather_modes_are_bitwise_equal():
+    """The breakage term gathered by the per-cell prep CTA or by the pair
+    tasks (for their own bins) uses the same lanes, loops and butterfly: RHS,
+    Jacobian-vector product and RK4 steps agree bit for bit, with lag chunks
+    (few tiles) and without, on geometric and generic grids. Conflicting or
+    unknown plan flags are rejected."""
+    torch = _torch()
+    rng = np.random.default_rng(77)
+    t_q, bw_q = DAUGHTER
+    for n_cells in (24, 160):            # lag chunks (few tiles), then none
+        grids, cell_n, cell_grid, N, params = mixed_batch(rng, 5, 2, n_cells=n_cells, n_max=400)
+        N = [np.abs(Nc) for Nc in N]
+        v = [rng.standard_normal(len(Nc)) * Nc for Nc in N]
+        outs = {}
+        for mode in ("prep", "tasks"):
+            with pg.BatchPlan(grids, cell_n, cell_grid, 5, 2, t_q, bw_q,
+                              breakage_gather=mode) as plan:
+                dN, dv, dp = t(np.concatenate(N)), t(np.concatenate(v)), t(params)
+                r = torch.zeros_like(dN)
+                jv = torch.zeros_like(dN)
+                assert plan.rhs(dN, r, dp) == 0
+                assert plan.jvp(dN, dv, jv, dp) == 0
+                Y = dN.clone()
+                assert plan.rk4(Y, dp, 0.25, 3) == 0
+                torch.cuda.synchronize()
+                outs[mode] = [a.cpu().numpy() for a in (r, jv, Y)]
+        for a, b in zip(outs["prep"], outs["tasks"]):
+            np.testing.assert_array_equal(a.view(np.int64), b.view(np.int64))
+    lib = pg.load()
+    import ctypes
+
+    h = ctypes.c_void_p()
+    g = np.ascontiguousarray(grids[0], dtype=np.float64)
+    gn = np.array([len(g)], dtype=np.int32)
+    cn = np.array([len(g)], dtype=np.int32)
+    cg = np.zeros(1, dtype=np.int32)
+    for flags in (pg.BATCH_BRK_PREP | pg.BATCH_BRK_TASKS, 64):
+        code = lib.pbe_batch_create(ctypes.byref(h), 1, gn.ctypes.data, g.ctypes.data, 1,
+                                    cn.ctypes.data, cg.ctypes.data, 5, -1, 0, None, None,
+                                    flags, None)
+        assert code == pg.ERR_INVALID_VALUE
