@@ -550,6 +550,8 @@ def classes_section(dev, stream):
 def profile_case(name: str) -> None:
     """A few launches of one kernel family on a mid-size case, for ncu:
       batched : 1024 cells of the batched workload (seed 2026), 4 batched RHS
+      batched_small: one cell of n = 3840 (x_i = 1e-21 2^(i/128), the
+                form of the batched workload) through the batched plan, 4 RHS
       death   : the 512-cell size-class workload, 3 DMMA and 3 moment death calls
       vjp     : the n = 16384 workload, 3 aggregation + breakage VJPs
       breakage: the n = 16384 workload, 3 breakage RHS calls in each mode
@@ -565,6 +567,18 @@ def profile_case(name: str) -> None:
         with pg.BatchPlan(cfg["grids"], cfg["cell_n"], cfg["cell_grid"], pg.AGG_BROWNIAN_SHEAR,
                           pg.SEL_POWERLAW, cfg["t_q"], cfg["bw_q"]) as plan:
             dN, P = torch.tensor(cfg["N"], **f64), torch.tensor(cfg["params"], **f64)
+            out = torch.zeros(plan.total, **f64)
+            for _ in range(4):
+                pg.check(plan.rhs(dN, out, P), "batch rhs")
+    elif name == "batched_small":
+        cfg = pg.grids.config_batched_cells(n_cells=1)
+        x = pg.grids.geometric_pow2(3840, 1e-21, 128.0)
+        N = pg.grids.lognormal_ic(x, 1280, 1.0, 1e13, cut=5.0)
+        with pg.BatchPlan([x], [3840], [0], pg.AGG_BROWNIAN_SHEAR, pg.SEL_POWERLAW,
+                          cfg["t_q"], cfg["bw_q"]) as plan:
+            prm = pg.batch.cell_params(1, beta0=0.0, beta_br=6.73e-18, beta_sh=4 * 50 / 3,
+                                       S0=1e-3, v_ref=float(x[1920]), alpha=1.0)
+            dN, P = torch.tensor(N, **f64), torch.tensor(prm, **f64)
             out = torch.zeros(plan.total, **f64)
             for _ in range(4):
                 pg.check(plan.rhs(dN, out, P), "batch rhs")
@@ -703,7 +717,8 @@ def reference_kernels_section(dev, stream, dN, dx, dt, db, rhs, ap, bp, flush, s
 
 def main():
     ap_ = argparse.ArgumentParser()
-    ap_.add_argument("--profile-case", choices=["batched", "death", "adjoint", "vjp", "breakage"],
+    ap_.add_argument("--profile-case", choices=["batched", "batched_small", "death", "adjoint",
+                                                "vjp", "breakage"],
                      help="run a few launches of one kernel family (for ncu) and exit")
     ap_.add_argument("--gpus", type=int, default=1)
     ap_.add_argument("--steps", type=int, default=200)

@@ -559,10 +559,11 @@ cudaError_t check_plan(pbe_batch_plan* p)
     return dev == p->device ? cudaSuccess : cudaErrorInvalidDevice;
 }
 
-// Selection function of every cell bin for the parameters of one
-// multi-stage call, computed once on s at the call's start (for the power law
-// one pow per bin instead of one per bin and stage): the plan's kernels read it
-// while the SelScope of the call is alive. Plans without breakage: nothing.
+// Selection function of every cell bin for the parameters of one call,
+// computed once on s at the call's start by a kernel over all bins (for the
+// power law one pow per bin instead of one per bin and stage, spread over
+// every SM instead of one CTA per cell): the plan's kernels read it while the
+// SelScope of the call is alive. Plans without breakage: nothing.
 struct SelScope {
     pbe_batch_plan* p;
     explicit SelScope(pbe_batch_plan* q) : p(q) {}
@@ -575,7 +576,7 @@ cudaError_t sel_cache(pbe_batch_plan* p, const pbe_batch_cell_params_t* prm, cud
 {
     p->d.Sx = nullptr;
     if (p->selection < 0 || p->nq <= 0 || !p->sx) return cudaSuccess;
-    cudaError_t e = batch_sel(p->d, prm, p->sx, s);   // (sx: allocated with the plan)
+    cudaError_t e = batch_sel(p->d, prm, p->sx, p->total, s);   // (sx: allocated with the plan)
     if (e == cudaSuccess) p->d.Sx = p->sx;
     return e;
 }
@@ -1234,7 +1235,10 @@ int pbe_batch_rhs(pbe_batch_t plan, const double* N, double* rhs,
     if (e != cudaSuccess) return e;
     if (!N || !rhs || !params) return cudaErrorInvalidDevicePointer;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    e = batch_prep(plan->d, const_cast<double*>(N), params, kStageRhs, 0.0, 0.0, s);
+    SelScope scope(plan);
+    e = sel_cache(plan, params, s);
+    if (e == cudaSuccess)
+        e = batch_prep(plan->d, const_cast<double*>(N), params, kStageRhs, 0.0, 0.0, s);
     if (e == cudaSuccess) e = batch_main(plan->d, N, params, rhs, true, s);
     return e;
 }
@@ -1296,6 +1300,9 @@ int pbe_batch_rhs_vjp(pbe_batch_t plan, const double* N, const double* lambda, d
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     e = vjp_setup(plan, s);
     if (e != cudaSuccess) return e;
+    SelScope scope(plan);
+    e = sel_cache(plan, params, s);
+    if (e != cudaSuccess) return e;
     return batch_vjp(plan->d, plan->vd, N, lambda, gN, gparams, params, s);
 }
 
@@ -1340,7 +1347,11 @@ int pbe_batch_jvp(pbe_batch_t plan, const double* N, const double* v,
     cudaError_t e = check_plan(plan);
     if (e != cudaSuccess) return e;
     if (!N || !v || !params || !out) return cudaErrorInvalidDevicePointer;
-    return jvp(plan, N, v, params, out, static_cast<cudaStream_t>(stream));
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    SelScope scope(plan);
+    e = sel_cache(plan, params, s);
+    if (e != cudaSuccess) return e;
+    return jvp(plan, N, v, params, out, s);
 }
 
 int pbe_batch_ros2(pbe_batch_t plan, double* N, const pbe_batch_cell_params_t* params, double dt,

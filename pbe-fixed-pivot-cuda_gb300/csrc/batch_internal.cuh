@@ -87,9 +87,9 @@ struct BatchDev {
     // change during a launch, so all tasks of a cell agree.
     const int* skip;
     // [total] or null: S(x_i) of every cell bin for the parameters of the
-    // current multi-stage call (RK4 steps, embedded RK, Rosenbrock, the tape),
-    // computed once at its start by batch_sel; null: the kernels evaluate the
-    // selection function per bin
+    // current call (an RHS, a Jacobian-vector product, RK4 steps, embedded
+    // RK, Rosenbrock, the tape), computed once at its start by batch_sel;
+    // null: the kernels evaluate the selection function per bin
     const double* Sx;
     // where the breakage term is gathered from SN: 0 by the prep kernel (one
     // CTA per cell, into Bk), 1 by the pair tasks in their epilogues (their
@@ -232,9 +232,10 @@ cudaError_t batch_ros2_control(const BatchDev& d, double* N, const double* K1, c
 // j side from A, k side from B, breakage (brk) as the product of its Jacobian
 // at the state G with B, else zero. Followed by batch_main with Y = B and a
 // copy of d whose A = A.
-// Sx[off_c + i] = S(x_i) of cell c's parameters, every cell (one CTA per cell).
+// Sx[off_c + i] = S(x_i) of cell c's parameters, every bin of the plan
+// (total = the packed length).
 cudaError_t batch_sel(const BatchDev& d, const pbe_batch_cell_params_t* params, double* Sx,
-                      cudaStream_t s);
+                      long long total, cudaStream_t s);
 cudaError_t batch_jvp_prep(const BatchDev& d, const double* A, const double* B, const double* G,
                            const pbe_batch_cell_params_t* params, bool brk, cudaStream_t s);
 // Persistent RHS kernel over the plan's bundles: out (+)= RHS(Y) for every cell.

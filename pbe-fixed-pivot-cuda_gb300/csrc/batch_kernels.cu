@@ -166,17 +166,25 @@ cell_stage_kernel(double* N, const double* k, double* kacc, double* Y, int n, in
     if (i < n) stage_update(stage, N, k, kacc, Y, i, c, dt6);
 }
 
-// Selection function of every cell bin for the given parameters (one CTA per
-// cell): evaluated once per multi-stage call instead of once per stage.
+// Selection function of every cell bin for the given parameters: one thread
+// per packed bin over the whole plan (its cell found by bisection of the
+// cells' offsets), so that a large cell's transcendentals spread over all
+// SMs instead of one CTA's; evaluated once per call instead of per stage.
 __global__ void __launch_bounds__(256)
 batch_sel_kernel(BatchDev d, const pbe_batch_cell_params_t* __restrict__ params,
-                 double* __restrict__ Sx)
+                 double* __restrict__ Sx, long long total)
 {
-    const BatchCellDev cd = d.cells[blockIdx.x];
-    const pbe_batch_cell_params_t P = params[blockIdx.x];
-    const double* x = d.gx + d.grids[cd.grid].off;
-    for (int i = threadIdx.x; i < cd.n; i += blockDim.x)
-        Sx[cd.off + i] = sel_value(d.selection, x[i], P.S0, P.v_ref, P.alpha, P.v_min);
+    for (long long e = blockIdx.x * 256LL + threadIdx.x; e < total; e += 256LL * gridDim.x) {
+        int lo = 0, hi = d.n_cells;          // cells[lo].off <= e < cells[hi].off
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (d.cells[mid].off <= e) lo = mid; else hi = mid;
+        }
+        const BatchCellDev cd = d.cells[lo];
+        const pbe_batch_cell_params_t P = params[lo];
+        const double* x = d.gx + d.grids[cd.grid].off;
+        Sx[e] = sel_value(d.selection, x[e - cd.off], P.S0, P.v_ref, P.alpha, P.v_min);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -740,10 +748,11 @@ cudaError_t batch_prep(const BatchDev& d, double* N, const pbe_batch_cell_params
 }
 
 cudaError_t batch_sel(const BatchDev& d, const pbe_batch_cell_params_t* params, double* Sx,
-                      cudaStream_t s)
+                      long long total, cudaStream_t s)
 {
-    if (d.n_cells <= 0 || d.selection < 0) return cudaErrorInvalidValue;
-    batch_sel_kernel<<<d.n_cells, 256, 0, s>>>(d, params, Sx);
+    if (d.n_cells <= 0 || d.selection < 0 || total <= 0) return cudaErrorInvalidValue;
+    const long long b = (total + 255) / 256, cap = 16LL * (d.num_sms > 0 ? d.num_sms : 1);
+    batch_sel_kernel<<<static_cast<int>(b < cap ? b : cap), 256, 0, s>>>(d, params, Sx, total);
     return cudaGetLastError();
 }
 
