@@ -459,9 +459,10 @@ cudaError_t create(pbe_batch_plan* p, int n_grids, const int* grid_n, const doub
     // breakage gather in the pair tasks for plans of at most one wave of prep
     // CTAs (measured: one n = 3840 cell 358 -> 233 us per RHS, 64 cells
     // 1540 -> 1435 us; 1024 cells 20.84 -> 21.12 ms, so those keep the prep)
-    d.brk_tasks = (p->nq > 0 && n_cells <= 2 * p->num_sms) ? 1 : 0;
-    if (flags & PBE_BATCH_BRK_PREP) d.brk_tasks = 0;
-    if ((flags & PBE_BATCH_BRK_TASKS) && p->nq > 0) d.brk_tasks = 1;
+    bool tasks = p->nq > 0 && n_cells <= 2 * p->num_sms;
+    if (flags & PBE_BATCH_BRK_PREP) tasks = false;
+    if ((flags & PBE_BATCH_BRK_TASKS) && p->nq > 0) tasks = true;
+    d.brk = tasks ? kBrkTasks : 0;
     const size_t G = static_cast<size_t>(goff), C = static_cast<size_t>(off);
     BatchCellDev* dcells = nullptr;
     e = plan_alloc(p, &d.grids, static_cast<size_t>(n_grids));
@@ -875,7 +876,7 @@ cudaError_t jvp(pbe_batch_plan* p, const double* N, const double* v,
     if (e == cudaSuccess) e = batch_main(d1, v, prm, out, false, s);
     BatchDev d2 = d;
     d2.A = v;
-    d2.nobrk = 1;                          // breakage is linear: first pass only
+    d2.brk |= kBrkNone;                    // breakage is linear: first pass only
     if (e == cudaSuccess) e = batch_jvp_prep(d, v, N, N, prm, false, s);
     if (e == cudaSuccess) e = batch_main(d2, N, prm, out, true, s);
     return e;

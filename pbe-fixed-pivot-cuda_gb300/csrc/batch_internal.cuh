@@ -41,6 +41,14 @@ struct BatchDev {
     int kernel;        // aggregation kernel type, -1 = no aggregation
     int selection;     // breakage selection, -1 = no breakage
     int nq;            // quadrature points (0 = no breakage)
+    // breakage gather (in the padding after nq, so the struct keeps its size):
+    // bit kBrkTasks: gathered from SN by the pair tasks in their epilogues
+    // (their own bins) instead of by the prep kernel (one CTA per cell, into
+    // Bk); plans of few cells take it, so that one large cell's prep does not
+    // hold up the launch, while many cells balance the prep CTAs anyway.
+    // bit kBrkNone: no breakage term in this pass (the second pass of a
+    // Jacobian-vector product).
+    int brk;
     // per grid bin (packed by BatchGridDev::off)
     double* gx; double* ga; double* gia; double* ginv_dx; double* gBd; double* gSd; int* gLd;
     double* gSl;    // shear factor of lag d seen from the larger member: (1 + rho)^3 x_0 / x_d
@@ -55,7 +63,7 @@ struct BatchDev {
     double* Hj;     // j-side x N factor: beta x N (beta0, beta_sh)
     double* Hk;     // x N (Sum, Product)
     double* SN;     // S(x) N, 0 where the breakage guard skips the bin
-    double* Bk;     // breakage term of the stage (gathered by the prep kernel unless brk_tasks)
+    double* Bk;     // breakage term of the stage (gathered by the prep kernel, brk without kBrkTasks)
     double* k;      // stage derivative (RK4)
     double* kacc;   // k1 + 2 k2 + 2 k3 (+ k4)
     // Jacobian-vector passes (batch_jvp.cu): the j-side vector of the pass,
@@ -91,15 +99,9 @@ struct BatchDev {
     // RK, Rosenbrock, the tape), computed once at its start by batch_sel;
     // null: the kernels evaluate the selection function per bin
     const double* Sx;
-    // where the breakage term is gathered from SN: 0 by the prep kernel (one
-    // CTA per cell, into Bk), 1 by the pair tasks in their epilogues (their
-    // own bins). Plans of few cells take 1, so that one large cell's prep
-    // does not hold up the launch; many cells balance the prep CTAs anyway.
-    int brk_tasks;
-    // 1: no breakage term in this pass (the second pass of a Jacobian-vector
-    // product)
-    int nobrk;
 };
+constexpr int kBrkTasks = 1;
+constexpr int kBrkNone = 2;
 
 // Scratch of the batched VJP (batch_vjp.cu).
 struct BatchVjpDev {

@@ -227,7 +227,7 @@ __device__ double cell_clip(const AggCellView& v, const TileGroup& G)
     return acc;
 }
 
-// Breakage of every bin of a cell (one CTA, prep kernels when !brk_tasks): bin
+// Breakage of every bin of a cell (one CTA, prep kernels without kBrkTasks): bin
 // i takes the hi-shares of the fragments bracketed at i-1 and the lo-shares of
 // those at i (bin 0 also the fragments clipped below x[0]), minus S_i N_i. A
 // warp covers 32/nqp bins, nqp = the quadrature points rounded up to a power
@@ -262,7 +262,7 @@ __device__ void cell_breakage(const BatchDev& d, const BatchGridDev& gd, const d
 }
 
 // The same breakage term for the bins I .. I+W-1 of a cell (those in
-// [0, n)), gathered by a task's group into out[0 .. W) (brk_tasks), with the
+// [0, n)), gathered by a task's group into out[0 .. W) (kBrkTasks), with the
 // same lanes per bin, loops and butterfly, so the sums are bitwise those of
 // cell_breakage.
 __device__ void tile_breakage(const BatchDev& d, const BatchGridDev& gd, const double* SN, int n,
@@ -380,7 +380,7 @@ batch_prep_kernel(BatchDev d, double* N, const pbe_batch_cell_params_t* __restri
         const double clip = block_sum(cell_clip<K>(v, G), sh);
         if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + 5] = clip;
     }
-    if (d.nq > 0 && !d.brk_tasks) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
+    if (d.nq > 0 && !(d.brk & kBrkTasks)) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
 }
 
 // Hand-over of bin `bin` of a cell (the first bin of tile slot `slot`): its
@@ -411,7 +411,7 @@ __device__ __forceinline__ void batch_first_done(const BatchDev& d, double* out,
 // deposits S_j b_j as the RHS deposits S_j N_j, for the bins whose G_j (the
 // state) passes the guard S_j != 0 && G_j > 2.2e-308 (SN = S b there, 0
 // elsewhere; gathered here or by the pair tasks, as for the RHS); the pass
-// without brk runs its pair kernel with nobrk.
+// without brk runs its pair kernel with kBrkNone.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
@@ -482,8 +482,8 @@ batch_jvp_prep_kernel(BatchDev d, const double* __restrict__ A, const double* __
         const double clip = block_sum(cell_clip<K>(v, G), sh);
         if (threadIdx.x == 0) d.mom[blockIdx.x * 8 + 5] = clip;
     }
-    // first pass only (the second runs with nobrk)
-    if (d.nq > 0 && !d.brk_tasks && brk) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
+    // first pass only (the second runs with kBrkNone)
+    if (d.nq > 0 && !(d.brk & kBrkTasks) && brk) cell_breakage(d, gd, d.SN + off, d.Bk + off, n);
 }
 
 template <int K>
@@ -558,8 +558,9 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
         for (int q = 0; q < 5; ++q) v.M[q] = sm.cinfo[G.g][q];
         v.b0 = sm.cinfo[G.g][5]; v.bbr = sm.cinfo[G.g][6]; v.bsh = sm.cinfo[G.g][7];
     }
-    const bool brk = d.nq > 0 && !d.nobrk;
-    if (brk && d.brk_tasks) {
+    const bool brk = d.nq > 0 && !(d.brk & kBrkNone);
+    const bool brk_tasks = (d.brk & kBrkTasks) != 0;
+    if (brk && brk_tasks) {
         tile_breakage(d, gd, d.SN + cd.off, n, I, sm.extra[G.g], G);
         G.sync();
     }
@@ -572,7 +573,7 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
                 if (i == n - 1) birth += d.mom[c * 8 + 5];     // clipped pairs (prep)
                 val = birth - agg_death<K>(v, i);
             }
-            if (brk) val += d.brk_tasks ? sm.extra[G.g][G.lane] : d.Bk[cd.off + i];   // breakage
+            if (brk) val += brk_tasks ? sm.extra[G.g][G.lane] : d.Bk[cd.off + i];   // breakage
             if (agg && G.lane == 0 && I >= 1) {
                 // the w-part of slot I-1 comes from the tile below
                 d.tfirst[cd.tile_off + tile] = val;
