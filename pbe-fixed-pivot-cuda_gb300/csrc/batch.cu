@@ -54,6 +54,8 @@ struct pbe_batch_plan {
     int4* d_death_items = nullptr;
     int* d_gcells = nullptr;
     int n_death_items = -1;
+    int death_split = 1;               // k slices of the death GEMM
+    double* death_part = nullptr;      // [death_split * total] slice partials
     // batched VJP (set up on first use)
     bool vjp_ready = false;
     pbe_gb300::BatchVjpDev vd{};
@@ -1181,9 +1183,24 @@ cudaError_t death_items(pbe_batch_plan* p, cudaStream_t s)
         e = cudaMemcpyAsync(dg, gcells.data(), gcells.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
+    // k slices so that the GEMM has about 4 CTAs per SM (each CTA's slice
+    // still spans >= 256 of the k range)
+    int kmax = 0;
+    for (int c = 0; c < p->n_cells; ++c) kmax = std::max(kmax, p->cell_n[c]);
+    const int want = items.empty() ? 1
+        : static_cast<int>((4LL * p->num_sms + static_cast<long long>(items.size()) - 1) /
+                           static_cast<long long>(items.size()));
+    const int split = std::max(1, std::min({want, 16, (2 * kmax) / 256}));
+    double* part = nullptr;
+    if (split > 1) {
+        e = plan_alloc(p, &part, static_cast<size_t>(split) * static_cast<size_t>(p->total));
+        if (e != cudaSuccess) return e;
+    }
     p->d_death_items = di;
     p->d_gcells = dg;
     p->n_death_items = static_cast<int>(items.size());
+    p->death_split = split;
+    p->death_part = part;
     return cudaSuccess;
 }
 
@@ -1289,7 +1306,8 @@ int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_para
         if (e != cudaSuccess) return e;
     }
     return batch_death(plan->d, N, params, death, method, plan->d_death_items,
-                       plan->n_death_items, plan->d_gcells, s);
+                       plan->n_death_items, plan->d_gcells, plan->death_part, plan->death_split,
+                       plan->total, s);
 }
 
 int pbe_batch_rhs_vjp(pbe_batch_t plan, const double* N, const double* lambda, double* gN,

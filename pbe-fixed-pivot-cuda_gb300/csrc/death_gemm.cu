@@ -16,8 +16,11 @@
 // covers Brownian + shear with per-cell coefficients. It runs on the FP64
 // tensor cores with mma.sync.m8n8k4.f64 (tcgen05 has no FP64 kind); B tiles
 // are generated in shared memory from the grid's cube roots, never stored.
-// A CTA owns 64 cells x 64 bins (4 warps of 32 x 32); 2 n^2 C flops per
-// component. On GB300 the FP64 MMA rate is no higher than the DFMA rate, so
+// A CTA owns 64 cells x 64 bins (4 warps of 32 x 32) and one of S slices of
+// the k range (grid y): with few cells per grid there are few 64 x 64 tiles,
+// so the slices give the SMs enough CTAs; each slice stores its partial D and
+// death_reduce_kernel adds the S partials in slice order and multiplies by N
+// (S = 1: the CTA writes N D itself). 2 n^2 C flops per component. On GB300 the FP64 MMA rate is no higher than the DFMA rate, so
 // this form is measured beside the moment form rather than used by the RHS.
 // =============================================================================
 #include "batch_internal.cuh"
@@ -61,12 +64,15 @@ __device__ __forceinline__ double comp_coef(int s, const pbe_batch_cell_params_t
     else return s == 0 ? P.beta_br : P.beta_sh;
 }
 
-// item = {grid, first row in gcells, rows (<= 64), first bin}
+// item = {grid, first row in gcells, rows (<= 64), first bin}; k slice
+// blockIdx.y of gridDim.y; part: [gridDim.y][total] partial D (null when
+// gridDim.y == 1: out = N D directly).
 template <int K>
 __global__ void __launch_bounds__(128)
 death_dmma_kernel(BatchDev d, const double* __restrict__ N,
                   const pbe_batch_cell_params_t* __restrict__ params, double* __restrict__ out,
-                  const int4* __restrict__ items, const int* __restrict__ gcells)
+                  const int4* __restrict__ items, const int* __restrict__ gcells,
+                  double* __restrict__ part, long long total)
 {
     __shared__ double As[kBK][kBM + kPad];
     __shared__ double Bs[kBK][kBN + kPad];
@@ -107,13 +113,17 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
         for (int ni = 0; ni < 4; ++ni) acc[mi][ni][0] = acc[mi][ni][1] = 0.0;
 
     const int ktot = NC * kmax;
-    for (int kb = 0; kb < ktot; kb += kBK) {
+    const int S = gridDim.y;
+    const int kc = ((ktot + S - 1) / S + kBK - 1) / kBK * kBK;     // slice length, kBK multiple
+    const int kbeg = min(ktot, static_cast<int>(blockIdx.y) * kc);
+    const int kend = min(ktot, kbeg + kc);
+    for (int kb = kbeg; kb < kend; kb += kBK) {
         // A tile: rows = cells, k contiguous in N (coalesced)
         for (int e = tid; e < kBM * kBK; e += blockDim.x) {
             const int m = e / kBK, kk = e - m * kBK;
             const int kg = kb + kk;
             double v = 0.0;
-            if (kg < ktot) {
+            if (kg < kend) {
                 const int s = kg / kmax, k = kg - s * kmax;
                 if (k < s_n[m]) v = s_coef[s][m] * N[s_off[m] + k];
             }
@@ -124,7 +134,7 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
             const int ib = e / kBK, kk = e - ib * kBK;
             const int kg = kb + kk, bin = i0 + ib;
             double v = 0.0;
-            if (kg < ktot && bin < gd.n) {
+            if (kg < kend && bin < gd.n) {
                 const int s = kg / kmax, k = kg - s * kmax;
                 v = comp_value<K>(s, x[bin], a[bin], ia[bin], x[k], a[k], ia[k]);
             }
@@ -155,8 +165,22 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 const int bin = i0 + wn * 32 + ni * 8 + 2 * t + r;
-                if (bin < n) out[off + bin] = N[off + bin] * acc[mi][ni][r];
+                if (bin >= n) continue;
+                if (part) part[blockIdx.y * total + off + bin] = acc[mi][ni][r];
+                else out[off + bin] = N[off + bin] * acc[mi][ni][r];
             }
+    }
+}
+
+// out = N (sum of the S slices' partial D, in slice order), every packed bin.
+__global__ void __launch_bounds__(256)
+death_reduce_kernel(const double* __restrict__ N, const double* __restrict__ part, int S,
+                    long long total, double* __restrict__ out)
+{
+    for (long long e = blockIdx.x * 256LL + threadIdx.x; e < total; e += 256LL * gridDim.x) {
+        double s_ = 0.0;
+        for (int q = 0; q < S; ++q) s_ += part[q * total + e];
+        out[e] = N[e] * s_;
     }
 }
 
@@ -193,13 +217,20 @@ death_moments_kernel(BatchDev d, const double* __restrict__ N,
 template <int K>
 cudaError_t death_k(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
                     double* out, int method, const int4* items, int n_items, const int* gcells,
-                    cudaStream_t s)
+                    double* part, int S, long long total, cudaStream_t s)
 {
     if (method == 0) {
         death_moments_kernel<K><<<d.n_cells, 256, 0, s>>>(d, N, params, out);
     } else {
         if (n_items <= 0) return cudaSuccess;
-        death_dmma_kernel<K><<<n_items, 128, 0, s>>>(d, N, params, out, items, gcells);
+        const bool split = S > 1 && part;
+        death_dmma_kernel<K><<<dim3(n_items, split ? S : 1), 128, 0, s>>>(
+            d, N, params, out, items, gcells, split ? part : nullptr, total);
+        if (split) {
+            const long long b = (total + 255) / 256, cap = 16LL * (d.num_sms > 0 ? d.num_sms : 1);
+            death_reduce_kernel<<<static_cast<int>(b < cap ? b : cap), 256, 0, s>>>(N, part, S,
+                                                                                     total, out);
+        }
     }
     return cudaGetLastError();
 }
@@ -208,15 +239,15 @@ cudaError_t death_k(const BatchDev& d, const double* N, const pbe_batch_cell_par
 
 cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
                         double* out, int method, const int4* items, int n_items,
-                        const int* gcells, cudaStream_t s)
+                        const int* gcells, double* part, int S, long long total, cudaStream_t s)
 {
     switch (d.kernel) {
-    case 0: return death_k<0>(d, N, params, out, method, items, n_items, gcells, s);
-    case 1: return death_k<1>(d, N, params, out, method, items, n_items, gcells, s);
-    case 2: return death_k<2>(d, N, params, out, method, items, n_items, gcells, s);
-    case 3: return death_k<3>(d, N, params, out, method, items, n_items, gcells, s);
-    case 4: return death_k<4>(d, N, params, out, method, items, n_items, gcells, s);
-    case 5: return death_k<5>(d, N, params, out, method, items, n_items, gcells, s);
+    case 0: return death_k<0>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 1: return death_k<1>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 2: return death_k<2>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 3: return death_k<3>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 4: return death_k<4>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 5: return death_k<5>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
     default: return cudaErrorInvalidValue;
     }
 }
