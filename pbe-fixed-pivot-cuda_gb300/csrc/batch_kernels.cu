@@ -227,70 +227,68 @@ __device__ double cell_clip(const AggCellView& v, const TileGroup& G)
     return acc;
 }
 
-// Breakage of every bin of a cell (one CTA, prep kernels without kBrkTasks): bin
-// i takes the hi-shares of the fragments bracketed at i-1 and the lo-shares of
-// those at i (bin 0 also the fragments clipped below x[0]), minus S_i N_i. A
-// warp covers 32/nqp bins, nqp = the quadrature points rounded up to a power
-// of two (<= 32) lanes per bin, summed in a fixed butterfly.
+// One lane's part of the breakage gather of bin i (0 <= i < n) of a cell:
+// quadrature points q = q0, q0 + nqp, ..., each adding the hi-shares of the
+// fragments bracketed at i-1 and the lo-shares of those at i (bin 0 also the
+// fragments clipped below x[0]). The nqp lanes of a bin then add their parts
+// in a fixed butterfly.
+__device__ __forceinline__ double brk_lane(const BatchDev& d, const BatchGridDev& gd,
+                                           const double* SN, int n, int i, int q0, int nqp)
+{
+    const int ng = gd.n;
+    double acc = 0.0;
+    for (int q = q0; q < d.nq; q += nqp) {
+        const int* fq = d.bfirst + gd.foff + q * (ng + 2);
+        const double* wl = d.bwlo + gd.woff + q * ng;
+        const double* wh = d.bwhi + gd.woff + q * ng;
+        const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
+        const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
+        const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
+        if (i == 0) { for (int j = 0; j < fb; ++j) acc = fma(SN[j], wl[j], acc); }
+        else        { for (int j = fa; j < fb; ++j) acc = fma(SN[j], wh[j], acc); }
+        for (int j = fb; j < fc; ++j) acc = fma(SN[j], wl[j], acc);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ int brk_lanes(int nq)
+{
+    int nqp = 1;
+    while (nqp < nq && nqp < 32) nqp <<= 1;
+    return nqp;
+}
+
+// Breakage term of every bin of a cell (one CTA; the prep kernels without
+// kBrkTasks), minus S_i N_i: a warp covers 32/nqp bins, nqp = the quadrature
+// points rounded up to a power of two (<= 32) lanes per bin.
 __device__ void cell_breakage(const BatchDev& d, const BatchGridDev& gd, const double* SN,
                               double* Bk, int n)
 {
-    int nqp = 1;
-    while (nqp < d.nq && nqp < 32) nqp <<= 1;
+    const int nqp = brk_lanes(d.nq);
     const int per_warp = 32 / nqp;
     const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    const int ng = gd.n;
     for (int base = w * per_warp; base < n; base += nw * per_warp) {   // uniform per warp
         const int i = base + l / nqp;
-        double acc = 0.0;
-        if (i < n) {
-            for (int q = l % nqp; q < d.nq; q += nqp) {
-                const int* fq = d.bfirst + gd.foff + q * (ng + 2);
-                const double* wl = d.bwlo + gd.woff + q * ng;
-                const double* wh = d.bwhi + gd.woff + q * ng;
-                const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
-                const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
-                const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
-                if (i == 0) { for (int j = 0; j < fb; ++j) acc = fma(SN[j], wl[j], acc); }
-                else        { for (int j = fa; j < fb; ++j) acc = fma(SN[j], wh[j], acc); }
-                for (int j = fb; j < fc; ++j) acc = fma(SN[j], wl[j], acc);
-            }
-        }
+        double acc = (i < n) ? brk_lane(d, gd, SN, n, i, l % nqp, nqp) : 0.0;
         for (int o = nqp >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (i < n && (l % nqp) == 0) Bk[i] = acc - SN[i];
     }
 }
 
-// The same breakage term for the bins I .. I+W-1 of a cell (those in
-// [0, n)), gathered by a task's group into out[0 .. W) (kBrkTasks), with the
-// same lanes per bin, loops and butterfly, so the sums are bitwise those of
-// cell_breakage.
+// The same term for the bins I .. I+W-1 of a cell (those in [0, n)), by a
+// task's group into out[0 .. W) (kBrkTasks): the same lanes per bin, loops and
+// butterfly, so the sums are bitwise those of cell_breakage.
 __device__ void tile_breakage(const BatchDev& d, const BatchGridDev& gd, const double* SN, int n,
                               int I, double* out, const TileGroup& G)
 {
-    int nqp = 1;
-    while (nqp < d.nq && nqp < 32) nqp <<= 1;
+    const int nqp = brk_lanes(d.nq);
     const int per_warp = 32 / nqp;
     const int nw = G.T >> 5, w = G.lane >> 5, l = G.lane & 31;
-    const int ng = gd.n;
     for (int base = w * per_warp; base < W; base += nw * per_warp) {   // uniform per warp
         const int t = base + l / nqp;
         const int i = I + t;
         const bool in = t < W && i >= 0 && i < n;
-        double acc = 0.0;
-        if (in) {
-            for (int q = l % nqp; q < d.nq; q += nqp) {
-                const int* fq = d.bfirst + gd.foff + q * (ng + 2);
-                const double* wl = d.bwlo + gd.woff + q * ng;
-                const double* wh = d.bwhi + gd.woff + q * ng;
-                const int fa = min(max(fq[i], 0), n);         // first j with lo >= i-1
-                const int fb = min(max(fq[i + 1], fa), n);    // first j with lo >= i
-                const int fc = min(max(fq[i + 2], fb), n);    // first j with lo >= i+1
-                if (i == 0) { for (int j = 0; j < fb; ++j) acc = fma(SN[j], wl[j], acc); }
-                else        { for (int j = fa; j < fb; ++j) acc = fma(SN[j], wh[j], acc); }
-                for (int j = fb; j < fc; ++j) acc = fma(SN[j], wl[j], acc);
-            }
-        }
+        double acc = in ? brk_lane(d, gd, SN, n, i, l % nqp, nqp) : 0.0;
         for (int o = nqp >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (t < W && (l % nqp) == 0) out[t] = in ? acc - SN[i] : 0.0;
     }

@@ -112,32 +112,31 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
 #pragma unroll
         for (int ni = 0; ni < 4; ++ni) acc[mi][ni][0] = acc[mi][ni][1] = 0.0;
 
-    const int ktot = NC * kmax;
+    // components concatenated along k with a stride of kmax rounded up to kBK,
+    // so a k block lies in one component (the padding has A = 0)
+    const int kpad = (kmax + kBK - 1) / kBK * kBK;
+    const int ktot = NC * kpad;
     const int S = gridDim.y;
     const int kc = ((ktot + S - 1) / S + kBK - 1) / kBK * kBK;     // slice length, kBK multiple
     const int kbeg = min(ktot, static_cast<int>(blockIdx.y) * kc);
     const int kend = min(ktot, kbeg + kc);
     for (int kb = kbeg; kb < kend; kb += kBK) {
+        const int sc = kb / kpad, kb0 = kb - sc * kpad;     // component, its first k here
         // A tile: rows = cells, k contiguous in N (coalesced)
         for (int e = tid; e < kBM * kBK; e += blockDim.x) {
             const int m = e / kBK, kk = e - m * kBK;
-            const int kg = kb + kk;
+            const int k = kb0 + kk;
             double v = 0.0;
-            if (kg < kend) {
-                const int s = kg / kmax, k = kg - s * kmax;
-                if (k < s_n[m]) v = s_coef[s][m] * N[s_off[m] + k];
-            }
+            if (kb + kk < kend && k < s_n[m]) v = s_coef[sc][m] * N[s_off[m] + k];
             As[kk][m] = v;
         }
         // B tile: generated from the grid's pivots and cube roots
         for (int e = tid; e < kBN * kBK; e += blockDim.x) {
             const int ib = e / kBK, kk = e - ib * kBK;
-            const int kg = kb + kk, bin = i0 + ib;
+            const int k = kb0 + kk, bin = i0 + ib;
             double v = 0.0;
-            if (kg < kend && bin < gd.n) {
-                const int s = kg / kmax, k = kg - s * kmax;
-                v = comp_value<K>(s, x[bin], a[bin], ia[bin], x[k], a[k], ia[k]);
-            }
+            if (kb + kk < kend && k < kmax && bin < gd.n)
+                v = comp_value<K>(sc, x[bin], a[bin], ia[bin], x[k], a[k], ia[k]);
             Bs[kk][ib] = v;
         }
         __syncthreads();
