@@ -704,9 +704,19 @@ cudaError_t vjp_setup(pbe_batch_plan* p, cudaStream_t s)
     const size_t C = static_cast<size_t>(p->total);
     std::vector<int> tile_off(static_cast<size_t>(p->n_cells) + 1, 0);
     for (int c = 0; c < p->n_cells; ++c) tile_off[c + 1] = tile_off[c] + (p->cell_n[c] + W - 1) / W;
+    // every row tile meets all n partners, so with few tiles larger groups
+    // (fewer tasks per bundle) give each CTA slot a bundle: T >= 256 x (CTA
+    // slots) / tiles, a power of two in [forward T, 256]
+    int gs[kClasses];
+    const long long tiles = tile_off.back();
+    for (int c = 0; c < kClasses; ++c) {
+        int T = p->group_size[c] > 0 ? p->group_size[c] : 32;
+        while (T < kMainThreads && tiles * T < 256LL * 2 * p->num_sms) T <<= 1;
+        gs[c] = T;
+    }
     std::vector<int4> b;
     std::vector<int4> t;
-    build_schedule(*p, p->group_size, nullptr, b, t, true);
+    build_schedule(*p, gs, nullptr, b, t, true);
     int* dto = nullptr;
     int4* db = nullptr;
     int4* dt = nullptr;
