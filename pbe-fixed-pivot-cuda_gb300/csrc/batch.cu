@@ -56,6 +56,8 @@ struct pbe_batch_plan {
     int n_death_items = -1;
     int death_split = 1;               // k slices of the death GEMM
     double* death_part = nullptr;      // [death_split * total] slice partials
+    double* death_b = nullptr;         // every used grid's B matrix (death GEMM)
+    long long* death_boff = nullptr;   // [n_grids] its offsets (device)
     // batched VJP (set up on first use)
     bool vjp_ready = false;
     pbe_gb300::BatchVjpDev vd{};
@@ -1206,11 +1208,39 @@ cudaError_t death_items(pbe_batch_plan* p, cudaStream_t s)
         e = plan_alloc(p, &part, static_cast<size_t>(split) * static_cast<size_t>(p->total));
         if (e != cudaSuccess) return e;
     }
+    // the grids' B matrices (n_g x NC ld_g, ld_g = n_g rounded up to 16),
+    // filled once: the GEMM's k loop then only loads its tiles
+    const int ncomp = (p->kernel == 5) ? 2 : 1;
+    std::vector<long long> hboff(static_cast<size_t>(p->n_grids), 0);
+    std::vector<int> used;
+    long long btotal = 0;
+    for (int g = 0; g < p->n_grids; ++g) {
+        bool any = false;
+        for (int c = 0; c < p->n_cells && !any; ++c) any = p->cell_grid[c] == g;
+        hboff[g] = btotal;
+        if (!any) continue;
+        used.push_back(g);
+        const long long n = p->grid_n[g], ld = (n + 15) / 16 * 16;
+        btotal += n * ncomp * ld;
+    }
+    double* bm = nullptr;
+    long long* dbo = nullptr;
+    e = plan_alloc(p, &bm, static_cast<size_t>(btotal));
+    if (e == cudaSuccess) e = plan_alloc(p, &dbo, hboff.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dbo, hboff.data(), hboff.size() * sizeof(long long),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !used.empty())
+        e = batch_death_b(p->d, used.data(), static_cast<int>(used.size()), bm, hboff.data(), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
     p->d_death_items = di;
     p->d_gcells = dg;
     p->n_death_items = static_cast<int>(items.size());
     p->death_split = split;
     p->death_part = part;
+    p->death_b = bm;
+    p->death_boff = dbo;
     return cudaSuccess;
 }
 
@@ -1317,7 +1347,7 @@ int pbe_batch_death(pbe_batch_t plan, const double* N, const pbe_batch_cell_para
     }
     return batch_death(plan->d, N, params, death, method, plan->d_death_items,
                        plan->n_death_items, plan->d_gcells, plan->death_part, plan->death_split,
-                       plan->total, s);
+                       plan->total, plan->death_b, plan->death_boff, s);
 }
 
 int pbe_batch_rhs_vjp(pbe_batch_t plan, const double* N, const double* lambda, double* gN,

@@ -251,10 +251,15 @@ cudaError_t batch_main_bundles(const BatchDev& d, const double* Y,
 // Death term N_i sum_k beta(x_i, x_k) N_k of every cell (death_gemm.cu):
 // method 0 = per-cell moments, 1 = FP64 tensor-core GEMM over the work items
 // {grid, first row of gcells, rows <= 64, first bin} (cells grouped by grid).
-// (DMMA: S > 1 k slices with partials in part [S * total], then a reduce.)
+// (DMMA: S > 1 k slices with partials in part [S * total], then a reduce;
+// Bm: every grid's B at boff[g] (device; hboff the host copy), filled once per
+// plan by batch_death_b for the grids in grids_used.)
+cudaError_t batch_death_b(const BatchDev& d, const int* grids_used, int n_used, double* Bm,
+                          const long long* hboff, cudaStream_t s);
 cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
                         double* out, int method, const int4* items, int n_items,
-                        const int* gcells, double* part, int S, long long total, cudaStream_t s);
+                        const int* gcells, double* part, int S, long long total, const double* Bm,
+                        const long long* boff, cudaStream_t s);
 // Batched VJP: gN += dL/dN, gparams[8 c + j] += dL/d(parameter j of cell c)
 // for L = lambda . RHS(N) (batch_vjp.cu). batch_vjp_setup once per plan.
 cudaError_t batch_vjp_setup(int kernel);

@@ -64,6 +64,28 @@ __device__ __forceinline__ double comp_coef(int s, const pbe_batch_cell_params_t
     else return s == 0 ? P.beta_br : P.beta_sh;
 }
 
+// B of every grid, once per plan: Bm[boff[g] + i * (NC ld) + s ld + k] =
+// f_s(x_i, x_k), ld = n_g rounded up to kBK (grid-stride over the grid's
+// n_g x NC ld entries; the padding is 0).
+template <int K>
+__global__ void __launch_bounds__(256)
+death_b_kernel(BatchDev d, int g, double* __restrict__ Bm)
+{
+    constexpr int NC = Comps<K>::n;
+    const BatchGridDev gd = d.grids[g];
+    const int n = gd.n, ld = (n + kBK - 1) / kBK * kBK;
+    const double* x = d.gx + gd.off;
+    const double* a = d.ga + gd.off;
+    const double* ia = d.gia + gd.off;
+    const long long cols = static_cast<long long>(NC) * ld, total = cols * n;
+    for (long long e = blockIdx.x * 256LL + threadIdx.x; e < total; e += 256LL * gridDim.x) {
+        const int i = static_cast<int>(e / cols);
+        const int c = static_cast<int>(e - static_cast<long long>(i) * cols);
+        const int s = c / ld, k = c - s * ld;
+        Bm[e] = (k < n) ? comp_value<K>(s, x[i], a[i], ia[i], x[k], a[k], ia[k]) : 0.0;
+    }
+}
+
 // item = {grid, first row in gcells, rows (<= 64), first bin}; k slice
 // blockIdx.y of gridDim.y; part: [gridDim.y][total] partial D (null when
 // gridDim.y == 1: out = N D directly).
@@ -72,7 +94,8 @@ __global__ void __launch_bounds__(128)
 death_dmma_kernel(BatchDev d, const double* __restrict__ N,
                   const pbe_batch_cell_params_t* __restrict__ params, double* __restrict__ out,
                   const int4* __restrict__ items, const int* __restrict__ gcells,
-                  double* __restrict__ part, long long total)
+                  double* __restrict__ part, long long total, const double* __restrict__ Bm,
+                  const long long* __restrict__ boff)
 {
     __shared__ double As[kBK][kBM + kPad];
     __shared__ double Bs[kBK][kBN + kPad];
@@ -115,6 +138,8 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
     // components concatenated along k with a stride of kmax rounded up to kBK,
     // so a k block lies in one component (the padding has A = 0)
     const int kpad = (kmax + kBK - 1) / kBK * kBK;
+    const int ldg = (gd.n + kBK - 1) / kBK * kBK;                 // B's component stride
+    const double* Bg = Bm + boff[it.x];
     const int ktot = NC * kpad;
     const int S = gridDim.y;
     const int kc = ((ktot + S - 1) / S + kBK - 1) / kBK * kBK;     // slice length, kBK multiple
@@ -130,13 +155,13 @@ death_dmma_kernel(BatchDev d, const double* __restrict__ N,
             if (kb + kk < kend && k < s_n[m]) v = s_coef[sc][m] * N[s_off[m] + k];
             As[kk][m] = v;
         }
-        // B tile: generated from the grid's pivots and cube roots
+        // B tile: the grid's precomputed B (16 consecutive k per bin)
         for (int e = tid; e < kBN * kBK; e += blockDim.x) {
             const int ib = e / kBK, kk = e - ib * kBK;
             const int k = kb0 + kk, bin = i0 + ib;
             double v = 0.0;
             if (kb + kk < kend && k < kmax && bin < gd.n)
-                v = comp_value<K>(sc, x[bin], a[bin], ia[bin], x[k], a[k], ia[k]);
+                v = Bg[static_cast<size_t>(bin) * (NC * ldg) + sc * ldg + k];
             Bs[kk][ib] = v;
         }
         __syncthreads();
@@ -214,9 +239,21 @@ death_moments_kernel(BatchDev d, const double* __restrict__ N,
 }
 
 template <int K>
+cudaError_t death_b_k(const BatchDev& d, const int* grids_used, int n_used, double* Bm,
+                      const long long* hboff, cudaStream_t s)
+{
+    for (int q = 0; q < n_used; ++q) {
+        const int g = grids_used[q];
+        death_b_kernel<K><<<16 * (d.num_sms > 0 ? d.num_sms : 1), 256, 0, s>>>(d, g, Bm + hboff[g]);
+    }
+    return cudaGetLastError();
+}
+
+template <int K>
 cudaError_t death_k(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
                     double* out, int method, const int4* items, int n_items, const int* gcells,
-                    double* part, int S, long long total, cudaStream_t s)
+                    double* part, int S, long long total, const double* Bm, const long long* boff,
+                    cudaStream_t s)
 {
     if (method == 0) {
         death_moments_kernel<K><<<d.n_cells, 256, 0, s>>>(d, N, params, out);
@@ -224,7 +261,7 @@ cudaError_t death_k(const BatchDev& d, const double* N, const pbe_batch_cell_par
         if (n_items <= 0) return cudaSuccess;
         const bool split = S > 1 && part;
         death_dmma_kernel<K><<<dim3(n_items, split ? S : 1), 128, 0, s>>>(
-            d, N, params, out, items, gcells, split ? part : nullptr, total);
+            d, N, params, out, items, gcells, split ? part : nullptr, total, Bm, boff);
         if (split) {
             const long long b = (total + 255) / 256, cap = 16LL * (d.num_sms > 0 ? d.num_sms : 1);
             death_reduce_kernel<<<static_cast<int>(b < cap ? b : cap), 256, 0, s>>>(N, part, S,
@@ -236,17 +273,32 @@ cudaError_t death_k(const BatchDev& d, const double* N, const pbe_batch_cell_par
 
 } // namespace
 
-cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
-                        double* out, int method, const int4* items, int n_items,
-                        const int* gcells, double* part, int S, long long total, cudaStream_t s)
+cudaError_t batch_death_b(const BatchDev& d, const int* grids_used, int n_used, double* Bm,
+                          const long long* hboff, cudaStream_t s)
 {
     switch (d.kernel) {
-    case 0: return death_k<0>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
-    case 1: return death_k<1>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
-    case 2: return death_k<2>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
-    case 3: return death_k<3>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
-    case 4: return death_k<4>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
-    case 5: return death_k<5>(d, N, params, out, method, items, n_items, gcells, part, S, total, s);
+    case 0: return death_b_k<0>(d, grids_used, n_used, Bm, hboff, s);
+    case 1: return death_b_k<1>(d, grids_used, n_used, Bm, hboff, s);
+    case 2: return death_b_k<2>(d, grids_used, n_used, Bm, hboff, s);
+    case 3: return death_b_k<3>(d, grids_used, n_used, Bm, hboff, s);
+    case 4: return death_b_k<4>(d, grids_used, n_used, Bm, hboff, s);
+    case 5: return death_b_k<5>(d, grids_used, n_used, Bm, hboff, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t batch_death(const BatchDev& d, const double* N, const pbe_batch_cell_params_t* params,
+                        double* out, int method, const int4* items, int n_items,
+                        const int* gcells, double* part, int S, long long total, const double* Bm,
+                        const long long* boff, cudaStream_t s)
+{
+    switch (d.kernel) {
+    case 0: return death_k<0>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
+    case 1: return death_k<1>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
+    case 2: return death_k<2>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
+    case 3: return death_k<3>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
+    case 4: return death_k<4>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
+    case 5: return death_k<5>(d, N, params, out, method, items, n_items, gcells, part, S, total, Bm, boff, s);
     default: return cudaErrorInvalidValue;
     }
 }
