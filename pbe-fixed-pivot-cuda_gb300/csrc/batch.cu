@@ -7,7 +7,15 @@
 // about min(I + W, n) lags. Cells are classed by floor(log2 n). Each class has a group
 // size T (threads per task): a bundle packs 256/T tasks of one class, so a
 // CTA of the persistent kernel runs up to eight small tiles at once. Bundles
-// are sorted by work (largest first) and pulled from an atomic counter.
+// are sorted by work (largest first) and pulled from an atomic counter. A
+// plan with few tiles (a handful of cells) also cuts each tile's lags into
+// chunks (chunk_setup) and gathers the breakage term in the pair tasks
+// instead of one prep CTA per cell; its VJP takes larger groups.
+//
+// Per call. The selection function of every bin is evaluated once per call
+// into the plan's cache (sel_cache, SelScope). The adaptive integrators and
+// the GMRES solves pass a per-cell skip mask, so finished cells and ended
+// solves are left out of the prep and pair launches.
 //
 // Autotuner. With PBE_BATCH_TUNE, each class present in the plan times the
 // persistent kernel on its own tasks for T = 32, 64, 128, 256 (synthetic
@@ -20,6 +28,12 @@
 // the previous stage's update in place (batch_internal.cuh, BatchStage).
 // pbe_batch_rk4 captures n_steps steps plus the closing update into one CUDA
 // graph on a private stream and launches it on the caller's stream.
+//
+// Beyond RK4: embedded Dormand-Prince 5(4) with a step size per cell
+// (pbe_batch_rk45), Jacobian-vector products (pbe_batch_jvp), and the
+// linearly implicit ROS2 (pbe_batch_ros2, pbe_batch_ros2_adaptive), whose
+// stage systems are solved by matrix-free, right-preconditioned GMRES(m)
+// with an optional tolerance and restarts (batch_implicit.cu).
 // =============================================================================
 #include <algorithm>
 #include <cmath>
