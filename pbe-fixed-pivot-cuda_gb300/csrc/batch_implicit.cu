@@ -1,7 +1,9 @@
 // =============================================================================
 // batch_implicit.cu -- linear solves of the batched Rosenbrock integrator:
 // (I - g J(N)) x = r for every cell at once, g = gamma dt, by GMRES(m)
-// without restart, right-preconditioned by the diagonal
+// (a cell's solve may end early at a relative residual tol, and cells above
+// tol after m steps may restart on r - A x), right-preconditioned by the
+// diagonal
 // P_i = 1 + g (sum_k beta_ik N_k + beta_ii N_i + S_i [N_i guarded]), i.e. the
 // loss part of -J_ii (death and breakage; the birth terms are left out).
 // J is never formed: each Arnoldi step takes one Jacobian-vector product
