@@ -58,7 +58,11 @@ def shard_cells(cell_n: Sequence[int], rank: int, world: int) -> np.ndarray:
 class BatchPlan:
     """A plan over `cell_n` cells; cell c uses the first cell_n[c] pivots of
     grids[cell_grid[c]]. kernel: AGG_* or -1 (no aggregation); selection:
-    SEL_* or -1 (no breakage) with the daughter table (t_q, bw_q)."""
+    SEL_* or -1 (no breakage) with the daughter table (t_q, bw_q).
+    tune / retune: time the tile group sizes per size class (cached);
+    breakage_gather: "prep" or "tasks" forces where the breakage term is
+    gathered (bitwise the same result; by default the plan picks by its
+    cell count)."""
 
     def __init__(self, grids: Sequence[np.ndarray], cell_n: Sequence[int],
                  cell_grid: Sequence[int], kernel: int, selection: int = -1,
