@@ -58,8 +58,8 @@ FLOPS_PER_FRAGMENT = 8   # per breakage fragment
 # numerator runs on the integer pipe. fp64_instr_per_launch() counts the
 # evaluations of both kinds the kernel performs on a given grid (each pair
 # once: tiles hand the w-part of their top slot to the tile above), plus 4 per
-# clipped pair (the clip tasks); profiles/ cross-checks the count with the
-# SASS instruction counters.
+# clipped pair (the clip tasks); profiles/ cross-checks the count with ncu's
+# FP64 instruction counters (dadd + dfma + dmul per cycle x cycles).
 FP64_PHASE1, FP64_PHASE2 = 5, 4
 
 
