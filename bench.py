@@ -16,14 +16,27 @@ integrator asks for once per stage).
   e2e   : the same step through the C ABI from pinned HOST buffers: H2D copy of
           N, the RHS, D2H copy of rhs, all inside the timed events.
 
+  roofline: the pair kernel (agg_main_kernel) timed alone with CUDA events;
+          bound = the FP64 pipe, in FP64 instructions per second against the
+          DFMA-chain probe's rate (one pipe slot per instruction). The
+          reference-formula flop rate (22 flops per pair) is reported beside
+          it as reference_equivalent_*: it exceeds the peak because the
+          kernel executes about 4.5 FP64 instructions per pair.
+  cpu_baseline: the oracle port on this host, all threads and one thread.
+
 --impl reference times the reference's path on the machine's host cores. The
 reference implements the path only in CUDA (no CPU implementation), so the arm
 runs the oracle port (oracle/pbe_oracle.cpp: the reference's pair and fragment
 loops restated serially, aggregation rows spread over all host threads) on
-the same workload; each step is one full n = 16384 RHS evaluation and the
-number of timed steps is capped so the arm ends within a few minutes. Our own
-line also carries `reference_kernels_sm103a`: the reference's CUDA kernels,
-built unmodified from its sources (oracle/_ref), timed on the same GPU.
+the same workload and config; each step is one full n = 16384 RHS
+evaluation, with --steps and --warmup honoured unless the steps would take
+more than about four minutes.
+
+The JSON line ends with `summary`: the headline figures of the other sections
+(the reference's CUDA kernels built unmodified from its sources into
+oracle/_ref and timed on the same GPU, the other accumulation mode, the VJP,
+batched cells, the adjoint tape, size classes). The sections themselves go to
+--sections-out (default bench_sections.json) and to stderr.
 
 Multi-GPU: the single-instance RHS does not shard; with torchrun each rank runs
 an independent replica on its own GPU ("replicas only"), value = total steps/s.
@@ -58,8 +71,8 @@ FLOPS_PER_FRAGMENT = 8   # per breakage fragment
 # numerator runs on the integer pipe. fp64_instr_per_launch() counts the
 # evaluations of both kinds the kernel performs on a given grid (each pair
 # once: tiles hand the w-part of their top slot to the tile above), plus 4 per
-# clipped pair (the clip tasks); profiles/ cross-checks the count with ncu's
-# FP64 instruction counters (dadd + dfma + dmul per cycle x cycles).
+# clipped pair (the clip tasks). On this workload the count is within 3 % of
+# ncu's FP64 instruction counters (dadd + dfma + dmul) for one launch.
 FP64_PHASE1, FP64_PHASE2 = 5, 4
 
 
@@ -79,8 +92,11 @@ def fp64_instr_per_launch(x) -> int:
     return (FP64_PHASE1 * int(cnt[d_all < D0].sum()) + FP64_PHASE2 * int(cnt[d_all >= D0].sum())
             + 4 * clipped)
 # dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
-# this workload, from the ncu capture in profiles/agg_main_kernel_n16384.md.
+# this workload, read from an ncu capture of that launch (L2 flushed before it,
+# as in the timed loop); not measured by this script.
 MAIN_KERNEL_DRAM_BYTES = 1343488
+# algorithmic bytes of one aggregation RHS: N and x read, rhs read and written
+ALGO_BYTES_PER_LAUNCH = 24 * N_BINS
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -140,6 +156,37 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+WORKLOAD = ("single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), BrownianShear + "
+            "threshold breakage, n_quad=16")
+
+
+def run_config() -> dict:
+    """The `config` of both arms' JSON lines (identical on purpose)."""
+    return {"workload": WORKLOAD, "n": N_BINS, "n_quad": N_QUAD, "pairs_per_eval": PAIRS,
+            "fragments_per_eval": FRAGMENTS,
+            "l2": "GPU arm: flushed before every timed step (512 MiB write)",
+            "parallelism": "single instance per GPU (replicas only)"}
+
+
+def cpu_model() -> str:
+    """CPU model name of this host (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                             text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def workload():
     import pbe_gb300 as pg
 
@@ -169,25 +216,41 @@ def fp64_peak_tflops(stream) -> float | None:
     return v if v > 0 else None
 
 
-def cpu_baseline(x, N, t_q, bw_q, ap, bp, seconds=3.0):
-    """Oracle port (serial C++ restatement), all host threads for aggregation.
-    Sample: whole n = 16384 RHS evaluations, repeated until `seconds` elapsed."""
+def cpu_baseline(x, N, t_q, bw_q, ap, bp, seconds=3.0, serial_evals=3):
+    """Oracle port (the reference's pair and fragment loops restated as serial
+    C++, g++ -O3 -ffp-contract=off) on this host's cores, full n = 16384 RHS
+    evaluations: `value` with aggregation rows spread over every host thread
+    (OpenMP, repeated for `seconds`), `serial` on one thread (`serial_evals`
+    evaluations)."""
     import pyoracle
 
     threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    evals = 0
-    while True:
-        pyoracle.aggregation_rhs_mt(N, x, ap.kernel_type, ap.beta0, ap.beta_br, ap.beta_sh,
-                                    ap.log_x0, ap.inv_log_r, nthreads=threads)
-        pyoracle.breakage_rhs(N, x, t_q, bw_q, bp.selection, bp.S0, bp.v_ref, bp.alpha, bp.v_min)
-        evals += 1
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            break
+
+    def run(nthreads, min_s, min_evals):
+        t0 = time.perf_counter()
+        evals = 0
+        while True:
+            pyoracle.aggregation_rhs_mt(N, x, ap.kernel_type, ap.beta0, ap.beta_br, ap.beta_sh,
+                                        ap.log_x0, ap.inv_log_r, nthreads=nthreads)
+            pyoracle.breakage_rhs(N, x, t_q, bw_q, bp.selection, bp.S0, bp.v_ref, bp.alpha,
+                                  bp.v_min)
+            evals += 1
+            el = time.perf_counter() - t0
+            if el >= min_s and evals >= min_evals:
+                return evals, el
+
+    evals, el = run(threads, seconds, 1)
+    s_evals, s_el = run(1, 0.0, serial_evals)
+    model = cpu_model()
     return {"value": evals / el, "unit": "evals/s", "cores": threads, "kind": "port",
             "sample": "%d full n=16384 agg+brk RHS evaluations (%.1f s wall, OpenMP over "
-                      "aggregation rows, breakage serial)" % (evals, el)}
+                      "aggregation rows, breakage serial)" % (evals, el),
+            "cpu_model": model,
+            "serial": {"value": s_evals / s_el, "unit": "evals/s", "cores": 1,
+                       "sample": "%d full n=16384 agg+brk RHS evaluations on one thread (%.1f s)"
+                                 % (s_evals, s_el)},
+            "build": "g++ -O3 -ffp-contract=off (portable flags: the same oracle binary "
+                     "semantics on x86_64 and aarch64, no -march=native)"}
 
 
 def fp64_instr_tiles(x, n_cell=None) -> int:
@@ -547,6 +610,38 @@ def classes_section(dev, stream):
     }
 
 
+def summarize(sections: dict, value: float) -> dict:
+    """Headline figures of each section, for the one JSON line."""
+    out = {}
+    rk = sections.get("reference_kernels_sm103a", {})
+    if "evals_per_s" in rk:
+        out["reference_kernels_sm103a"] = {"evals_per_s": rk["evals_per_s"],
+                                           "speedup_of_value": round(value / rk["evals_per_s"], 2)}
+    elif rk:
+        out["reference_kernels_sm103a"] = rk
+    if "vjp" in sections:
+        out["vjp_rhs_ratio_n16384"] = sections["vjp"]["vjp_rhs_ratio"]
+    if "other_mode" in sections:
+        om = sections["other_mode"]
+        out["other_mode"] = {"mode": om["mode"], "evals_per_s": om["evals_per_s"]}
+    b = sections.get("batched")
+    if b:
+        out["batched_config3"] = {k: b[k] for k in ("cell_steps_per_s", "percell_loop_cell_steps_per_s",
+                                                    "speedup_vs_percell_loop", "finite_after_100_steps")}
+        out["batched_config3"]["fp64_pipe_frac"] = b["roofline"]["fp64_pipe_frac"]
+    a = sections.get("adjoint")
+    if a:
+        out["adjoint_config4"] = {k: a[k] for k in ("forward_ms", "backward_ms", "gradient_cost_ratio",
+                                                    "rhs_ms_n3840", "vjp_rhs_ratio_n3840")}
+    c = sections.get("classes")
+    if c:
+        out["classes_config5"] = {"cell_steps_per_s": c["cell_steps_per_s"],
+                                  "adjoint_backward_forward": c["adjoint"]["backward_forward_ratio"],
+                                  "jvp_rhs_ratio": c["jvp_rhs_ratio"],
+                                  "death_dmma_over_moments_time": c["dmma_over_moments_time"]}
+    return out
+
+
 def profile_case(name: str) -> None:
     """A few launches of one kernel family on a mid-size case, for ncu:
       batched : 1024 cells of the batched workload (seed 2026), 4 batched RHS
@@ -637,11 +732,13 @@ def reference_arm(args) -> None:
                                     ap.log_x0, ap.inv_log_r, nthreads=threads)
         pyoracle.breakage_rhs(N, x, t_q, bw_q, bp.selection, bp.S0, bp.v_ref, bp.alpha, bp.v_min)
 
+    warmup = max(args.warmup, 0)
     w0 = time.perf_counter()
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(max(warmup, 1)):
         step()
-    per = (time.perf_counter() - w0) / max(1, min(args.warmup, 2))
-    steps = int(min(args.steps, max(3, 90.0 / max(per, 1e-3))))
+    per = (time.perf_counter() - w0) / max(warmup, 1)
+    # every requested step unless that would take more than about four minutes
+    steps = int(min(args.steps, max(3, 240.0 / max(per, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(steps):
         step()
@@ -655,27 +752,24 @@ def reference_arm(args) -> None:
         "unit": "evals/s",
         "n_gpus": world,
         "steps": steps,
-        "steps_requested": args.steps,
-        "warmup": max(1, min(args.warmup, 2)),
+        "warmup": max(warmup, 1),
         "ms_per_step": round(el / steps * 1e3, 3),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded lognormal N on the stated grid)",
-        "config": {"workload": "single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), "
-                               "Brownian+shear (beta_br=6.73e-18, beta_sh=4*50/3) + threshold "
-                               "breakage (S0=1e-3, v_min=x_8192), symmetric daughter as n_quad=16",
-                   "n": N_BINS, "n_quad": N_QUAD, "pairs_per_eval": PAIRS,
-                   "fragments_per_eval": FRAGMENTS, "parallelism": "host cores"},
+        "config": run_config(),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "evals/s", "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample, "cpu_model": cpu_model()},
         "e2e": {"value": round(value, 4), "unit": "evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "reference_note": "the reference implements this path only in CUDA; the oracle port "
                           "restates its loops on the CPU (oracle/pbe_oracle.cpp)",
     }
+    if steps != args.steps:
+        out["steps_requested"] = args.steps
     print(json.dumps(out))
 
 
@@ -728,6 +822,8 @@ def main():
     ap_.add_argument("--no-cpu-baseline", action="store_true")
     ap_.add_argument("--no-extras", action="store_true",
                      help="skip the batched-cell and adjoint sections")
+    ap_.add_argument("--sections-out", default="bench_sections.json",
+                     help="file for the full per-section results (a summary stays in the line)")
     args = ap_.parse_args()
     if args.profile_case:
         profile_case(args.profile_case)
@@ -876,6 +972,37 @@ def main():
             dist.destroy_process_group()
         return
 
+    peak = fp64_peak_tflops(stream)
+    mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
+    instr = fp64_instr_per_launch(x)
+    # FP64 pipe: every FP64 instruction (DFMA, DMUL, DADD) takes one issue slot
+    # of the pipe per thread; the DFMA-chain probe runs it at peak/2 slots per
+    # second (2 flops per DFMA).
+    slots_peak = peak / 2.0 if peak else None                # T FP64 instructions/s
+    achieved = instr / mk / 1e12 if mk else None
+    ref_equiv = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
+    roofline = {
+        "bound": "fp64",
+        "kernel": "agg_main_kernel<5>",
+        "achieved": round(achieved, 4) if achieved else None,
+        "peak": round(slots_peak, 4) if slots_peak else None,
+        "unit": "T FP64 instr/s",
+        "frac": round(achieved / slots_peak, 4) if (achieved and slots_peak) else None,
+        "traffic": MAIN_KERNEL_DRAM_BYTES,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of "
+                          "this workload after an L2 flush, captured apart from this run",
+        "algo_bytes": ALGO_BYTES_PER_LAUNCH,
+        "kernel_ms": round(mk * 1e3, 5) if mk else None,
+        "fp64_instr_per_launch": instr,
+        "fp64_instr_source": "instruction model of the tile kernel on this grid (within 3 % of "
+                             "ncu's FP64 instruction counters)",
+        "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; "
+                       "MEASURED_PEAKS.json has no FP64 entry",
+        "reference_equivalent_tflops": round(ref_equiv, 4) if ref_equiv else None,
+        "reference_equivalent_frac": round(ref_equiv / peak, 4) if (ref_equiv and peak) else None,
+        "reference_equivalent_unit": "22 FP64 flops per pair interaction (the reference's "
+                                     "formula) per s, over the DFMA peak in TFLOP/s",
+    }
     out = {
         "metric": "Agg+br RHS evals/s at N=16384 FP64",
         "value": round(value, 3),
@@ -889,65 +1016,51 @@ def main():
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded lognormal N on the stated grid)",
-        "config": {"workload": "single-instance agg+brk RHS, n=16384, x_i=1e-21*2^(i/512), "
-                               "Brownian+shear (beta_br=6.73e-18, beta_sh=4*50/3) + threshold "
-                               "breakage (S0=1e-3, v_min=x_8192), symmetric daughter as n_quad=16",
-                   "n": N_BINS, "n_quad": N_QUAD, "mode": args.mode,
-                   "pairs_per_eval": PAIRS, "fragments_per_eval": FRAGMENTS,
-                   "l2": "flushed before every timed step (512 MiB write)",
-                   "parallelism": "replicas" if n_gpus > 1 else "single GPU"},
-        "pair_interactions_per_s": round(value * PAIRS, 1),
-        "fragments_per_s": round(value * N_BINS * N_QUAD, 1),
-        "wall_s_timed_loop": round(wall, 4),
+        "config": run_config(),
+        "mode": args.mode,
         "e2e": {"value": round(e2e_value, 3), "unit": "evals/s",
                 "h2d_bytes_per_step": N_BINS * 8, "d2h_bytes_per_step": N_BINS * 8},
         "gpu_launches": launches_per_step * args.steps,
         "memsets_per_step": 1,
         "clocks": clk,
+        "roofline": roofline,
+        "pair_interactions_per_s": round(value * PAIRS, 1),
+        "fragments_per_s": round(value * N_BINS * N_QUAD, 1),
+        "wall_s_timed_loop": round(wall, 4),
     }
+    sections = {}
     if vjp_ms is not None:
-        out["other_mode"] = {"mode": "scatter" if other == pg.MODE_SCATTER else "gather",
-                             "evals_per_s": round(1e3 / other_ms, 3),
-                             "ms_per_step": round(other_ms, 5),
-                             "what": "the same step in the other accumulation mode, device-resident, "
-                                     "L2 flushed"}
-        out["vjp"] = {"ms_per_eval": round(vjp_ms, 5),
-                      "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
-                      "what": "aggregation + breakage VJP (dL/dN and parameter gradients) of "
-                              "the same n=16384 step, device-resident, L2 flushed"}
-    peak = fp64_peak_tflops(stream)
-    mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
-    achieved = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
-    instr = fp64_instr_per_launch(x)
-    instr_rate = instr / mk if mk else None
-    out["roofline"] = {
-        "bound": "fp64",
-        "kernel": "agg_main_kernel<5>",
-        "achieved": round(achieved, 4) if achieved else None,
-        "peak": round(peak, 4) if peak else None,
-        "unit": "TFLOP/s",
-        "frac": round(achieved / peak, 4) if (achieved and peak) else None,
-        "traffic": MAIN_KERNEL_DRAM_BYTES,
-        "kernel_ms": round(mk * 1e3, 5) if mk else None,
-        "flops_per_launch": FLOPS_PER_PAIR * PAIRS,
-        "algorithmic_unit": "22 FP64 flops per pair interaction (reference formula, cube roots "
-                            "per bin); frac > 1 because the kernel executes %.2f FP64 "
-                            "instructions per pair" % (instr / PAIRS),
-        "fp64_instr_per_launch": instr,
-        "fp64_pipe_frac": round(instr_rate / (peak * 1e12 / 2.0), 4) if (instr_rate and peak) else None,
-        "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; no "
-                       "FP64 entry in MEASURED_PEAKS.json",
-    }
+        sections["other_mode"] = {"mode": "scatter" if other == pg.MODE_SCATTER else "gather",
+                                  "evals_per_s": round(1e3 / other_ms, 3),
+                                  "ms_per_step": round(other_ms, 5),
+                                  "what": "the same step in the other accumulation mode, "
+                                          "device-resident, L2 flushed"}
+        sections["vjp"] = {"ms_per_eval": round(vjp_ms, 5),
+                           "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
+                           "what": "aggregation + breakage VJP (dL/dN and parameter gradients) "
+                                   "of the same n=16384 step, device-resident, L2 flushed"}
     if n_gpus == 1 and not args.no_extras:
         rk = reference_kernels_section(dev, stream, dN, dx, dt, db, rhs, ap, bp, flush)
         if "evals_per_s" in rk:
             rk["speedup_of_value"] = round(value / rk["evals_per_s"], 2)
-        out["reference_kernels_sm103a"] = rk
-        out["batched"] = batched_section(dev, stream)
-        out["adjoint"] = adjoint_section(dev, stream)
-        out["classes"] = classes_section(dev, stream)
+        sections["reference_kernels_sm103a"] = rk
+        sections["batched"] = batched_section(dev, stream)
+        sections["adjoint"] = adjoint_section(dev, stream)
+        sections["classes"] = classes_section(dev, stream)
     if n_gpus == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(x, N, t_q, bw_q, ap, bp)
+    # the full sections go to a file (and stderr); the JSON line keeps a short
+    # summary of each so the headline figures stay in the line's tail
+    if sections:
+        path = args.sections_out
+        try:
+            with open(path, "w") as f:
+                json.dump(sections, f, indent=1)
+            out["sections_file"] = path
+        except OSError as exc:
+            out["sections_file"] = "not written: %s" % exc
+        print(json.dumps({"bench_sections": sections}), file=sys.stderr)
+        out["summary"] = summarize(sections, value)
     print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

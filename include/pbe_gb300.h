@@ -425,6 +425,15 @@ const char* pbe_error_string(int code);
 /* Library version, e.g. 100 for 0.1.0. */
 int pbe_version(void);
 
+/* Diagnostic (no reference counterpart): on the current device, the bytes the
+ * library's private scratch pool holds from the driver (*reserved_bytes) and
+ * the high-water mark of its bytes in use (*used_high_bytes) since the pool
+ * was created or the mark was last reset; reset_high != 0 resets the mark
+ * after reading it. Both are 0 before the first pool-using call on the
+ * device. Lets a caller check which calls take scratch from the pool. */
+int pbe_scratch_pool_usage(unsigned long long* reserved_bytes,
+                           unsigned long long* used_high_bytes, int reset_high);
+
 /* Profiling aid (no reference counterpart): when start and stop are both
  * non-NULL cudaEvent_t handles, every aggregation call records `start` just
  * before and `stop` just after its pair kernel, on the call's stream, so a

@@ -28,6 +28,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE, "_build")
 ORACLE_LIB = os.path.join(ORACLE_BUILD, "liboracle.so")
 REF_RUNNER_LIB = os.path.join(ORACLE_BUILD, "libref_runner.so")
+# the reference's C++ API over its own kernels (ref_dropin_shim.cpp + ref_runner.cpp)
+REF_DROPIN_LIB = os.path.join(ORACLE_BUILD, "liboracle_ref_dropin.so")
 
 SOURCES = ["aggregation.cu", "breakage.cu", "vjp.cu", "api.cu", "noalloc.cu",
            "batch_kernels.cu", "batch.cu", "adjoint.cu", "death_gemm.cu",
@@ -57,6 +59,17 @@ def _run(cmd: list[str], cwd: str | None = None) -> None:
     proc = subprocess.run(cmd, cwd=cwd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if proc.returncode != 0:
         raise RuntimeError("command failed (%d): %s\n%s" % (proc.returncode, " ".join(cmd), proc.stdout))
+
+
+def _cuda_libdirs(cuda: str) -> list[str]:
+    """-L flags for libcudart and the libcuda stub (x86_64 and aarch64 layouts)."""
+    out = []
+    for d in ("lib64", os.path.join("lib64", "stubs"), os.path.join("targets", "sbsa-linux", "lib", "stubs"),
+              os.path.join("targets", "x86_64-linux", "lib", "stubs")):
+        p = os.path.join(cuda, d)
+        if os.path.isdir(p):
+            out.append("-L" + p)
+    return out
 
 
 def _headers() -> list[str]:
@@ -106,19 +119,19 @@ def build_oracle(force: bool = False) -> None:
     src = os.path.join(ORACLE, "pbe_oracle.cpp")
     if force or not _newer(ORACLE_LIB, [src]):
         # no FMA contraction: identical oracle results on x86_64 and aarch64
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
               src, "-o", ORACLE_LIB])
     cuda = _cuda_home()
     rsrc = os.path.join(ORACLE, "ref_runner.cpp")
     if force or not _newer(REF_RUNNER_LIB, [rsrc]):
-        libdirs = []
-        for d in ("lib64", os.path.join("lib64", "stubs"), os.path.join("targets", "sbsa-linux", "lib", "stubs"),
-                  os.path.join("targets", "x86_64-linux", "lib", "stubs")):
-            p = os.path.join(cuda, d)
-            if os.path.isdir(p):
-                libdirs.append("-L" + p)
+        libdirs = _cuda_libdirs(cuda)
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + os.path.join(cuda, "include"),
               rsrc, *libdirs, "-lcuda", "-o", REF_RUNNER_LIB])
+    shim = os.path.join(ORACLE, "ref_dropin_shim.cpp")
+    if force or not _newer(REF_DROPIN_LIB, [rsrc, shim] + _headers()):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + os.path.join(cuda, "include"),
+              "-I" + INCLUDE, shim, rsrc, *_cuda_libdirs(cuda), "-lcudart", "-lcuda", "-ldl",
+              "-o", REF_DROPIN_LIB])
     ref_script = os.path.join(ORACLE, "build_ref.sh")
     _run(["sh", ref_script])
 

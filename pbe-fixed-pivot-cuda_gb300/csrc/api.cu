@@ -24,6 +24,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <cstdint>
+#include <cstddef>
+#include <type_traits>
 
 #include "pbe_internal.cuh"
 #include "pbe_gb300.h"
@@ -35,13 +37,17 @@ namespace {
 constexpr int kMaxDevices = 64;
 
 struct DeviceState {
-    std::once_flag once;
-    cudaError_t init_err = cudaSuccess;
+    std::mutex mu;
+    bool ready = false;           // set only once the set-up below has succeeded
     cudaMemPool_t pool = nullptr;
     int num_sms = 0;
 };
 DeviceState g_dev[kMaxDevices];
 
+// Per-device set-up (SM count, the scratch pool). A failed attempt is not
+// remembered: it is released and the next call tries again, so one failure
+// (for instance a first call made inside stream capture) does not poison the
+// device for the rest of the process.
 cudaError_t device_state(DeviceState** out)
 {
     int dev = 0;
@@ -49,8 +55,11 @@ cudaError_t device_state(DeviceState** out)
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     DeviceState& st = g_dev[dev];
-    std::call_once(st.once, [&]() {
-        cudaError_t err = cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, dev);
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (!st.ready) {
+        int sms = 0;
+        cudaMemPool_t pool = nullptr;
+        cudaError_t err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (err == cudaSuccess) {
             cudaMemPoolProps props;
             std::memset(&props, 0, sizeof(props));
@@ -58,15 +67,20 @@ cudaError_t device_state(DeviceState** out)
             props.handleTypes = cudaMemHandleTypeNone;
             props.location.type = cudaMemLocationTypeDevice;
             props.location.id = dev;
-            err = cudaMemPoolCreate(&st.pool, &props);
+            err = cudaMemPoolCreate(&pool, &props);
         }
         if (err == cudaSuccess) {
             uint64_t keep = UINT64_MAX;
-            err = cudaMemPoolSetAttribute(st.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            err = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        st.init_err = err;
-    });
-    if (st.init_err != cudaSuccess) return st.init_err;
+        if (err != cudaSuccess) {
+            if (pool) cudaMemPoolDestroy(pool);
+            return err;
+        }
+        st.num_sms = sms;
+        st.pool = pool;
+        st.ready = true;
+    }
     *out = &st;
     return cudaSuccess;
 }
@@ -279,6 +293,33 @@ int pbe_breakage_rhs_vjp(const double* N, const double* x, const double* t_q, co
                                          workspace_bytes, static_cast<cudaStream_t>(stream)));
 }
 
+int pbe_scratch_pool_usage(unsigned long long* reserved_bytes, unsigned long long* used_high_bytes,
+                           int reset_high)
+{
+    if (!reserved_bytes || !used_high_bytes) return cudaErrorInvalidValue;
+    *reserved_bytes = 0;
+    *used_high_bytes = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    DeviceState& st = g_dev[dev];
+    std::lock_guard<std::mutex> lock(st.mu);
+    if (!st.ready) return cudaSuccess;   // no pool yet: nothing was ever allocated from it
+    unsigned long long v = 0;
+    e = cudaMemPoolGetAttribute(st.pool, cudaMemPoolAttrReservedMemCurrent, &v);
+    if (e != cudaSuccess) return e;
+    *reserved_bytes = v;
+    e = cudaMemPoolGetAttribute(st.pool, cudaMemPoolAttrUsedMemHigh, &v);
+    if (e != cudaSuccess) return e;
+    *used_high_bytes = v;
+    if (reset_high) {
+        unsigned long long zero = 0;
+        e = cudaMemPoolSetAttribute(st.pool, cudaMemPoolAttrUsedMemHigh, &zero);
+    }
+    return e;
+}
+
 int pbe_set_profile_events(void* start, void* stop)
 {
     g_prof_start = static_cast<cudaEvent_t>(start);
@@ -291,10 +332,36 @@ int pbe_set_profile_events(void* start, void* stop)
 // ---------------------------------------------------------------------------
 // C++ drop-in API (pbe_cuda namespace, reference signatures)
 // ---------------------------------------------------------------------------
+// The C structs and the C++ structs must share their layout member by member,
+// so a caller may pass either through the other interface.
+#define PBE_SAME_MEMBER(CPP, C, m)                                                     \
+    static_assert(offsetof(pbe_cuda::CPP, m) == offsetof(C, m) &&                      \
+                      sizeof(pbe_cuda::CPP::m) == sizeof(((C*)nullptr)->m),            \
+                  #CPP "::" #m " and " #C "." #m " differ in offset or size")
 static_assert(sizeof(pbe_cuda::AggregationParams) == sizeof(pbe_agg_params_t),
               "AggregationParams and pbe_agg_params_t must share their layout");
 static_assert(sizeof(pbe_cuda::BreakageParams) == sizeof(pbe_brk_params_t),
               "BreakageParams and pbe_brk_params_t must share their layout");
+static_assert(std::is_standard_layout<pbe_cuda::AggregationParams>::value &&
+                  std::is_standard_layout<pbe_cuda::BreakageParams>::value,
+              "the C++ parameter structs must be standard-layout");
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, n);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, log_x0);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, inv_log_r);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, kernel_type);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, beta0);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, beta_br);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, beta_sh);
+PBE_SAME_MEMBER(AggregationParams, pbe_agg_params_t, block_size);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, n);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, n_quad);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, selection);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, S0);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, v_ref);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, alpha);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, v_min);
+PBE_SAME_MEMBER(BreakageParams, pbe_brk_params_t, block_size);
+#undef PBE_SAME_MEMBER
 
 namespace pbe_cuda {
 

@@ -17,7 +17,8 @@
 // Set-up: the first call on each device (with that device current) looks up
 // the array's device address with cudaGetSymbolAddress; in host code the
 // array's name is only a host-side stand-in and must never be handed to a
-// kernel. Make that first call before any stream capture begins.
+// kernel. Make that first call before any stream capture begins. If the
+// look-up fails, the call returns its error and the next call tries again.
 //
 // Sharing: every call on a device uses the same array and it keeps the last
 // call's contents. Each call's own kernels rewrite everything they read
@@ -43,8 +44,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
 struct NoAllocDevice {
-    std::once_flag once;
-    cudaError_t err = cudaSuccess;
+    std::mutex mu;
+    bool ready = false;        // set only once the look-up below has succeeded
     void* scratch = nullptr;   // device address of g_noalloc_scratch on this device
     int num_sms = 0;
 };
@@ -82,15 +83,20 @@ extern "C" int pbe_aggregation_rhs_noalloc(const double* N, const double* x, dou
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     NoAllocDevice& st = g_na[dev];
-    std::call_once(st.once, [&]() {
-        void* p = nullptr;
-        cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (err == cudaSuccess)
-            err = cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, dev);
-        st.scratch = p;
-        st.err = err;
-    });
-    if (st.err != cudaSuccess) return st.err;
+    {
+        // A failed look-up is not remembered: the next call retries it.
+        std::lock_guard<std::mutex> lock(st.mu);
+        if (!st.ready) {
+            void* p = nullptr;
+            int sms = 0;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            st.scratch = p;
+            st.num_sms = sms;
+            st.ready = true;
+        }
+    }
 
     AggArgs a{N, x, rhs, params->n, params->kernel_type, params->beta0, params->beta_br,
               params->beta_sh};

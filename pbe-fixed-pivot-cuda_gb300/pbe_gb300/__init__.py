@@ -35,6 +35,7 @@ from ._lib import (  # noqa: F401
     PbeError,
     check,
     error_string,
+    scratch_pool_usage,
     load,
 )
 from .rhs import (  # noqa: F401

@@ -98,6 +98,8 @@ _SIGNATURES = {
     "pbe_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "pbe_version": (ctypes.c_int, []),
     "pbe_set_profile_events": (ctypes.c_int, [_P, _P]),
+    "pbe_scratch_pool_usage": (ctypes.c_int, [ctypes.POINTER(ctypes.c_ulonglong),
+                                              ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]),
     "pbe_vjp_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int]),
     "pbe_aggregation_rhs_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(AggregationParams),
                                                _P, ctypes.c_size_t, _P]),
@@ -153,6 +155,16 @@ def load() -> ctypes.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def scratch_pool_usage(reset_high: bool = False) -> tuple[int, int]:
+    """(bytes the library's scratch pool reserves on the current device,
+    high-water mark of its bytes in use); reset_high clears the mark after
+    reading it."""
+    r, h = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
+    check(load().pbe_scratch_pool_usage(ctypes.byref(r), ctypes.byref(h), int(reset_high)),
+          "scratch pool usage")
+    return int(r.value), int(h.value)
 
 
 def error_string(code: int) -> str:

@@ -24,3 +24,10 @@ def test_reference_arm_prints_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["cpu_baseline"]["value"] == line["value"] == line["e2e"]["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    # the requested steps and warm-up are honoured, and the config equals our arm's
+    assert line["steps"] == 1 and line["warmup"] == 1
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert line["config"] == bench.run_config()
+    assert line["cpu_baseline"]["cpu_model"]

@@ -167,7 +167,8 @@ def test_flocculation_two_stage_adjoint_full_size():
     """n = 3840, 200 RK4 steps, checkpoints every 20, shear switching at step
     100: the forward equals the serial oracle's run of the same workload
     (committed golden), the gradient is finite and matches central differences
-    for a few initial bins and for the shear coefficient of both stages."""
+    for a few initial bins, the shear coefficient, the selection prefactor S0
+    and the power-law exponent a of both stages."""
     torch = _torch()
     cfg = pg.grids.config_flocculation_adjoint()
     x, N0 = cfg["x"], cfg["N0"]
@@ -208,3 +209,37 @@ def test_flocculation_two_stage_adjoint_full_size():
         am[k].beta_sh -= h
         fd = (L(agg_=ap) - L(agg_=am)) / (2 * h)
         assert abs(fd - ga[k, 2]) <= 1e-5 * abs(ga[k, 2]) + 1e-11 * L0 / h, (k, fd, ga[k, 2])
+    # selection prefactor S0 and power-law exponent a of both stages
+    for k in range(2):
+        for name, g in (("S0", gb[k, 0]), ("alpha", gb[k, 2])):
+            h = 1e-6 * getattr(brk[k], name)
+            bp = [type(b).from_buffer_copy(b) for b in brk]
+            bm = [type(b).from_buffer_copy(b) for b in brk]
+            setattr(bp[k], name, getattr(bp[k], name) + h)
+            setattr(bm[k], name, getattr(bm[k], name) - h)
+            fd = (L(brk_=bp) - L(brk_=bm)) / (2 * h)
+            assert abs(fd - g) <= 1e-5 * abs(g) + 1e-11 * L0 / h, (k, name, fd, g)
+
+
+def test_flocculation_adjoint_20_steps_matches_serial_oracle_adjoint():
+    """The flocculation workload at full width (n = 3840) cut to 20 steps
+    (shear switching at step 10), checkpoints every 5: every gradient the tape
+    returns -- dL/dN(0), dL/dbeta_br, dL/dbeta_sh, dL/dS0 and dL/da of both
+    stages -- against the serial FP64 discrete adjoint of the oracle (no
+    checkpointing; tests/golden/flocculation_adjoint_20steps.npz, generator
+    make_flocculation_adjoint_golden.py). Bounds as the small-case oracle
+    comparison: rtol 1e-10 on dL/dN(0), 1e-9 on the coefficients."""
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                                "flocculation_adjoint_20steps.npz"))
+    steps, switch = int(gold["n_steps"]), int(gold["switch_step"])
+    cfg = pg.grids.config_flocculation_adjoint(n_steps=steps, switch_step=switch)
+    NT, gN0, ga, gb = run_tape(cfg["x"], cfg["N0"], cfg["t_q"], cfg["bw_q"], cfg["agg_sets"],
+                               cfg["brk_sets"], cfg["step_set"], cfg["dt"], 5, cfg["lam_T"])
+    np.testing.assert_allclose(NT, gold["N_T"], rtol=1e-11, atol=1e-11 * np.abs(cfg["N0"]).max())
+    np.testing.assert_allclose(gN0, gold["gN0"], rtol=1e-10, atol=1e-10 * np.abs(gold["gN0"]).max())
+    np.testing.assert_allclose(ga[:, 1:], gold["g_agg"][:, 1:], rtol=1e-9)       # beta_br, beta_sh
+    np.testing.assert_allclose(gb[:, [0, 2]], gold["g_brk"][:, [0, 2]], rtol=1e-9)  # S0, a
+    print("20-step adjoint vs oracle: max rel dL/dN0 %.2e, coefficients %s vs %s" % (
+        float(np.max(np.abs(gN0 - gold["gN0"])) / np.abs(gold["gN0"]).max()),
+        np.r_[ga[:, 1:].ravel(), gb[:, [0, 2]].ravel()].tolist(),
+        np.r_[gold["g_agg"][:, 1:].ravel(), gold["g_brk"][:, [0, 2]].ravel()].tolist()))
