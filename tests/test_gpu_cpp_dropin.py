@@ -45,7 +45,10 @@ DOCUMENTED = {
     "aggregation_constant": {"N_tot error": 1.7e-4, "M1 error": None},
     "aggregation_sum": {"M0 error": 1.4e-4, "M1 error": 1.6e-4},
     "aggregation_product": {"M0 error": 1.7e-4, "M2 error": 4.8e-3, "M1 error": 1.6e-4},
-    "breakage_linear_symmetricbinary": {"N_tot error": 1e-4, "V_tot error": None},
+    # docs/examples.md gives "N_tot error ~1e-04" here, but the program as shipped
+    # prints machine precision on both libraries: with the linear selection
+    # function dN_tot/dt = S0 M1 / v_ref is constant, so explicit Euler is exact
+    "breakage_linear_symmetricbinary": {"N_tot error": None, "V_tot error": None},
     "breakage_linear_uniform": {"M0 error": 2.2e-4, "M1 error": 1.8e-4},
 }
 
@@ -150,17 +153,27 @@ def test_reference_example_same_output_on_both_libraries(example_bins, name):
     ref = _run(example_bins[(name, "ref")])
     n = _compare_outputs(ours, ref, name)
     assert n > 10
-    assert "WARN" not in ours
-    errs = _final_errors(ours)
+    # the words (PASS / WARN verdicts, labels) are the same too
+    words = lambda txt: [_NUM.sub("#", ln) for ln in txt.splitlines() if "Wall time" not in ln]  # noqa: E731
+    assert words(ours) == words(ref), "%s: the printed text differs" % name
+    errs, rerrs = _final_errors(ours), _final_errors(ref)
+    notes = []
     for key, want in DOCUMENTED.get(name, {}).items():
-        assert key in errs, "%s: no '%s' line in:\n%s" % (name, key, ours[-1500:])
+        assert key in errs and key in rerrs, "%s: no '%s' line in:\n%s" % (name, key, ours[-1500:])
         got = errs[key]
+        in_doc = (rerrs[key] < 1e-10) if want is None else (0.4 * want <= rerrs[key] <= 2.5 * want)
+        if not in_doc:
+            # the reference's own program disagrees with its documentation: the
+            # comparison with the reference's kernels above is the check
+            notes.append("%s: reference prints %g, docs give %s" % (key, rerrs[key], want))
+            continue
         if want is None:
             assert got < 1e-10, "%s: %s = %g, documented at machine precision" % (name, key, got)
         else:
             assert 0.4 * want <= got <= 2.5 * want, \
                 "%s: %s = %g, documented ~%g" % (name, key, got, want)
-    print("%s: %d printed numbers equal on both libraries; final errors %s" % (name, n, errs))
+    print("%s: %d printed numbers equal on both libraries; final errors %s (reference %s)%s"
+          % (name, n, errs, rerrs, ("; " + "; ".join(notes)) if notes else ""))
 
 
 def test_cpp_api_bitwise_equals_c_abi(tmp_path):
