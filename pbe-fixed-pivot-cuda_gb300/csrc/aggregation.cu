@@ -39,9 +39,11 @@
 // reproducible. SCATTER mode: every task flushes its bins with FP64 atomicAdd.
 // =============================================================================
 #include <cstdlib>
+#include <cstring>
 
 #include "pbe_internal.cuh"
 #include "agg_tile.cuh"
+#include "agg_lane.cuh"
 
 namespace pbe_gb300 {
 namespace {
@@ -83,6 +85,8 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         const double ai = cbrt(xi);
         const double iai = 1.0 / ai;
         ws.h[i] = hi;
+        ws.Ncp[i] = Ni;          // 256-byte aligned copies: bulk-copy sources of the lane tasks
+        ws.xcp[i] = xi;
         ws.a[i] = ai;
         ws.ia[i] = iai;
         ws.inv_dx[i] = (i < n - 1) ? 1.0 / (x[i + 1] - xi) : 0.0;
@@ -168,6 +172,7 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         ws.mom[5] = geo ? 1.0 : 0.0;
         ws.mom[6] = mx;
         ws.counter[0] = 0;          // task counter of the main kernel
+        ws.counter[4] = 0;          // lane-task staging error flag
         ws.counter[1] = d0_s;       // lags d >= counter[1] have lo(j, j+d) = j + d
         ws.counter[3] = 0;          // contributors to bin n-1 done (clip tasks + top tile)
     }
@@ -250,16 +255,21 @@ __device__ __forceinline__ void first_bin_done(double* rhs, int I, const AggWs& 
 // is evaluated once. Thread-private partial sums are reduced in a fixed
 // order, so for a given T the gather result is bitwise reproducible.
 // ---------------------------------------------------------------------------
-template <int K, bool SCATTER>
+template <int K, bool SCATTER, bool STAGE>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile,
-                int ntasks, int nclip, double b0, double bbr, double bsh, int T, int Cg)
+                int ntasks, int nclip, double b0, double bbr, double bsh, int T, int Cg,
+                int ntasks_lane, int lane_C)
 {
-    extern __shared__ double red[];               // [2 W][kMainThreads]
+    // [2 W][kMainThreads] tile reductions, or the lane tasks' sums and staged
+    // windows (bulk-copy destinations: 16-byte aligned offsets)
+    extern __shared__ __align__(128) double red[];
     __shared__ TileShared sm;
     __shared__ int s_task[kMaxGroups];
     __shared__ int s_last[kMaxGroups];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_flag;
 
     const int tid = threadIdx.x;
     AggCellView v;
@@ -273,6 +283,53 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     v.b0 = b0; v.bbr = bbr; v.bsh = bsh;
 #pragma unroll
     for (int q = 0; q < 5; ++q) v.M[q] = ws.mom[q];
+
+    if (ntasks_lane > 0 && v.geo) {
+        // lane-block tasks (agg_lane.cuh): the whole CTA works on one task
+        if (tid == 0) {
+            mbar_init(&s_bar, 1);
+            s_flag = 0;
+        }
+        __syncthreads();
+        const LaneSmem lsm{red, red + 2 * kLaneWarps * 32, red + 2 * kLaneWarps * 32 + kLaneWinMax,
+                           red + 2 * kLaneWarps * 32 + 2 * kLaneWinMax};
+        const LaneArgs la{ws.Ncp, ws.xcp, ws.lpart, ws.cticket, ws.counter + 4, lane_C};
+        const TileGroup G0{0, tid, kMainThreads};
+        unsigned phase = 0;
+        for (;;) {
+            if (tid == 0) s_task[0] = atomicAdd(ws.counter, 1);
+            __syncthreads();
+            int task = s_task[0];
+            const int stop = s_flag;
+            __syncthreads();
+            if (task >= ntasks_lane || stop) break;
+            if (task < nclip) {
+                const double sc = group_sum(clip_part_sum<K>(v, task, nclip, G0), sm, G0);
+                if (tid == 0) {
+                    if constexpr (SCATTER) {
+                        if (sc != 0.0) atomicAdd(rhs + (n - 1), sc);
+                    } else {
+                        ws.clip_part[task] = sc;
+                        clip_contributor_done(rhs, n, ws, nclip);
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
+            task -= nclip;
+            int c = 0, cnt = 0;
+            for (;;) {
+                cnt = lane_chunk_blocks(n, c, lane_C);
+                if (cnt == 0 || task < cnt) break;
+                task -= cnt;
+                ++c;
+            }
+            if (cnt == 0) continue;
+            lane_task<K, SCATTER, STAGE>(v, ws, la, rhs, task, c, nclip, lsm, &s_bar, phase, &s_flag);
+        }
+        return;
+    }
+
     // groups of T threads pull tasks on their own (no CTA-wide barrier in the loop)
     const int g = tid / T;
     const TileGroup G{g, tid - g * T, T};
@@ -413,6 +470,22 @@ int agg_group_size_chunked()
     return forced ? forced : 32;
 }
 
+// Pair tasks on geometric grids: 1 = lane blocks with bulk-copy staging of the
+// j-side operands (default), 2 = lane blocks reading them through the
+// read-only cache, 0 = the tile tasks of every grid. PBE_GB300_AGG_PATH
+// ("lane", "lane_ldg", "tile") overrides.
+int agg_lane_mode()
+{
+    static const int mode = []() {
+        const char* e = std::getenv("PBE_GB300_AGG_PATH");
+        if (!e) return 1;
+        if (std::strcmp(e, "tile") == 0) return 0;
+        if (std::strcmp(e, "lane_ldg") == 0) return 2;
+        return 1;
+    }();
+    return mode;
+}
+
 // Tasks that sum the clipped pairs (about n + q^2 pairs on a grid with q bins
 // per octave, more on generic grids), spread over parts of ~1024 lags or rows.
 int agg_clip_tasks(int n)
@@ -456,14 +529,25 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     const long long ntasks_ll = ngather + nclip;
     if (ntasks_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
     const int ntasks = static_cast<int>(ntasks_ll);
+    // lane-block tasks, taken instead of the tiles when the grid turns out
+    // geometric (decided on the device by the prep kernel)
+    const int lane_mode = agg_lane_mode();
+    const int lane_C = lane_chunk_len(n);
+    const long long nlane_ll = lane_mode ? lane_tasks(n, lane_C) + nclip : 0;
+    if (nlane_ll > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const int ntasks_lane = static_cast<int>(nlane_ll);
     // chunked gather: many tasks of few lags; single warps keep the fixed-order
     // reduction (2 W T adds per task) small next to a chunk's pairs
     const int T = (Cg < n) ? agg_group_size_chunked() : agg_group_size(ntasks, num_sms);
-    const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
+    long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
+    if (ntasks_lane > need) need = ntasks_lane;
     const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
     const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
-    cudaError_t e = cudaFuncSetAttribute(agg_main_kernel<K, SC>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static_assert(sizeof(double) * (2 * kLaneWarps * 32 + 3 * kLaneWinMax) <=
+                      sizeof(double) * TileSlots<true>::rows * kMainThreads,
+                  "lane-task shared memory must fit the tile reduction buffer");
+    auto kern = (lane_mode == 2) ? agg_main_kernel<K, SC, false> : agg_main_kernel<K, SC, true>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(ws.counter, 0, 8 * sizeof(int), s);   // prep's block tickets
@@ -471,9 +555,8 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
-    agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile,
-                                                            ntasks, nclip, a.beta0, a.beta_br,
-                                                            a.beta_sh, T, Cg);
+    kern<<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, ntasks, nclip, a.beta0,
+                                          a.beta_br, a.beta_sh, T, Cg, ntasks_lane, lane_C);
     if (prof) cudaEventRecord(g_prof_stop, s);
     return cudaGetLastError();
 }

@@ -221,7 +221,11 @@ struct AggWs {
     double* cpart;     // [ntile * agg_chunk_bound(n) * 2 kTileW] lag-chunk partials of R, TH
     int*    cticket;   // [ntile] lag-chunk tasks of the tile done
     int*    counter;   // [8]  [0] task counter, [1] first lag with Ld[d] == d,
-                       //      [2] prep blocks done, [3] bin n-1 contributors done
+                       //      [2] prep blocks done, [3] bin n-1 contributors done,
+                       //      [4] a staging wait of the lane tasks gave up
+    double* Ncp;       // [n + 2] copy of N, 256-byte aligned (bulk-copy source)
+    double* xcp;       // [n + 2] copy of x, 256-byte aligned (bulk-copy source)
+    double* lpart;     // [lane_partial_doubles(n)] lane-task chunk partials
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
@@ -244,6 +248,51 @@ __host__ __device__ constexpr int agg_chunk_bound(int n)
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// Lane-block pair tasks (agg_lane.cuh): blocks of kLaneBins output bins
+// aligned to the top of the grid, cut into lag chunks of lane_chunk_len(n)
+// lags (at least n / 16, so at most 17 chunks per block). Task (block t,
+// chunk c) has the index sum_{c' < c} lane_chunk_blocks(c') + t; its chunk
+// partial (R, TH of 32 slots) is stored under that index.
+constexpr int kLaneBins = 32;
+constexpr int kLaneMinChunk = 256;                  // shortest lag chunk
+
+__host__ __device__ constexpr int lane_blocks(int n) { return (n + kLaneBins - 1) / kLaneBins; }
+// Highest slot of block t (slots exist up to n - 2); < 0 when the block has none.
+__host__ __device__ constexpr int lane_block_smax(int n, int t)
+{
+    return (n - kLaneBins * t - 1) < n - 2 ? (n - kLaneBins * t - 1) : n - 2;
+}
+// Lag chunk length: at least n / 16, a multiple of 64, at least kLaneMinChunk.
+__host__ __device__ constexpr int lane_chunk_len(int n)
+{
+    const int c = (((n + 15) / 16) + 63) / 64 * 64;
+    return c < kLaneMinChunk ? kLaneMinChunk : c;
+}
+// Chunks of block t: every block has chunk 0; chunk c >= 1 when c C <= smax_t.
+__host__ __device__ constexpr int lane_block_chunks(int n, int t, int C)
+{
+    return lane_block_smax(n, t) < 0 ? 1 : lane_block_smax(n, t) / C + 1;
+}
+// Blocks that have chunk c (they are blocks 0 .. cnt-1: smax_t falls with t).
+__host__ __device__ constexpr int lane_chunk_blocks(int n, int c, int C)
+{
+    if (c == 0) return lane_blocks(n);
+    if (static_cast<long long>(c) * C > n - 2) return 0;
+    const long long m = (n - 1 - static_cast<long long>(c) * C) / kLaneBins + 1;
+    return m < lane_blocks(n) ? static_cast<int>(m) : lane_blocks(n);
+}
+__host__ __device__ constexpr long long lane_tasks(int n, int C)
+{
+    long long s = 0;
+    for (int c = 0; lane_chunk_blocks(n, c, C) > 0; ++c) s += lane_chunk_blocks(n, c, C);
+    return s;
+}
+// Doubles of lane-task chunk partials: tasks x (R, TH) x kLaneBins.
+__host__ __device__ constexpr size_t lane_partial_doubles(int n)
+{
+    return static_cast<size_t>(lane_tasks(n, lane_chunk_len(n))) * 2 * kLaneBins;
+}
+
 // Size of the aggregation scratch for n bins, equal to agg_ws_layout(n) below
 // (kept in step with it; usable in constant expressions).
 constexpr size_t agg_ws_bytes(int n)
@@ -258,7 +307,9 @@ constexpr size_t agg_ws_bytes(int n)
          + align256(sizeof(double) * 2 * kTileW * static_cast<size_t>(agg_tiles(n)) *
                     static_cast<size_t>(agg_chunk_bound(n)))
          + align256(sizeof(int) * static_cast<size_t>(agg_tiles(n)))
-         + align256(sizeof(int) * 8);
+         + align256(sizeof(int) * 8)
+         + 2 * align256(sizeof(double) * (static_cast<size_t>(n) + 2))
+         + align256(sizeof(double) * lane_partial_doubles(n));
 }
 
 // Carves the aggregation scratch out of `base` (may be null to query the size).
@@ -286,6 +337,9 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
                                                  static_cast<size_t>(agg_chunk_bound(n))));
     w.cticket   = reinterpret_cast<int*>(take(sizeof(int) * nt));
     w.counter   = reinterpret_cast<int*>(take(sizeof(int) * 8));
+    w.Ncp       = reinterpret_cast<double*>(take(sizeof(double) * (static_cast<size_t>(n) + 2)));
+    w.xcp       = reinterpret_cast<double*>(take(sizeof(double) * (static_cast<size_t>(n) + 2)));
+    w.lpart     = reinterpret_cast<double*>(take(sizeof(double) * lane_partial_doubles(n)));
     if (ws) *ws = w;
     return off;
 }
