@@ -255,21 +255,17 @@ __device__ __forceinline__ void first_bin_done(double* rhs, int I, const AggWs& 
 // is evaluated once. Thread-private partial sums are reduced in a fixed
 // order, so for a given T the gather result is bitwise reproducible.
 // ---------------------------------------------------------------------------
-template <int K, bool SCATTER, bool STAGE>
+template <int K, bool SCATTER>
 __global__ void __launch_bounds__(kMainThreads, 2)
 agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double* __restrict__ rhs, AggWs ws, int n, int ntile,
                 int ntasks, int nclip, double b0, double bbr, double bsh, int T, int Cg,
-                int ntasks_lane, int lane_C)
+                int ntasks_lane)
 {
-    // [2 W][kMainThreads] tile reductions, or the lane tasks' sums and staged
-    // windows (bulk-copy destinations: 16-byte aligned offsets)
-    extern __shared__ __align__(128) double red[];
+    extern __shared__ double red[];               // [2 W][kMainThreads]
     __shared__ TileShared sm;
     __shared__ int s_task[kMaxGroups];
     __shared__ int s_last[kMaxGroups];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_flag;
 
     const int tid = threadIdx.x;
     AggCellView v;
@@ -284,51 +280,8 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 #pragma unroll
     for (int q = 0; q < 5; ++q) v.M[q] = ws.mom[q];
 
-    if (ntasks_lane > 0 && v.geo) {
-        // lane-block tasks (agg_lane.cuh): the whole CTA works on one task
-        if (tid == 0) {
-            mbar_init(&s_bar, 1);
-            s_flag = 0;
-        }
-        __syncthreads();
-        const LaneSmem lsm{red, red + 2 * kLaneWarps * 32, red + 2 * kLaneWarps * 32 + kLaneWinMax,
-                           red + 2 * kLaneWarps * 32 + 2 * kLaneWinMax};
-        const LaneArgs la{ws.Ncp, ws.xcp, ws.lpart, ws.cticket, ws.counter + 4, lane_C};
-        const TileGroup G0{0, tid, kMainThreads};
-        unsigned phase = 0;
-        for (;;) {
-            if (tid == 0) s_task[0] = atomicAdd(ws.counter, 1);
-            __syncthreads();
-            int task = s_task[0];
-            const int stop = s_flag;
-            __syncthreads();
-            if (task >= ntasks_lane || stop) break;
-            if (task < nclip) {
-                const double sc = group_sum(clip_part_sum<K>(v, task, nclip, G0), sm, G0);
-                if (tid == 0) {
-                    if constexpr (SCATTER) {
-                        if (sc != 0.0) atomicAdd(rhs + (n - 1), sc);
-                    } else {
-                        ws.clip_part[task] = sc;
-                        clip_contributor_done(rhs, n, ws, nclip);
-                    }
-                }
-                __syncthreads();
-                continue;
-            }
-            task -= nclip;
-            int c = 0, cnt = 0;
-            for (;;) {
-                cnt = lane_chunk_blocks(n, c, lane_C);
-                if (cnt == 0 || task < cnt) break;
-                task -= cnt;
-                ++c;
-            }
-            if (cnt == 0) continue;
-            lane_task<K, SCATTER, STAGE>(v, ws, la, rhs, task, c, nclip, lsm, &s_bar, phase, &s_flag);
-        }
-        return;
-    }
+    // geometric grids run the lane-block kernel instead (launched just before)
+    if (ntasks_lane > 0 && v.geo) return;
 
     // groups of T threads pull tasks on their own (no CTA-wide barrier in the loop)
     const int g = tid / T;
@@ -440,6 +393,94 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
     }
 }
 
+// ---------------------------------------------------------------------------
+// lane: persistent CTAs pulling lane-block tasks (agg_lane.cuh) on verified
+// geometric grids -- clip tasks first, then (block, lag chunk) tasks chunk by
+// chunk, top blocks first. Returns at once on other grids (the tile kernel
+// launched after it takes them). It needs fewer registers than the tile
+// kernel, so more CTAs fit on an SM.
+// ---------------------------------------------------------------------------
+#ifndef PBE_LANE_CTAS
+#define PBE_LANE_CTAS 3
+#endif
+constexpr int kLaneCtas = PBE_LANE_CTAS;           // CTAs per SM (register budget)
+
+template <int K, bool SCATTER, bool STAGE>
+__global__ void __launch_bounds__(kMainThreads, kLaneCtas)
+agg_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                double* __restrict__ rhs, AggWs ws, int n, int ntasks_lane, int nclip,
+                double b0, double bbr, double bsh, int lane_C)
+{
+    // per-warp slot sums, then the staged windows (16-byte aligned offsets)
+    extern __shared__ __align__(128) double lsmem[];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_flag;
+    __shared__ int s_task;
+    __shared__ double s_wsum[kMainThreads / 32];
+
+    if (ws.mom[5] == 0.0) return;                  // not geometric: the tile kernel runs
+    const int tid = threadIdx.x;
+    AggCellView v;
+    v.x = x; v.Nk = N; v.Hk = ws.h; v.Nj = N; v.Hj = ws.h; v.Aj = N; v.AHj = ws.h;
+    v.Fs = (K == 2) ? ws.h : N;
+    v.a = ws.a; v.ia = ws.ia; v.inv_dx = ws.inv_dx;
+    v.Bd = ws.Bd; v.Sd = ws.Sd; v.Ld = ws.Ld;
+    v.n = n;
+    v.D0 = ws.counter[1];
+    v.geo = true;
+    v.b0 = b0; v.bbr = bbr; v.bsh = bsh;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) v.M[q] = ws.mom[q];
+
+    if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        s_flag = 0;
+    }
+    __syncthreads();
+    constexpr int kRed = 2 * kLaneWarps * kLaneBins;     // per-warp R, TH of every slot
+    const LaneSmem lsm{lsmem, lsmem + kRed, lsmem + kRed + kLaneWinMax,
+                       lsmem + kRed + 2 * kLaneWinMax};
+    const LaneArgs la{ws.Ncp, ws.xcp, ws.lpart, ws.cticket, ws.counter + 4, lane_C};
+    const TileGroup G0{0, tid, kMainThreads};
+    unsigned phase = 0;
+    for (;;) {
+        if (tid == 0) s_task = atomicAdd(ws.counter, 1);
+        __syncthreads();
+        int task = s_task;
+        const int stop = s_flag;
+        __syncthreads();
+        if (task >= ntasks_lane || stop) break;
+        if (task < nclip) {
+            // a part of the pairs clipped at x[n-1], summed over the CTA in a fixed order
+            double sc = warp_sum(clip_part_sum<K>(v, task, nclip, G0));
+            if ((tid & 31) == 0) s_wsum[tid >> 5] = sc;
+            __syncthreads();
+            if (tid == 0) {
+                sc = 0.0;
+                for (int w = 0; w < kMainThreads / 32; ++w) sc += s_wsum[w];
+                if constexpr (SCATTER) {
+                    if (sc != 0.0) atomicAdd(rhs + (n - 1), sc);
+                } else {
+                    ws.clip_part[task] = sc;
+                    clip_contributor_done(rhs, n, ws, nclip);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        task -= nclip;
+        int c = 0, cnt = 0;
+        for (;;) {
+            cnt = lane_chunk_blocks(n, c, lane_C);
+            if (cnt == 0 || task < cnt) break;
+            task -= cnt;
+            ++c;
+        }
+        if (cnt == 0) continue;
+        lane_task<K, SCATTER, STAGE>(v, ws, la, rhs, task, c, nclip, lsm, &s_bar, phase, &s_flag);
+    }
+}
+
 // Threads per tile task. A smaller group keeps fewer partial sums per slot
 // (the fixed-order reduction costs 2 (W+1) T FP64 adds per task) but runs
 // each task longer; with few tasks per group slot the last wave idles.
@@ -539,24 +580,35 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
     // chunked gather: many tasks of few lags; single warps keep the fixed-order
     // reduction (2 W T adds per task) small next to a chunk's pairs
     const int T = (Cg < n) ? agg_group_size_chunked() : agg_group_size(ntasks, num_sms);
-    long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
-    if (ntasks_lane > need) need = ntasks_lane;
+    const long long need = (ntasks + (kMainThreads / T) - 1) / (kMainThreads / T);
     const int grid = static_cast<int>(need < 2LL * num_sms ? need : 2LL * num_sms);
     const size_t smem = sizeof(double) * TileSlots<true>::rows * kMainThreads;
-    static_assert(sizeof(double) * (2 * kLaneWarps * 32 + 3 * kLaneWinMax) <=
-                      sizeof(double) * TileSlots<true>::rows * kMainThreads,
-                  "lane-task shared memory must fit the tile reduction buffer");
-    auto kern = (lane_mode == 2) ? agg_main_kernel<K, SC, false> : agg_main_kernel<K, SC, true>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(agg_main_kernel<K, SC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+    auto lkern = (lane_mode == 2) ? agg_lane_kernel<K, SC, false> : agg_lane_kernel<K, SC, true>;
+    const size_t lsmem = sizeof(double) * (2 * kLaneWarps * kLaneBins + 3 * kLaneWinMax);
+    const long long lcap = static_cast<long long>(kLaneCtas) * num_sms;
+    const int lgrid = static_cast<int>(ntasks_lane < lcap ? ntasks_lane : lcap);
+    if (lane_mode) {
+        e = cudaFuncSetAttribute(lkern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(lsmem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(lkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (e != cudaSuccess) return e;
+    }
     e = cudaMemsetAsync(ws.counter, 0, 8 * sizeof(int), s);   // prep's block tickets
     if (e != cudaSuccess) return e;
     agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
-    kern<<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, ntasks, nclip, a.beta0,
-                                          a.beta_br, a.beta_sh, T, Cg, ntasks_lane, lane_C);
+    if (lane_mode && lgrid > 0)
+        lkern<<<lgrid, kMainThreads, lsmem, s>>>(a.N, a.x, a.rhs, ws, n, ntasks_lane, nclip,
+                                                 a.beta0, a.beta_br, a.beta_sh, lane_C);
+    agg_main_kernel<K, SC><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.rhs, ws, n, ntile, ntasks,
+                                                            nclip, a.beta0, a.beta_br, a.beta_sh,
+                                                            T, Cg, ntasks_lane);
     if (prof) cudaEventRecord(g_prof_stop, s);
     return cudaGetLastError();
 }
