@@ -91,6 +91,59 @@ def fp64_instr_per_launch(x) -> int:
     cnt = np.where(L <= n - 2, np.maximum(0, n - 1 - L), 0)
     return (FP64_PHASE1 * int(cnt[d_all < D0].sum()) + FP64_PHASE2 * int(cnt[d_all >= D0].sum())
             + 4 * clipped)
+# Lane-block pair kernel (agg_lane_kernel, geometric grids): one slot per lane,
+# blocks of 32 bins, lag chunks of max(256, n/16 rounded up to 64) lags split
+# evenly over 8 warps. Per non-clipped pair 4 FP64 instructions for
+# Brownian + shear (q = B N_j + S x_j N_j: DMUL + DFMA; its sum: DADD; its
+# weighted sum: DFMA); every run of lags with one bracket offset, in every
+# warp's share, costs 2 DFMA per lane when it is folded in; 4 per clipped pair.
+LANE_BINS, LANE_WARPS, LANE_MIN_CHUNK, LAG_CLIP = 32, 8, 256, 0x3fffffff
+
+
+def lane_fp64_instr_per_launch(x) -> int:
+    n = len(x)
+    v = x[0] + x
+    L = np.searchsorted(x, v, side="right") - 1          # bracket of x_0 + x_d
+    L = np.where(v >= x[-1], LAG_CLIP, L)
+    d_all = np.arange(n)
+    jlo = np.where(L >= LAG_CLIP, 0, np.maximum(0, n - 1 - L))
+    clipped = int(np.maximum(0, (n - 1 - d_all) - jlo + 1).sum())
+    pairs = int(np.where(L <= n - 2, np.maximum(0, n - 1 - L), 0).sum())
+    e = L - d_all
+    chg = np.concatenate([[0], np.cumsum(e[1:] != e[:-1])])   # run starts at d >= 1
+    C = max(LANE_MIN_CHUNK, ((n + 15) // 16 + 63) // 64 * 64)
+    nblk = (n + LANE_BINS - 1) // LANE_BINS
+    ts, cs = [], []
+    c = 0
+    while True:
+        if c == 0:
+            cnt = nblk
+        elif c * C > n - 2:
+            cnt = 0
+        else:
+            cnt = min(nblk, (n - 1 - c * C) // LANE_BINS + 1)
+        if cnt == 0:
+            break
+        ts.append(np.arange(cnt))
+        cs.append(np.full(cnt, c))
+        c += 1
+    t = np.concatenate(ts)
+    c = np.concatenate(cs)
+    smax = np.minimum(n - LANE_BINS * t - 1, n - 2)
+    dA = c * C
+    dB = np.minimum(dA + C, smax + 1)
+    Lc = np.where(L >= LAG_CLIP, np.iinfo(np.int64).max, L)
+    dB = np.clip(np.searchsorted(Lc, smax, side="right"), dA, np.maximum(dA, dB))
+    per = (dB - dA + LANE_WARPS - 1) // LANE_WARPS
+    runs = 0
+    for w in range(LANE_WARPS):
+        d0 = dA + w * per
+        d1 = np.minimum(dB, d0 + per)
+        ok = d1 > d0
+        runs += int((1 + chg[np.maximum(d1 - 1, 0)] - chg[np.minimum(d0, n - 1)])[ok].sum())
+    return 4 * pairs + 2 * 32 * runs + 4 * clipped
+
+
 # dram__bytes_read.sum + dram__bytes_write.sum of one agg_main_kernel launch on
 # this workload, read from an ncu capture of that launch (L2 flushed before it,
 # as in the timed loop); not measured by this script.
@@ -974,7 +1027,7 @@ def main():
 
     peak = fp64_peak_tflops(stream)
     mk = statistics.mean(main_ms) * 1e-3 if main_ms else None
-    instr = fp64_instr_per_launch(x)
+    instr = lane_fp64_instr_per_launch(x)
     # FP64 pipe: every FP64 instruction (DFMA, DMUL, DADD) takes one issue slot
     # of the pipe per thread; the DFMA-chain probe runs it at peak/2 slots per
     # second (2 flops per DFMA).
@@ -983,7 +1036,7 @@ def main():
     ref_equiv = FLOPS_PER_PAIR * PAIRS / mk / 1e12 if mk else None
     roofline = {
         "bound": "fp64",
-        "kernel": "agg_main_kernel<5>",
+        "kernel": "agg_lane_kernel<5> (+ agg_main_kernel<5>, which returns at once on this grid)",
         "achieved": round(achieved, 4) if achieved else None,
         "peak": round(slots_peak, 4) if slots_peak else None,
         "unit": "T FP64 instr/s",
@@ -994,8 +1047,7 @@ def main():
         "algo_bytes": ALGO_BYTES_PER_LAUNCH,
         "kernel_ms": round(mk * 1e3, 5) if mk else None,
         "fp64_instr_per_launch": instr,
-        "fp64_instr_source": "instruction model of the tile kernel on this grid (within 3 % of "
-                             "ncu's FP64 instruction counters)",
+        "fp64_instr_source": "instruction model of the lane-block kernel on this grid",
         "peak_source": "DFMA-chain probe timed in this run (libpbe_probe.so), of measured; "
                        "MEASURED_PEAKS.json has no FP64 entry",
         "reference_equivalent_tflops": round(ref_equiv, 4) if ref_equiv else None,

@@ -13,9 +13,22 @@
 //   dL/dtheta += sum_q (df/dtheta at Y_q)^T a_q,     h = dt/2, c = dt/6,
 // where J^T a is the VJP kernels' dL/dN for lambda = a (vjp.cu). Cost: one
 // forward, one recomputed forward and four VJPs per step.
+//
+// The pivots, quadrature table and coefficient sets do not change during a
+// call, so each call first writes the grid-only tables of every parameter set
+// (aggregation: cube roots, 1/dx, lag tables, geometric flag; breakage:
+// fragment brackets, run starts, the selection function per bin) into that
+// set's workspace, and every RHS then recomputes only its N-dependent part
+// (agg_stage_launch, brk_stage_launch): bitwise the drop-in calls' result.
+// A whole forward and a whole backward call are captured as CUDA graphs (on
+// internal copies of N, lambda_T and the gradients, so the caller's pointers
+// may change between calls; recaptured when x, t_q or bw_q move);
+// PBE_GB300_TAPE_GRAPH=0 launches the kernels one by one instead.
 // =============================================================================
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <new>
 #include <vector>
 
@@ -36,7 +49,19 @@ struct pbe_rk4_tape {
     std::vector<void*> allocs;
     double *ckpt = nullptr, *segY = nullptr, *k = nullptr, *acc = nullptr, *Y = nullptr;
     double *Ncur = nullptr, *lam = nullptr, *lsum = nullptr, *a = nullptr, *mu = nullptr;
-    void *agg_ws = nullptr, *brk_ws = nullptr, *vjp_ws = nullptr;
+    // one aggregation / breakage workspace per parameter set: the grid-only
+    // tables (written by a tables pass at the start of every forward and
+    // backward call) stay, the stage calls recompute only what depends on N
+    std::vector<void*> agg_ws, brk_ws;
+    void* vjp_ws = nullptr;
+    // whole forward and backward calls captured as CUDA graphs, on internal
+    // buffers (Nio, lam_in, gN_out, g_int), keyed by the pivot and quadrature
+    // pointers; the caller's arrays are copied in and out around each launch
+    bool use_graphs = true;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
+    const double *fwd_key[3] = {nullptr, nullptr, nullptr}, *bwd_key[3] = {nullptr, nullptr, nullptr};
+    double *Nio = nullptr, *lam_in = nullptr, *gN_out = nullptr, *g_int = nullptr;
 };
 
 namespace pbe_gb300 {
@@ -84,19 +109,42 @@ inline int blocks(int n) { return (n + 255) / 256; }
 
 int set_of(const pbe_rk4_tape* t, int s) { return t->step_set.empty() ? 0 : t->step_set[s]; }
 
+// Grid-only tables of every parameter set (pivots, quadrature table and
+// coefficients are fixed for the duration of a forward or backward call).
+cudaError_t tables(pbe_rk4_tape* t, const double* N, cudaStream_t s)
+{
+    cudaError_t e = cudaSuccess;
+    for (int m = 0; m < t->n_sets && e == cudaSuccess; ++m) {
+        if (t->kernel >= 0) {
+            const pbe_agg_params_t& p = t->agg[m];
+            AggArgs a{N, t->x, t->k, t->n, t->kernel, p.beta0, p.beta_br, p.beta_sh};
+            e = agg_tables_launch(a, t->agg_ws[m], t->num_sms, s);
+        }
+        if (e == cudaSuccess && t->selection >= 0) {
+            const pbe_brk_params_t& p = t->brk[m];
+            BrkArgs b{N, t->x, t->t_q, t->bw_q, t->k, t->n, t->nq, t->selection, p.S0, p.v_ref,
+                      p.alpha, p.v_min};
+            e = brk_tables_launch(b, t->brk_ws[m], s);
+        }
+    }
+    return e;
+}
+
+// k = RHS(Yin) with parameter set m, on the set's workspaces (bitwise the
+// result of the drop-in calls in gather mode).
 cudaError_t rhs(pbe_rk4_tape* t, int m, const double* Yin, cudaStream_t s)
 {
     cudaError_t e = cudaMemsetAsync(t->k, 0, sizeof(double) * t->n, s);
     if (e == cudaSuccess && t->kernel >= 0) {
         const pbe_agg_params_t& p = t->agg[m];
         AggArgs a{Yin, t->x, t->k, t->n, t->kernel, p.beta0, p.beta_br, p.beta_sh};
-        e = agg_launch(a, false, t->agg_ws, t->num_sms, s);
+        e = agg_stage_launch(a, false, t->agg_ws[m], t->num_sms, s);
     }
     if (e == cudaSuccess && t->selection >= 0) {
         const pbe_brk_params_t& p = t->brk[m];
         BrkArgs b{Yin, t->x, t->t_q, t->bw_q, t->k, t->n, t->nq, t->selection, p.S0, p.v_ref,
                   p.alpha, p.v_min};
-        e = brk_launch(b, false, t->brk_ws, s);
+        e = brk_stage_launch(b, t->brk_ws[m], s);
     }
     return e;
 }
@@ -139,10 +187,10 @@ cudaError_t vjp(pbe_rk4_tape* t, int m, const double* Yq, double* g_agg, double*
     return e;
 }
 
-cudaError_t forward(pbe_rk4_tape* t, double* N, cudaStream_t s)
+cudaError_t enqueue_forward(pbe_rk4_tape* t, double* N, cudaStream_t s)
 {
     const size_t un = static_cast<size_t>(t->n);
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = tables(t, N, s);
     for (int st = 0; st < t->n_steps && e == cudaSuccess; ++st) {
         if (st % t->every == 0)
             e = cudaMemcpyAsync(t->ckpt + (st / t->every) * un, N, sizeof(double) * un,
@@ -152,15 +200,17 @@ cudaError_t forward(pbe_rk4_tape* t, double* N, cudaStream_t s)
     return e;
 }
 
-cudaError_t backward(pbe_rk4_tape* t, const double* lamT, double* gN0, double* g_agg,
-                     double* g_brk, cudaStream_t s)
+cudaError_t enqueue_backward(pbe_rk4_tape* t, const double* lamT, double* gN0, double* g_agg,
+                             double* g_brk, cudaStream_t s)
 {
     const size_t un = static_cast<size_t>(t->n);
     const double h = 0.5 * t->dt, c6 = t->dt / 6.0;
     const double cs[3] = {h, h, t->dt};
     double* lam = t->lam;
     double* lsum = t->lsum;
-    cudaError_t e = cudaMemcpyAsync(lam, lamT, sizeof(double) * un, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e = tables(t, t->ckpt, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(lam, lamT, sizeof(double) * un, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess && t->kernel >= 0)
         e = cudaMemsetAsync(g_agg, 0, sizeof(double) * 3 * t->n_sets, s);
     if (e == cudaSuccess && t->selection >= 0)
@@ -195,6 +245,73 @@ cudaError_t backward(pbe_rk4_tape* t, const double* lamT, double* gN0, double* g
     return e;
 }
 
+// Captures `enqueue` on the tape's capture stream into *exec (replacing an
+// older graph), instantiates it and moves it to the device.
+template <class Fn>
+cudaError_t capture(pbe_rk4_tape* t, cudaGraphExec_t* exec, Fn&& enqueue)
+{
+    if (*exec) { cudaGraphExecDestroy(*exec); *exec = nullptr; }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(t->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t le = enqueue(t->cap);
+    e = cudaStreamEndCapture(t->cap, &graph);
+    if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return le; }
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { *exec = nullptr; return e; }
+    e = cudaGraphUpload(*exec, t->cap);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(t->cap);
+    return e;
+}
+
+bool same_key(const double* const* key, const pbe_rk4_tape* t)
+{
+    return key[0] == t->x && key[1] == t->t_q && key[2] == t->bw_q;
+}
+
+cudaError_t forward(pbe_rk4_tape* t, double* N, cudaStream_t s)
+{
+    if (!t->use_graphs) return enqueue_forward(t, N, s);
+    const size_t bytes = sizeof(double) * static_cast<size_t>(t->n);
+    cudaError_t e = cudaSuccess;
+    if (!t->fwd_exec || !same_key(t->fwd_key, t)) {
+        e = capture(t, &t->fwd_exec, [&](cudaStream_t c) { return enqueue_forward(t, t->Nio, c); });
+        if (e != cudaSuccess) return e;
+        t->fwd_key[0] = t->x; t->fwd_key[1] = t->t_q; t->fwd_key[2] = t->bw_q;
+    }
+    e = cudaMemcpyAsync(t->Nio, N, bytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(t->fwd_exec, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(N, t->Nio, bytes, cudaMemcpyDeviceToDevice, s);
+    return e;
+}
+
+cudaError_t backward(pbe_rk4_tape* t, const double* lamT, double* gN0, double* g_agg,
+                     double* g_brk, cudaStream_t s)
+{
+    if (!t->use_graphs) return enqueue_backward(t, lamT, gN0, g_agg, g_brk, s);
+    const size_t bytes = sizeof(double) * static_cast<size_t>(t->n);
+    double* ga = t->g_int;
+    double* gb = t->g_int + 3 * t->n_sets;
+    cudaError_t e = cudaSuccess;
+    if (!t->bwd_exec || !same_key(t->bwd_key, t)) {
+        e = capture(t, &t->bwd_exec, [&](cudaStream_t c) {
+            return enqueue_backward(t, t->lam_in, t->gN_out, ga, gb, c);
+        });
+        if (e != cudaSuccess) return e;
+        t->bwd_key[0] = t->x; t->bwd_key[1] = t->t_q; t->bwd_key[2] = t->bw_q;
+    }
+    e = cudaMemcpyAsync(t->lam_in, lamT, bytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(t->bwd_exec, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(gN0, t->gN_out, bytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && t->kernel >= 0)
+        e = cudaMemcpyAsync(g_agg, ga, sizeof(double) * 3 * t->n_sets, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && t->selection >= 0)
+        e = cudaMemcpyAsync(g_brk, gb, sizeof(double) * 4 * t->n_sets, cudaMemcpyDeviceToDevice, s);
+    return e;
+}
+
 template <class T>
 cudaError_t tape_alloc(pbe_rk4_tape* t, T** out, size_t bytes)
 {
@@ -208,6 +325,9 @@ cudaError_t tape_alloc(pbe_rk4_tape* t, T** out, size_t bytes)
 
 void destroy(pbe_rk4_tape* t)
 {
+    if (t->fwd_exec) cudaGraphExecDestroy(t->fwd_exec);
+    if (t->bwd_exec) cudaGraphExecDestroy(t->bwd_exec);
+    if (t->cap) cudaStreamDestroy(t->cap);
     for (void* q : t->allocs) cudaFree(q);
     delete t;
 }
@@ -266,12 +386,23 @@ int pbe_rk4_tape_create(pbe_rk4_tape_t* tape, int n_steps, double dt, int checkp
     const int seg = std::min(checkpoint_every, std::max(n_steps, 1));
     if (e == cudaSuccess) e = tape_alloc(t, &t->ckpt, dn * nck);
     if (e == cudaSuccess) e = tape_alloc(t, &t->segY, dn * 4 * seg);
-    for (double** p : {&t->k, &t->acc, &t->Y, &t->Ncur, &t->lam, &t->lsum, &t->a, &t->mu})
+    for (double** p : {&t->k, &t->acc, &t->Y, &t->Ncur, &t->lam, &t->lsum, &t->a, &t->mu,
+                       &t->Nio, &t->lam_in, &t->gN_out})
         if (e == cudaSuccess) e = tape_alloc(t, p, dn);
-    if (e == cudaSuccess && t->kernel >= 0)
-        e = tape_alloc(t, &t->agg_ws, agg_ws_layout(n, nullptr, nullptr));
-    if (e == cudaSuccess && t->selection >= 0)
-        e = tape_alloc(t, &t->brk_ws, brk_ws_layout(n, t->nq, nullptr, nullptr));
+    if (e == cudaSuccess) e = tape_alloc(t, &t->g_int, sizeof(double) * 7 * n_sets);
+    if (const char* g = std::getenv("PBE_GB300_TAPE_GRAPH")) t->use_graphs = std::strcmp(g, "0") != 0;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&t->cap, cudaStreamNonBlocking);
+    for (int m = 0; m < n_sets && e == cudaSuccess; ++m) {
+        void* w = nullptr;
+        if (t->kernel >= 0) {
+            e = tape_alloc(t, &w, agg_ws_layout(n, nullptr, nullptr));
+            t->agg_ws.push_back(w);
+        }
+        if (e == cudaSuccess && t->selection >= 0) {
+            e = tape_alloc(t, &w, brk_ws_layout(n, t->nq, nullptr, nullptr));
+            t->brk_ws.push_back(w);
+        }
+    }
     if (e == cudaSuccess) e = tape_alloc(t, &t->vjp_ws, vjp_ws_layout(n, nullptr, nullptr));
     if (e != cudaSuccess) { destroy(t); return e; }
     *tape = t;

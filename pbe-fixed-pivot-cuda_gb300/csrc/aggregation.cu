@@ -59,8 +59,17 @@ constexpr int W = kTileW;
 //     Brownian: Bd = c_d beta_br (rho + 1/rho + 2)
 //     Shear:    Sd = c_d beta_sh (1 + rho)^3
 //   Ld[d]: bracket of x_0 + x_d (kLagClipAll when it reaches x[n-1]).
+//
+// FULL = false (stage calls of a caller that keeps the workspace, e.g. the RK4
+// tape): every grid-only entry -- a, ia, inv_dx, the x copy, Bd, Sd, Ld, the
+// geometric flag mom[5..6] and D0 in counter[1] -- is left as an earlier FULL
+// call on the same pivots and coefficients wrote it; only the N-dependent
+// values (h, the N copy, moments) and the tickets are rewritten, with the
+// same arithmetic as a FULL call, so the results are bitwise the same.
+// Either way the last block resets counter[2] (the prep's block tickets), so
+// a following call on the same workspace needs no memset.
 // ---------------------------------------------------------------------------
-template <int K>
+template <int K, bool FULL>
 __global__ void __launch_bounds__(kPrepThreads)
 agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int n, AggWs ws,
                 double b0, double bbr, double bsh)
@@ -73,7 +82,7 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     double dev = 0.0;
     int d0 = n;      // this thread's lag if its pairs land on their larger member (Ld == d)
-    if (threadIdx.x == 0) {
+    if (FULL && threadIdx.x == 0) {
         d0_s = n;
         ax0_s = cbrt(x[0]);
         fit_s = geo_fit(x[0], x[n - 1], n);
@@ -82,53 +91,64 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     if (i < n) {
         const double xi = x[i], Ni = N[i];
         const double hi = xi * Ni;
-        const double ai = cbrt(xi);
-        const double iai = 1.0 / ai;
+        double ai, iai;
+        if constexpr (FULL) {
+            ai = cbrt(xi);
+            iai = 1.0 / ai;
+        } else {
+            ai = ws.a[i];
+            iai = ws.ia[i];
+        }
         ws.h[i] = hi;
         ws.Ncp[i] = Ni;          // 256-byte aligned copies: bulk-copy sources of the lane tasks
-        ws.xcp[i] = xi;
-        ws.a[i] = ai;
-        ws.ia[i] = iai;
-        ws.inv_dx[i] = (i < n - 1) ? 1.0 / (x[i + 1] - xi) : 0.0;
         m[0] = iai * Ni; m[1] = Ni; m[2] = ai * Ni; m[3] = (ai * ai) * Ni; m[4] = hi;
-
-        const double x0 = x[0];
-        const double c = (i == 0) ? 0.5 : 1.0;
-        double B = 0.0, S = 0.0;
-        if constexpr (K <= 2) B = c * b0;
-        if constexpr (K >= 3) {
-            const double rho = ai / ax0_s;
-            if constexpr (K == 3 || K == 5) B = c * bbr * (rho + 1.0 / rho + 2.0);
-            if constexpr (K == 4 || K == 5) { const double s = 1.0 + rho; S = c * bsh * (s * s) * s; }
-        }
-        ws.Bd[i] = B;
-        ws.Sd[i] = S;
-        const double v = x0 + xi;       // x[i] <= v: its bracket is at or above i
-        const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
-        ws.Ld[i] = L;
-        if (L == i) d0 = i;
         if (i < agg_tiles(n)) { ws.tticket[i] = 0; ws.cticket[i] = 0; }
-        if (n >= 2) {
-            dev = geo_dev(fit_s, xi, i);
-            if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
+        if constexpr (FULL) {
+            ws.xcp[i] = xi;
+            ws.a[i] = ai;
+            ws.ia[i] = iai;
+            ws.inv_dx[i] = (i < n - 1) ? 1.0 / (x[i + 1] - xi) : 0.0;
+            const double x0 = x[0];
+            const double c = (i == 0) ? 0.5 : 1.0;
+            double B = 0.0, S = 0.0;
+            if constexpr (K <= 2) B = c * b0;
+            if constexpr (K >= 3) {
+                const double rho = ai / ax0_s;
+                if constexpr (K == 3 || K == 5) B = c * bbr * (rho + 1.0 / rho + 2.0);
+                if constexpr (K == 4 || K == 5) { const double s = 1.0 + rho; S = c * bsh * (s * s) * s; }
+            }
+            ws.Bd[i] = B;
+            ws.Sd[i] = S;
+            const double v = x0 + xi;       // x[i] <= v: its bracket is at or above i
+            const int L = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
+            ws.Ld[i] = L;
+            if (L == i) d0 = i;
+            if (n >= 2) {
+                dev = geo_dev(fit_s, xi, i);
+                if (!(dev == dev)) dev = 1.0;   // NaN -> not geometric
+            }
         }
     }
-    atomicMin(&d0_s, d0);
+    if (FULL) atomicMin(&d0_s, d0);
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         const double s = block_sum(m[q], sh);
         if (threadIdx.x == 0) ws.mom_part[blockIdx.x * 8 + q] = s;
     }
-    dev = warp_max(dev);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
-    __syncthreads();
+    if (FULL) {
+        dev = warp_max(dev);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
+        __syncthreads();
+    }
     __shared__ int last_s;
     if (threadIdx.x == 0) {
-        double mx = 0.0;
-        for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
-        ws.mom_part[blockIdx.x * 8 + 5] = mx;
-        ws.mom_part[blockIdx.x * 8 + 6] = static_cast<double>(d0_s);
+        if (FULL) {
+            double mx = 0.0;
+            for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
+            ws.mom_part[blockIdx.x * 8 + 5] = mx;
+            ws.mom_part[blockIdx.x * 8 + 6] = static_cast<double>(d0_s);
+        }
         __threadfence();                       // partials visible before the ticket
         last_s = (atomicAdd(ws.counter + 2, 1) == static_cast<int>(gridDim.x) - 1);
     }
@@ -143,7 +163,7 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     // one moment each, r = 5 the largest deviation, r = 6 the smallest D0
     // candidate (lanes stride over the blocks, fixed butterflies)
     const int wq = threadIdx.x >> 5, lq = threadIdx.x & 31;
-    for (int r = wq; r < 7; r += kPrepThreads / 32) {
+    for (int r = wq; r < (FULL ? 7 : 5); r += kPrepThreads / 32) {
         if (r < 5) {
             double t = 0.0;
             for (int b = lq; b < nb; b += 32) t += __ldcg(ws.mom_part + b * 8 + r);
@@ -165,16 +185,19 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const double mx = sh[0];
-        // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
-        // its bracket pivot (precondition of sum_minus_scaled)
-        const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
-        ws.mom[5] = geo ? 1.0 : 0.0;
-        ws.mom[6] = mx;
+        if (FULL) {
+            const double mx = sh[0];
+            // neighbour ratio <= 64 keeps fl(x_j + x_k) within kMaxExpGap binades of
+            // its bracket pivot (precondition of sum_minus_scaled)
+            const bool geo = n >= 2 && mx <= kGeoTol && x[1] <= 64.0 * x[0];
+            ws.mom[5] = geo ? 1.0 : 0.0;
+            ws.mom[6] = mx;
+            ws.counter[1] = d0_s;   // lags d >= counter[1] have lo(j, j+d) = j + d
+        }
         ws.counter[0] = 0;          // task counter of the main kernel
-        ws.counter[4] = 0;          // lane-task staging error flag
-        ws.counter[1] = d0_s;       // lags d >= counter[1] have lo(j, j+d) = j + d
+        ws.counter[2] = 0;          // this kernel's block tickets, ready for the next call
         ws.counter[3] = 0;          // contributors to bin n-1 done (clip tasks + top tile)
+        ws.counter[4] = 0;          // lane-task staging error flag
     }
 }
 
@@ -535,8 +558,13 @@ int agg_clip_tasks(int n)
     return c < 1 ? 1 : (c > kMaxClipTasks ? kMaxClipTasks : c);
 }
 
+// kind: kAggFull = tables + pair kernels (the drop-in calls), kAggTables =
+// the FULL prep only, kAggStage = the light prep + pair kernels on a
+// workspace whose tables an earlier kAggTables / kAggFull call wrote.
+enum { kAggFull = 0, kAggTables = 1, kAggStage = 2 };
+
 template <int K, bool SC>
-cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_t s)
+cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_t s, int kind)
 {
     const int n = a.n;
     const int nb = agg_prep_blocks(n);
@@ -598,9 +626,17 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
             e = cudaFuncSetAttribute(lkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess) return e;
     }
-    e = cudaMemsetAsync(ws.counter, 0, 8 * sizeof(int), s);   // prep's block tickets
-    if (e != cudaSuccess) return e;
-    agg_prep_kernel<K><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br, a.beta_sh);
+    if (kind == kAggStage) {
+        // counter[2] was left at 0 by the previous prep on this workspace
+        agg_prep_kernel<K, false><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br,
+                                                              a.beta_sh);
+    } else {
+        e = cudaMemsetAsync(ws.counter, 0, 8 * sizeof(int), s);   // prep's block tickets
+        if (e != cudaSuccess) return e;
+        agg_prep_kernel<K, true><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, n, ws, a.beta0, a.beta_br,
+                                                             a.beta_sh);
+        if (kind == kAggTables) return cudaGetLastError();
+    }
     const bool prof = g_prof_start && g_prof_stop;
     if (prof) cudaEventRecord(g_prof_start, s);
     if (lane_mode && lgrid > 0)
@@ -614,15 +650,15 @@ cudaError_t launch_k(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_
 }
 
 template <bool SC>
-cudaError_t dispatch(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_t s)
+cudaError_t dispatch(const AggArgs& a, const AggWs& ws, int num_sms, cudaStream_t s, int kind)
 {
     switch (a.kernel) {
-    case 0: return launch_k<0, SC>(a, ws, num_sms, s);
-    case 1: return launch_k<1, SC>(a, ws, num_sms, s);
-    case 2: return launch_k<2, SC>(a, ws, num_sms, s);
-    case 3: return launch_k<3, SC>(a, ws, num_sms, s);
-    case 4: return launch_k<4, SC>(a, ws, num_sms, s);
-    case 5: return launch_k<5, SC>(a, ws, num_sms, s);
+    case 0: return launch_k<0, SC>(a, ws, num_sms, s, kind);
+    case 1: return launch_k<1, SC>(a, ws, num_sms, s, kind);
+    case 2: return launch_k<2, SC>(a, ws, num_sms, s, kind);
+    case 3: return launch_k<3, SC>(a, ws, num_sms, s, kind);
+    case 4: return launch_k<4, SC>(a, ws, num_sms, s, kind);
+    case 5: return launch_k<5, SC>(a, ws, num_sms, s, kind);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -636,7 +672,24 @@ cudaError_t agg_launch(const AggArgs& a, bool scatter, void* ws_base, int num_sm
 {
     AggWs ws;
     agg_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
-    return scatter ? dispatch<true>(a, ws, num_sms, s) : dispatch<false>(a, ws, num_sms, s);
+    return scatter ? dispatch<true>(a, ws, num_sms, s, kAggFull)
+                   : dispatch<false>(a, ws, num_sms, s, kAggFull);
+}
+
+cudaError_t agg_tables_launch(const AggArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+{
+    AggWs ws;
+    agg_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
+    return dispatch<false>(a, ws, num_sms, s, kAggTables);
+}
+
+cudaError_t agg_stage_launch(const AggArgs& a, bool scatter, void* ws_base, int num_sms,
+                             cudaStream_t s)
+{
+    AggWs ws;
+    agg_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
+    return scatter ? dispatch<true>(a, ws, num_sms, s, kAggStage)
+                   : dispatch<false>(a, ws, num_sms, s, kAggStage);
 }
 
 } // namespace pbe_gb300

@@ -35,7 +35,13 @@ __device__ __forceinline__ void frag_shares(const double* __restrict__ x, int n,
     chi = q * (v - xl);
 }
 
-template <int F>
+// prep modes: kBrkFull computes everything per call; kBrkTables only the
+// grid-only tables (fragment brackets lo, run starts, S per bin) into the
+// workspace; kBrkStage the N-dependent shares from those tables, with the
+// arithmetic of kBrkFull (bitwise the same shares and sums).
+enum { kBrkFull = 0, kBrkTables = 1, kBrkStage = 2 };
+
+template <int F, int MODE>
 __global__ void __launch_bounds__(256)
 brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const double* __restrict__ t_q, const double* __restrict__ bw_q, int n, int nq,
@@ -51,37 +57,54 @@ brk_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (live) {
         q = static_cast<int>(idx / n);
         j = static_cast<int>(idx - static_cast<long long>(q) * n);
-        const double xj = x[j], Nj = N[j];
-        const double S = selection<F>(xj, S0, v_ref, alpha, v_min);
-        const bool active = (S != 0.0) && (Nj > kBreakageNMin);
+        const double xj = x[j];
         tq = t_q[q];
-        const double contrib = active ? S * Nj * bw_q[q] : 0.0;
         const double v = xj * tq;
-        lo = frag_bracket(x, n, v);
-        double clo, chi;
-        frag_shares(x, n, lo, v, contrib, clo, chi);
-        ws.clo[idx] = clo;
-        ws.chi[idx] = chi;
-        if (lo < 0) clipped = clo;               // all of it goes to bin 0
-        if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
+        double S;
+        if constexpr (MODE == kBrkStage) {
+            S = ws.Ssel[j];
+            lo = ws.lo[idx];
+        } else {
+            S = selection<F>(xj, S0, v_ref, alpha, v_min);
+            lo = frag_bracket(x, n, v);
+        }
+        if constexpr (MODE == kBrkTables) {
+            ws.lo[idx] = lo;
+            if (q == 0) ws.Ssel[j] = S;
+        } else {
+            const double Nj = N[j];
+            const bool active = (S != 0.0) && (Nj > kBreakageNMin);
+            const double contrib = active ? S * Nj * bw_q[q] : 0.0;
+            double clo, chi;
+            frag_shares(x, n, lo, v, contrib, clo, chi);
+            ws.clo[idx] = clo;
+            ws.chi[idx] = chi;
+            if (lo < 0) clipped = clo;           // all of it goes to bin 0
+            if (q == 0) ws.SN[j] = active ? S * Nj : 0.0;
+        }
     }
-    // bracket of the previous parent's fragment (same q): the lane below has it
-    const int lo_left = __shfl_up_sync(0xffffffffu, lo, 1);
-    if (live) {
-        // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
-        int* fq = ws.first + static_cast<long long>(q) * (n + 2);
-        const int lo_prev = (j == 0) ? -2 : (lane > 0 ? lo_left : frag_bracket_below(x, n, x[j - 1] * tq, lo));
-        for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
-        if (j == n - 1)
-            for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
+    if constexpr (MODE != kBrkStage) {
+        // bracket of the previous parent's fragment (same q): the lane below has it
+        const int lo_left = __shfl_up_sync(0xffffffffu, lo, 1);
+        if (live) {
+            // run starts: first[q][m+1] = j for every bracket m in (lo(j-1), lo(j)]
+            int* fq = ws.first + static_cast<long long>(q) * (n + 2);
+            const int lo_prev = (j == 0) ? -2
+                              : (lane > 0 ? lo_left : frag_bracket_below(x, n, x[j - 1] * tq, lo));
+            for (int m = max(lo_prev + 1, -1); m <= lo; ++m) fq[m + 1] = j;
+            if (j == n - 1)
+                for (int m = max(lo + 1, -1); m <= n; ++m) fq[m + 1] = n;
+        }
     }
-    // this block's fragments clipped below x[0], summed in a fixed order (most
-    // blocks have none: one barrier tells)
-    if (__syncthreads_or(clipped != 0.0)) {
-        const double cs = block_sum(clipped, sh);
-        if (threadIdx.x == 0) ws.clipsum[blockIdx.x] = cs;
-    } else if (threadIdx.x == 0) {
-        ws.clipsum[blockIdx.x] = 0.0;
+    if constexpr (MODE != kBrkTables) {
+        // this block's fragments clipped below x[0], summed in a fixed order (most
+        // blocks have none: one barrier tells)
+        if (__syncthreads_or(clipped != 0.0)) {
+            const double cs = block_sum(clipped, sh);
+            if (threadIdx.x == 0) ws.clipsum[blockIdx.x] = cs;
+        } else if (threadIdx.x == 0) {
+            ws.clipsum[blockIdx.x] = 0.0;
+        }
     }
 }
 
@@ -159,7 +182,7 @@ brk_scatter_kernel(const double* __restrict__ N, const double* __restrict__ x,
 }
 
 template <int F>
-cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s)
+cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s, int kind)
 {
     const long long m = static_cast<long long>(a.n) * a.n_quad;
     const int grid = static_cast<int>((m + 255) / 256);
@@ -169,8 +192,20 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
     } else {
         BrkWs ws;
         brk_ws_layout(a.n, a.n_quad, static_cast<char*>(ws_base), &ws);
-        brk_prep_kernel<F><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n, a.n_quad, ws, a.S0,
-                                                a.v_ref, a.alpha, a.v_min);
+        if (kind == kBrkTables) {
+            brk_prep_kernel<F, kBrkTables><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n,
+                                                                a.n_quad, ws, a.S0, a.v_ref,
+                                                                a.alpha, a.v_min);
+            return cudaGetLastError();
+        }
+        if (kind == kBrkStage)
+            brk_prep_kernel<F, kBrkStage><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n,
+                                                               a.n_quad, ws, a.S0, a.v_ref,
+                                                               a.alpha, a.v_min);
+        else
+            brk_prep_kernel<F, kBrkFull><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n,
+                                                              a.n_quad, ws, a.S0, a.v_ref,
+                                                              a.alpha, a.v_min);
         int nqp = 1;
         while (nqp < a.n_quad && nqp < 32) nqp <<= 1;
         const int per_block = 8 * (32 / nqp);               // bins per 256-thread block
@@ -181,15 +216,32 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
 
 } // namespace
 
-cudaError_t brk_launch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s)
+namespace {
+cudaError_t brk_dispatch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s, int kind)
 {
     switch (a.selection) {
-    case 0: return launch_f<0>(a, scatter, ws_base, s);
-    case 1: return launch_f<1>(a, scatter, ws_base, s);
-    case 2: return launch_f<2>(a, scatter, ws_base, s);
-    case 3: return launch_f<3>(a, scatter, ws_base, s);
+    case 0: return launch_f<0>(a, scatter, ws_base, s, kind);
+    case 1: return launch_f<1>(a, scatter, ws_base, s, kind);
+    case 2: return launch_f<2>(a, scatter, ws_base, s, kind);
+    case 3: return launch_f<3>(a, scatter, ws_base, s, kind);
     default: return cudaErrorInvalidValue;
     }
+}
+} // namespace
+
+cudaError_t brk_launch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s)
+{
+    return brk_dispatch(a, scatter, ws_base, s, kBrkFull);
+}
+
+cudaError_t brk_tables_launch(const BrkArgs& a, void* ws_base, cudaStream_t s)
+{
+    return brk_dispatch(a, false, ws_base, s, kBrkTables);
+}
+
+cudaError_t brk_stage_launch(const BrkArgs& a, void* ws_base, cudaStream_t s)
+{
+    return brk_dispatch(a, false, ws_base, s, kBrkStage);
 }
 
 } // namespace pbe_gb300

@@ -353,6 +353,8 @@ struct BrkWs {
     int*    first; // [nq * (n + 2)]  first[q][m+1] = first j with lo(q, j) >= m, m in [-1, n]
     double* SN;    // [n]  S(x_j) N_j (0 where the guard skips bin j)
     double* clipsum; // [nq * n / 256] per prep block: shares clipped below x[0]
+    int*    lo;    // [nq * n]  bracket of fragment (q, j) (kept by brk_tables_launch)
+    double* Ssel;  // [n]  S(x_j) (kept by brk_tables_launch)
 };
 
 inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
@@ -366,6 +368,8 @@ inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
     w.first = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(nq) * (static_cast<size_t>(n) + 2)));
     w.SN    = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(n)));
     w.clipsum = reinterpret_cast<double*>(take(sizeof(double) * ((m + 255) / 256)));
+    w.lo    = reinterpret_cast<int*>(take(sizeof(int) * m));
+    w.Ssel  = reinterpret_cast<double*>(take(sizeof(double) * static_cast<size_t>(n)));
     if (ws) *ws = w;
     return off;
 }
@@ -451,7 +455,22 @@ bool mode_is_scatter(int mode);
 // Launch the aggregation kernels with a scratch buffer `ws_base` of at least
 // agg_ws_layout(n) bytes. scatter selects the atomic-flush variant.
 cudaError_t agg_launch(const AggArgs& a, bool scatter, void* ws_base, int num_sms, cudaStream_t s);
+// For callers that keep a workspace per (pivots, coefficients) -- the RK4
+// tape: agg_tables_launch writes the grid-only tables (cube roots, 1/dx, lag
+// tables, geometric flag, D0) into it; agg_stage_launch then evaluates the
+// RHS for any N on that workspace, recomputing only what depends on N, and
+// gives bitwise the result of agg_launch.
+cudaError_t agg_tables_launch(const AggArgs& a, void* ws_base, int num_sms, cudaStream_t s);
+cudaError_t agg_stage_launch(const AggArgs& a, bool scatter, void* ws_base, int num_sms,
+                             cudaStream_t s);
 // Breakage: scatter needs no scratch (ws_base may be null).
 cudaError_t brk_launch(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t s);
+// Gather mode on a kept workspace (the RK4 tape): brk_tables_launch writes the
+// grid-only tables (fragment brackets and run starts, the selection function
+// per bin) for the pivots, quadrature table and selection parameters;
+// brk_stage_launch then evaluates the RHS for any N on that workspace with
+// bitwise the result of brk_launch in gather mode.
+cudaError_t brk_tables_launch(const BrkArgs& a, void* ws_base, cudaStream_t s);
+cudaError_t brk_stage_launch(const BrkArgs& a, void* ws_base, cudaStream_t s);
 
 } // namespace pbe_gb300

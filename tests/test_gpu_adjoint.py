@@ -75,6 +75,51 @@ def test_tape_matches_oracle_adjoint():
     np.testing.assert_allclose(gb[:, 1], rgb[:, 1], rtol=1e-9, atol=1e-9 * np.abs(rgb[:, 1]).max())
 
 
+def test_tape_forward_bitwise_equals_drop_in_calls():
+    """The tape keeps the grid-only tables per parameter set and recomputes
+    only the N-dependent part of each RHS: its RK4 steps must equal, bit for
+    bit, RK4 driven from the host through the drop-in calls (gather mode) with
+    the reference examples' stage arithmetic (each product and sum rounded on
+    its own), including the switch of parameter set mid-run."""
+    torch = _torch()
+    for n, q in ((3840, 128.0), (500, 16.0)):
+        x = pg.grids.geometric_pow2(n, 1e-21, q)
+        N0 = pg.grids.lognormal_ic(x, n // 6, 1.0, 1e12, cut=5.0)
+        t_q, bw_q = pg.quadrature.power_law(2.0, 4)
+        agg = [pg.AggregationParams(n=n, kernel_type=5, beta0=0.0, beta_br=6.73e-18,
+                                    beta_sh=4 * G / 3) for G in (100.0, 20.0)]
+        brk = [pg.BreakageParams(n=n, n_quad=len(t_q), selection=2, S0=5e-4 * f, v_ref=1e-18,
+                                 alpha=1.0 + 0.2 * f) for f in (1.0, 2.0)]
+        step_set = np.array([0, 0, 1, 1], dtype=np.int32)
+        dt = 0.5
+        dx, dtq, dbw = t(x), t(t_q), t(bw_q)
+        with pg.Rk4Tape(len(step_set), dt, 2, agg, brk, step_set) as tape:
+            Nt = t(N0)
+            assert tape.forward(Nt, dx, dtq, dbw) == 0
+            torch.cuda.synchronize()
+        N = t(N0)
+
+        def f(Y, m):
+            k = torch.zeros(n, dtype=torch.float64, device="cuda")
+            assert pg.aggregation_rhs(Y, dx, k, agg[m], mode=pg.MODE_GATHER) == 0
+            assert pg.breakage_rhs(Y, dx, dtq, dbw, k, brk[m], mode=pg.MODE_GATHER) == 0
+            return k
+        h, dt6 = 0.5 * dt, dt / 6.0
+        for m in step_set:
+            k1 = f(N, m)
+            k2 = f(N + h * k1, m)
+            k3 = f(N + h * k2, m)
+            k4 = f(N + dt * k3, m)
+            acc = k1 + 2.0 * k2
+            acc = acc + 2.0 * k3
+            N = N + dt6 * (acc + k4)
+        torch.cuda.synchronize()
+        a, b = Nt.cpu().numpy(), N.cpu().numpy()
+        assert np.array_equal(a.view(np.int64), b.view(np.int64)), \
+            "n=%d: %d bins differ, max rel %.3e" % (n, int((a != b).sum()),
+                                                    float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))))
+
+
 def test_checkpoint_interval_does_not_change_the_result():
     x, N0, t_q, bw_q, agg, brk, step_set = small_case(n=120, steps=9, switch=4)
     lam = np.random.default_rng(3).normal(size=len(x))
