@@ -18,6 +18,9 @@
 // the fragments clipped below x[0]), then the death term -S_i N_i.
 // SCATTER: one thread per fragment adds its shares with FP64 atomicAdd.
 // =============================================================================
+#include <cstdlib>
+#include <cstring>
+
 #include "pbe_internal.cuh"
 
 namespace pbe_gb300 {
@@ -157,6 +160,233 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Gather in one pass (the drop-in calls): block = 32 consecutive output bins
+// x W warps (W = min(n_quad, 16)); warp w takes the quadrature points
+// q = w, w + W, ..., lane l the bin i = i0 + l. For (i, q) the parents whose
+// fragment x_j t_q has bracket i - 1 or i form the index ranges [fa, fb) and
+// [fb, fc), fb = first_parent(i) (brackets grow with j for t_q > 0); the
+// thread walks them and forms each fragment's share from 1/dx staged in
+// shared memory. Bin 0 also takes the fragments clipped below x[0], summed
+// by each warp's lanes. Sums run in a fixed order (fragments by j, points by
+// q within a warp, warps in order): bitwise reproducible.
+// ---------------------------------------------------------------------------
+constexpr int kBinWarpsMax = 8;
+
+// S_j N_j with the reference's guard (S != 0, N_j > 2.2e-308), from the
+// cache `SN` when the selection needs it (Linear, PowerLaw), else inline.
+template <int F>
+__device__ __forceinline__ double bin_sn(const double* __restrict__ N, const double* __restrict__ x,
+                                        const double* __restrict__ SN, int j, double S0,
+                                        double v_min)
+{
+    if constexpr (F == 1 || F == 2) {
+        return SN[j];
+    } else {
+        // comparisons on bit patterns (the integer pipe): x_j > 0, so
+        // x_j > v_min <=> bits(x_j) > bits(v_min) for any v_min, and
+        // N_j > 2.2e-308 <=> bits(N_j) > bits(2.2e-308) for any N_j
+        const double S = (F == 0) ? S0 : ((dbits(__ldg(x + j)) > dbits(v_min)) ? S0 : 0.0);
+        const double Nj = __ldg(N + j);
+        return (S != 0.0 && dbits(Nj) > dbits(kBreakageNMin)) ? S * Nj : 0.0;
+    }
+}
+
+// The parent's factor of its fragments' shares: N_j (guarded: 0 where the
+// reference skips the parent) for Constant / Threshold, whose S0 goes into
+// the per-lane factor; S_j N_j from the cache otherwise.
+template <int F>
+__device__ __forceinline__ double bin_unit(const double* __restrict__ N, const double* __restrict__ x,
+                                          const double* __restrict__ SN, int j, double v_min)
+{
+    if constexpr (F == 1 || F == 2) {
+        return SN[j];
+    } else {
+        const bool on = (F == 0) || dbits(__ldg(x + j)) > dbits(v_min);
+        const double Nj = __ldg(N + j);
+        return (on && dbits(Nj) > dbits(kBreakageNMin)) ? Nj : 0.0;
+    }
+}
+
+// First parent j in [0, n] whose fragment x_j t_q has bracket >= ib
+// (ib = 0: x_j t_q > x[0]; 1 <= ib <= n - 1: x_j t_q >= x[ib]; ib >= n: n),
+// given a lower bound lb <= the answer and a guess: the exact test
+// fl(x_j t_q) on the guess, a gallop away from it until the answer is
+// bracketed, then bisection. One or two tests when the guess is right (on a
+// geometric grid the first parents of consecutive bins are consecutive).
+__device__ __forceinline__ int first_parent_near(const double* __restrict__ x, int n, int ib,
+                                                 double tq, int lb, int guess)
+{
+    if (ib >= n) return n;
+    const long long xb = dbits(__ldg(x + ib));
+    auto P = [&](int j) {                     // bracket of fragment j >= ib; P(n) := true
+        if (j >= n) return true;
+        const long long vb = dbits(__ldg(x + j) * tq);
+        return ib == 0 ? (vb > xb && vb > 0) : vb >= xb;
+    };
+    int g = guess < lb ? lb : (guess > n ? n : guess);
+    int a, b;                                 // answer in (a, b]: P(b), a < lb or !P(a)
+    if (P(g)) {
+        b = g;
+        int step = 1;
+        a = g - 1;
+        while (a >= lb && P(a)) {
+            b = a;
+            step <<= 1;
+            a = b - step;
+        }
+        if (a < lb - 1) a = lb - 1;
+    } else {
+        a = g;
+        int step = 1;
+        b = g + 1 < n ? g + 1 : n;
+        while (!P(b)) {
+            a = b;
+            step <<= 1;
+            b = a + step < n ? a + step : n;
+        }
+    }
+    while (b - a > 1) {
+        const int mid = (a + b) >> 1;
+        if (P(mid)) b = mid; else a = mid;
+    }
+    return b;
+}
+
+// Starting point for a warp: the first parent of bin ib by bisection of x's
+// bit patterns against x[ib] / t_q (integer compares; every lane of the warp
+// walks the same addresses), finished exactly by first_parent_near.
+__device__ __forceinline__ int first_parent(const double* __restrict__ x, int n, int ib, double tq,
+                                            double itq)
+{
+    if (ib >= n) return n;
+    const long long yb = dbits(__ldg(x + ib) * itq);
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (dbits(__ldg(x + mid)) >= yb) hi = mid; else lo = mid + 1;
+    }
+    return first_parent_near(x, n, ib, tq, 0, lo);
+}
+
+template <int F>
+__global__ void __launch_bounds__(32 * kBinWarpsMax)
+brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
+               const double* __restrict__ t_q, const double* __restrict__ bw_q,
+               double* __restrict__ rhs, int n, int nq, const double* __restrict__ SN,
+               double S0, double v_ref, double alpha, double v_min)
+{
+    if ((F == 0 || F == 3) && S0 == 0.0) return;     // S = 0 everywhere: no breakage at all
+    extern __shared__ double s_itq[];                 // [nq] 1 / t_q
+    __shared__ double s_inv[34];                      // 1/(x[b+1] - x[b]), b = i0 - 1 .. i0 + 32
+    __shared__ double s_acc[kBinWarpsMax][32];
+    const int i0 = blockIdx.x * 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
+    for (int k = threadIdx.x; k < 34; k += blockDim.x) {
+        const int b = i0 - 1 + k;
+        s_inv[k] = (b >= 0 && b < n - 1) ? 1.0 / (__ldg(x + b + 1) - __ldg(x + b)) : 0.0;
+    }
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) s_itq[q] = 1.0 / __ldg(t_q + q);
+    __syncthreads();
+
+    const int i = i0 + lane;
+    const bool live = i < n;
+    const double xi = live ? __ldg(x + i) : 0.0;
+    const double xlo = (live && i >= 1) ? __ldg(x + i - 1) : 0.0;     // x[i-1]
+    const double xhi = (live && i <= n - 2) ? __ldg(x + i + 1) : 0.0;  // x[i+1]
+    const double inv_lo = s_inv[lane];        // 1/(x[i] - x[i-1]): bracket i-1
+    const double inv_hi = s_inv[lane + 1];    // 1/(x[i+1] - x[i]): bracket i
+    // selections with a per-bin S of S0 or 0 (Constant, Threshold): the share
+    // factor S0 bw / dx is per lane and quadrature point, the parent adds N_j
+    constexpr bool kS0 = (F == 0 || F == 3);
+    double acc = 0.0;
+    for (int q = w; q < nq; q += W) {
+        const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q), itq = s_itq[q];
+        const double fbw = kS0 ? S0 * bw : bw;
+        const double k_lo = fbw * inv_lo, k_hi = fbw * inv_hi;
+        // fb of bins i0 - 1 + lane and, for lanes 0 and 1, of i0 + 31 and i0 + 32:
+        // the warp's bin ib0 by a uniform bisection, the others near ib0's
+        // parent plus their bin offset
+        const int ib0 = max(i0 - 1, 0);
+        const int g0 = first_parent(x, n, ib0, tq, itq);
+        const int ibl = max(i0 - 1 + lane, 0);
+        const int f0 = first_parent_near(x, n, ibl, tq, g0, g0 + (ibl - ib0));
+        int f1 = 0;
+        if (lane < 2) f1 = first_parent_near(x, n, i0 + 31 + lane, tq, g0, g0 + (i0 + 31 + lane - ib0));
+        // every lane runs every shuffle (full mask), then selects
+        const int fa = (i0 - 1 + lane < 0) ? 0 : f0;            // first parent with bracket >= i-1
+        const int up1 = __shfl_down_sync(0xffffffffu, f0, 1);
+        const int up2 = __shfl_down_sync(0xffffffffu, f0, 2);
+        const int e30 = __shfl_sync(0xffffffffu, f1, 0);
+        const int e31 = __shfl_sync(0xffffffffu, f1, 1);
+        const int fb = (lane < 31) ? up1 : e30;                 // bracket >= i
+        const int fc = (lane < 30) ? up2 : (lane == 30 ? e30 : e31);   // bracket >= i+1
+        double a = 0.0;
+        if (live) {
+            if (i >= 1) {                                       // bracket i-1: the upper share
+                for (int j = fa; j < fb; ++j) {
+                    const double u = bin_unit<F>(N, x, SN, j, v_min);
+                    const double v = __ldg(x + j) * tq;
+                    a = fma(u * k_lo, v - xlo, a);
+                }
+            }
+            for (int j = fb; j < fc; ++j) {                     // bracket i: the lower share
+                const double u = bin_unit<F>(N, x, SN, j, v_min);
+                if (i <= n - 2) {
+                    const double v = __ldg(x + j) * tq;
+                    a = fma(u * k_hi, xhi - v, a);
+                } else {
+                    a = fma(u, fbw, a);                         // clipped at x[n-1]: all of it
+                }
+            }
+        }
+        if (i0 == 0) {
+            // bin 0 also takes the fragments at or below x[0], the parents
+            // [0, fb(0)): lanes stride over them, a fixed butterfly adds
+            const int fz = __shfl_sync(0xffffffffu, f0, 1);      // lane 1 computed fb(0)
+            double cz = 0.0;
+            for (int j = lane; j < fz; j += 32) cz = fma(bin_unit<F>(N, x, SN, j, v_min), fbw, cz);
+            cz = warp_sum(cz);
+            if (lane == 0) a += cz;
+        }
+        acc += a;
+    }
+    s_acc[w][lane] = acc;
+    __syncthreads();
+    if (w == 0 && live) {
+        double t = 0.0;
+        for (int k = 0; k < W; ++k) t += s_acc[k][lane];
+        double sn_i;
+        if constexpr (F == 1 || F == 2) sn_i = SN[i];
+        else sn_i = bin_sn<F>(N, x, SN, i, S0, v_min);
+        rhs[i] = (rhs[i] - sn_i) + t;
+    }
+}
+
+// S_j N_j with the reference's guard, one thread per bin (Linear and
+// PowerLaw selections: one division or pow per bin instead of per fragment).
+template <int F>
+__global__ void __launch_bounds__(256)
+brk_sn_kernel(const double* __restrict__ N, const double* __restrict__ x, int n, double* SN,
+              double S0, double v_ref, double alpha, double v_min)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double S = selection<F>(x[j], S0, v_ref, alpha, v_min);
+    const double Nj = N[j];
+    SN[j] = (S != 0.0 && Nj > kBreakageNMin) ? S * Nj : 0.0;
+}
+
+int brk_gather_path()
+{
+    // PBE_GB300_BRK_PATH=prep: the per-fragment prep + gather kernels instead
+    static const int path = []() {
+        const char* e = std::getenv("PBE_GB300_BRK_PATH");
+        return (e && std::strcmp(e, "prep") == 0) ? 1 : 0;
+    }();
+    return path;
+}
+
 template <int F>
 __global__ void __launch_bounds__(256)
 brk_scatter_kernel(const double* __restrict__ N, const double* __restrict__ x,
@@ -192,6 +422,16 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
     } else {
         BrkWs ws;
         brk_ws_layout(a.n, a.n_quad, static_cast<char*>(ws_base), &ws);
+        if (kind == kBrkFull && brk_gather_path() == 0) {
+            if (F == 1 || F == 2)
+                brk_sn_kernel<F><<<(a.n + 255) / 256, 256, 0, s>>>(a.N, a.x, a.n, ws.SN, a.S0,
+                                                                  a.v_ref, a.alpha, a.v_min);
+            const int W = a.n_quad < kBinWarpsMax ? a.n_quad : kBinWarpsMax;
+            brk_bin_kernel<F><<<(a.n + 31) / 32, 32 * W, sizeof(double) * a.n_quad, s>>>(
+                a.N, a.x, a.t_q, a.bw_q, a.rhs, a.n, a.n_quad, ws.SN, a.S0, a.v_ref, a.alpha,
+                a.v_min);
+            return cudaGetLastError();
+        }
         if (kind == kBrkTables) {
             brk_prep_kernel<F, kBrkTables><<<grid, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.n,
                                                                 a.n_quad, ws, a.S0, a.v_ref,
