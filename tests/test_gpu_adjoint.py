@@ -75,12 +75,17 @@ def test_tape_matches_oracle_adjoint():
     np.testing.assert_allclose(gb[:, 1], rgb[:, 1], rtol=1e-9, atol=1e-9 * np.abs(rgb[:, 1]).max())
 
 
-def test_tape_forward_bitwise_equals_drop_in_calls():
+@pytest.mark.parametrize("with_breakage", [False, True], ids=["agg", "agg+brk"])
+def test_tape_forward_equals_drop_in_calls(with_breakage):
     """The tape keeps the grid-only tables per parameter set and recomputes
-    only the N-dependent part of each RHS: its RK4 steps must equal, bit for
-    bit, RK4 driven from the host through the drop-in calls (gather mode) with
-    the reference examples' stage arithmetic (each product and sum rounded on
-    its own), including the switch of parameter set mid-run."""
+    only the N-dependent part of each RHS. Its RK4 steps are compared with RK4
+    driven from the host through the drop-in calls (gather mode) with the
+    reference examples' stage arithmetic (each product and sum rounded on its
+    own), across a switch of parameter set: bit for bit for aggregation (the
+    same kernels on cached tables); with breakage within 1e-14 relative per
+    bin, because the drop-in breakage call gathers in one pass with the share
+    factors regrouped while the tape gathers from its cached fragment
+    brackets (a last-bit difference)."""
     torch = _torch()
     for n, q in ((3840, 128.0), (500, 16.0)):
         x = pg.grids.geometric_pow2(n, 1e-21, q)
@@ -90,6 +95,8 @@ def test_tape_forward_bitwise_equals_drop_in_calls():
                                     beta_sh=4 * G / 3) for G in (100.0, 20.0)]
         brk = [pg.BreakageParams(n=n, n_quad=len(t_q), selection=2, S0=5e-4 * f, v_ref=1e-18,
                                  alpha=1.0 + 0.2 * f) for f in (1.0, 2.0)]
+        if not with_breakage:
+            brk = None
         step_set = np.array([0, 0, 1, 1], dtype=np.int32)
         dt = 0.5
         dx, dtq, dbw = t(x), t(t_q), t(bw_q)
@@ -102,7 +109,8 @@ def test_tape_forward_bitwise_equals_drop_in_calls():
         def f(Y, m):
             k = torch.zeros(n, dtype=torch.float64, device="cuda")
             assert pg.aggregation_rhs(Y, dx, k, agg[m], mode=pg.MODE_GATHER) == 0
-            assert pg.breakage_rhs(Y, dx, dtq, dbw, k, brk[m], mode=pg.MODE_GATHER) == 0
+            if brk is not None:
+                assert pg.breakage_rhs(Y, dx, dtq, dbw, k, brk[m], mode=pg.MODE_GATHER) == 0
             return k
         h, dt6 = 0.5 * dt, dt / 6.0
         for m in step_set:
@@ -115,9 +123,13 @@ def test_tape_forward_bitwise_equals_drop_in_calls():
             N = N + dt6 * (acc + k4)
         torch.cuda.synchronize()
         a, b = Nt.cpu().numpy(), N.cpu().numpy()
-        assert np.array_equal(a.view(np.int64), b.view(np.int64)), \
-            "n=%d: %d bins differ, max rel %.3e" % (n, int((a != b).sum()),
-                                                    float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))))
+        if with_breakage:
+            np.testing.assert_allclose(a, b, rtol=1e-14, atol=1e-14 * np.abs(b).max())
+        else:
+            assert np.array_equal(a.view(np.int64), b.view(np.int64)), \
+                "n=%d: %d bins differ, max rel %.3e" % (
+                    n, int((a != b).sum()),
+                    float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))))
 
 
 def test_checkpoint_interval_does_not_change_the_result():
