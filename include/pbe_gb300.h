@@ -128,7 +128,7 @@ int pbe_breakage_rhs_ex(const double* N, const double* x, const double* t_q,
  * codes that forbid allocation once time stepping starts, plug-in interfaces
  * with no way to pass a workspace -- this runs the same kernels as
  * pbe_aggregation_rhs_ex with its scratch in a fixed device array compiled
- * into the library (about 3.7 MiB, held by every GPU that loads the library).
+ * into the library (about 8.5 MiB, held by every GPU that loads the library).
  *   Limit: params->n <= 32768; larger n returns cudaErrorInvalidValue.
  *   The first call on a device looks up that array's address; make it before
  *   any stream capture starts.

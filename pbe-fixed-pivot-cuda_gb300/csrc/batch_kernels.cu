@@ -588,8 +588,11 @@ __device__ void batch_task(const BatchDev& d, const double* __restrict__ Yg,
     }
 }
 
+#ifndef PBE_BATCH_CTAS
+#define PBE_BATCH_CTAS 2
+#endif
 template <int K>
-__global__ void __launch_bounds__(kMainThreads, 2)
+__global__ void __launch_bounds__(kMainThreads, PBE_BATCH_CTAS)
 batch_main_kernel(BatchDev d, const double* __restrict__ Y,
                   const pbe_batch_cell_params_t* __restrict__ params, double* out, int accumulate,
                   const int4* __restrict__ bundles, const int4* __restrict__ tasks, int n_bundles)
@@ -624,7 +627,7 @@ cudaError_t main_k(const BatchDev& d, const double* Y, const pbe_batch_cell_para
     cudaError_t e = cudaMemsetAsync(d.counter, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     if (n_bundles <= 0) return cudaSuccess;
-    const int grid = n_bundles < 2 * d.num_sms ? n_bundles : 2 * d.num_sms;
+    const int grid = n_bundles < PBE_BATCH_CTAS * d.num_sms ? n_bundles : PBE_BATCH_CTAS * d.num_sms;
     batch_main_kernel<K><<<grid, kMainThreads, smem, s>>>(d, Y, params, out, accumulate ? 1 : 0,
                                                           bundles, tasks, n_bundles);
     return cudaGetLastError();

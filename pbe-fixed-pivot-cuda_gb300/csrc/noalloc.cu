@@ -11,7 +11,7 @@
 // file-scope device array below, which the library image carries and which
 // every GPU that loads the library holds until the process exits.
 //
-// Limit: n <= kNoAllocMaxN (32768 bins, about 3.7 MiB of scratch); larger n
+// Limit: n <= kNoAllocMaxN (32768 bins, about 8.5 MiB of scratch); larger n
 // returns cudaErrorInvalidValue without launching anything.
 //
 // Set-up: the first call on each device (with that device current) looks up
