@@ -253,20 +253,29 @@ __device__ __forceinline__ int first_parent_near(const double* __restrict__ x, i
     return b;
 }
 
-// Starting point for a warp: the first parent of bin ib by bisection of x's
-// bit patterns against x[ib] / t_q (integer compares; every lane of the warp
-// walks the same addresses), finished exactly by first_parent_near.
+// log2 of a positive normal double in FP32 (exponent from the bits, the
+// mantissa's log2 by the SFU): a few 1e-5 absolute, enough to guess an index.
+__device__ __forceinline__ float log2_approx(double v)
+{
+    const long long b = dbits(v);
+    const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+    const float m = __int_as_float(0x3f800000 | static_cast<int>((b >> 29) & 0x7fffff));   // [1, 2)
+    return static_cast<float>(e) + __log2f(m);
+}
+
+// Starting point for a warp: the first parent of bin ib, guessed where a
+// geometric grid through x[0] and x[n-1] would put x[ib] / t_q (FP32 logs on
+// the integer / SFU pipes, no FP64), finished exactly by first_parent_near
+// (on a geometric grid the guess is within a bin; elsewhere the gallop
+// corrects it in a logarithmic number of tests).
 __device__ __forceinline__ int first_parent(const double* __restrict__ x, int n, int ib, double tq,
-                                            double itq)
+                                            float lx0, float inv_span)
 {
     if (ib >= n) return n;
-    const long long yb = dbits(__ldg(x + ib) * itq);
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (dbits(__ldg(x + mid)) >= yb) hi = mid; else lo = mid + 1;
-    }
-    return first_parent_near(x, n, ib, tq, 0, lo);
+    const float ly = log2_approx(__ldg(x + ib)) - __log2f(static_cast<float>(tq));
+    float gf = (ly - lx0) * inv_span;
+    gf = fminf(fmaxf(gf, 0.0f), static_cast<float>(n));
+    return first_parent_near(x, n, ib, tq, 0, static_cast<int>(gf));
 }
 
 template <int F>
@@ -277,7 +286,6 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
                double S0, double v_ref, double alpha, double v_min)
 {
     if ((F == 0 || F == 3) && S0 == 0.0) return;     // S = 0 everywhere: no breakage at all
-    extern __shared__ double s_itq[];                 // [nq] 1 / t_q
     __shared__ double s_inv[34];                      // 1/(x[b+1] - x[b]), b = i0 - 1 .. i0 + 32
     __shared__ double s_acc[kBinWarpsMax][32];
     const int i0 = blockIdx.x * 32;
@@ -286,8 +294,11 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
         const int b = i0 - 1 + k;
         s_inv[k] = (b >= 0 && b < n - 1) ? 1.0 / (__ldg(x + b + 1) - __ldg(x + b)) : 0.0;
     }
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) s_itq[q] = 1.0 / __ldg(t_q + q);
     __syncthreads();
+    // index of a volume on the geometric grid through x[0] and x[n-1] (guesses only)
+    const float lx0 = log2_approx(__ldg(x));
+    const float span = log2_approx(__ldg(x + n - 1)) - lx0;
+    const float inv_span = (n > 1 && span > 0.0f) ? static_cast<float>(n - 1) / span : 0.0f;
 
     const int i = i0 + lane;
     const bool live = i < n;
@@ -301,14 +312,14 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
     constexpr bool kS0 = (F == 0 || F == 3);
     double acc = 0.0;
     for (int q = w; q < nq; q += W) {
-        const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q), itq = s_itq[q];
+        const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q);
         const double fbw = kS0 ? S0 * bw : bw;
         const double k_lo = fbw * inv_lo, k_hi = fbw * inv_hi;
         // fb of bins i0 - 1 + lane and, for lanes 0 and 1, of i0 + 31 and i0 + 32:
         // the warp's bin ib0 by a uniform bisection, the others near ib0's
         // parent plus their bin offset
         const int ib0 = max(i0 - 1, 0);
-        const int g0 = first_parent(x, n, ib0, tq, itq);
+        const int g0 = first_parent(x, n, ib0, tq, lx0, inv_span);
         const int ibl = max(i0 - 1 + lane, 0);
         const int f0 = first_parent_near(x, n, ibl, tq, g0, g0 + (ibl - ib0));
         int f1 = 0;
@@ -427,7 +438,7 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
                 brk_sn_kernel<F><<<(a.n + 255) / 256, 256, 0, s>>>(a.N, a.x, a.n, ws.SN, a.S0,
                                                                   a.v_ref, a.alpha, a.v_min);
             const int W = a.n_quad < kBinWarpsMax ? a.n_quad : kBinWarpsMax;
-            brk_bin_kernel<F><<<(a.n + 31) / 32, 32 * W, sizeof(double) * a.n_quad, s>>>(
+            brk_bin_kernel<F><<<(a.n + 31) / 32, 32 * W, 0, s>>>(
                 a.N, a.x, a.t_q, a.bw_q, a.rhs, a.n, a.n_quad, ws.SN, a.S0, a.v_ref, a.alpha,
                 a.v_min);
             return cudaGetLastError();
