@@ -56,6 +56,92 @@ struct VjpShared {
     double cinfo[kVMaxGroups][16];        // per-task cell values (batched)
 };
 
+// Rows of a geometric-grid pass: t in [T0, T0 + kVPass) of the task.
+#ifndef PBE_VJP_PASS
+#define PBE_VJP_PASS 6
+#endif
+constexpr int kVPass = PBE_VJP_PASS;
+static_assert(kVW % kVPass == 0 && kVW / kVPass <= 3, "row passes must split the task's rows in one to three");
+
+template <int K, int T0>
+__device__ __forceinline__ void vjp_geo_rows(const VjpCellView& v, int I, int r_begin, int r_end,
+                                             int tmax, double lamlast, double* R0, double* R1,
+                                             int lane, int T)
+{
+    const int n = v.n;
+    const double* __restrict__ x = v.x;
+    const double* __restrict__ N = v.N;
+    const double* __restrict__ h = v.h;
+    const double* __restrict__ lam = v.lam;
+    const double* __restrict__ D = v.D;
+    for (int d = r_begin + lane; d < r_end; d += T) {
+        const int L = __ldg(v.Ld + d);
+        const double sc = (d == 0) ? v.lag0_scale : 1.0;
+        const double Bf = __ldg(v.Bf + d) * sc, Sf = __ldg(v.Sf + d) * sc;
+        // upper visits: partner k = m + d
+#pragma unroll
+        for (int t = T0; t < T0 + kVPass; ++t) {
+            const int m = I + t, k = m + d;
+            if (t < tmax && k < n) {
+                const double Nk = __ldg(N + k);
+                const int lo = (L >= kLagClipAll) ? n : m + L;
+                double P;
+                if (lo >= n - 1) {
+                    P = lamlast;
+                } else {
+                    const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + m),
+                                                       __ldg(x + lo), 0);
+                    P = fma(th, __ldg(D + lo), __ldg(lam + lo));
+                }
+                if constexpr (K == 2) {
+                    R0[t] = fma(P, __ldg(h + k), R0[t]);
+                } else {
+                    const double t1 = P * Nk;
+                    if constexpr (K == 0) R0[t] += t1;
+                    if constexpr (K == 1) { R0[t] += t1; R1[t] = fma(P, __ldg(h + k), R1[t]); }
+                    if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
+                    if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sf, R1[t]);
+                }
+            }
+        }
+    }
+    for (int d = r_begin + lane; d < r_end; d += T) {
+        // lower visits: partner k = m - d (d >= 1); a lag whose every pair
+        // is clipped (L = kLagClipAll) gives lo >= n - 1 -> P = lambda_{n-1}
+        if (d == 0) continue;
+        const int L = __ldg(v.Ld + d);
+        const double Bf = __ldg(v.Bf + d), Sl = __ldg(v.Sl + d);
+        const int e = L - d;
+#pragma unroll
+        for (int t = T0; t < T0 + kVPass; ++t) {
+            const int m = I + t, k = m - d;
+            if (t < tmax && k >= 0) {
+                const int lo = m + e;
+                double P;
+                if (lo >= n - 1) {
+                    P = lamlast;
+                } else {
+                    const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
+                                                       __ldg(x + lo), 0);
+                    P = fma(th, __ldg(D + lo), __ldg(lam + lo));
+                }
+                if constexpr (K == 2) {
+                    R0[t] = fma(P, __ldg(h + k), R0[t]);
+                } else {
+                    const double Nk = __ldg(N + k);
+                    if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
+                    if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(h + k), R1[t]); }
+                    if constexpr (K >= 3) {
+                        const double t1 = P * Nk;
+                        if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
+                        if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sl, R1[t]);
+                    }
+                }
+            }
+        }
+    }
+}
+
 // Row sums of the task's rows into sm.fin[G.g]; red: the group's first column
 // of the kVRows x kMainThreads reduction buffer (row stride kMainThreads).
 // Row sums over the partner range [r_begin, r_end) (lags on a geometric
@@ -82,75 +168,14 @@ __device__ __forceinline__ void vjp_tile_accumulate(const VjpCellView& v, int I,
     for (int t = 0; t < VW; ++t) { R0[t] = 0.0; R1[t] = 0.0; }
 
     if (v.geo) {
-        // two passes over the lags (upper visits, then lower visits), so each
-        // hot loop is half the code: the unrolled 12-row body with the inlined
-        // weight emulation otherwise overflows the instruction cache
-        for (int d = r_begin + lane; d < r_end; d += T) {
-            const int L = __ldg(v.Ld + d);
-            const double sc = (d == 0) ? v.lag0_scale : 1.0;
-            const double Bf = __ldg(v.Bf + d) * sc, Sf = __ldg(v.Sf + d) * sc;
-            // upper visits: partner k = m + d
-#pragma unroll
-            for (int t = 0; t < VW; ++t) {
-                const int m = I + t, k = m + d;
-                if (t < tmax && k < n) {
-                    const double Nk = __ldg(N + k);
-                    const int lo = (L >= kLagClipAll) ? n : m + L;
-                    double P;
-                    if (lo >= n - 1) {
-                        P = lamlast;
-                    } else {
-                        const double th = sum_minus_scaled(__ldg(x + k), __ldg(x + m),
-                                                           __ldg(x + lo), 0);
-                        P = fma(th, __ldg(D + lo), __ldg(lam + lo));
-                    }
-                    if constexpr (K == 2) {
-                        R0[t] = fma(P, __ldg(h + k), R0[t]);
-                    } else {
-                        const double t1 = P * Nk;
-                        if constexpr (K == 0) R0[t] += t1;
-                        if constexpr (K == 1) { R0[t] += t1; R1[t] = fma(P, __ldg(h + k), R1[t]); }
-                        if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
-                        if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sf, R1[t]);
-                    }
-                }
-            }
-        }
-        for (int d = r_begin + lane; d < r_end; d += T) {
-            // lower visits: partner k = m - d (d >= 1); a lag whose every pair
-            // is clipped (L = kLagClipAll) gives lo >= n - 1 -> P = lambda_{n-1}
-            if (d == 0) continue;
-            const int L = __ldg(v.Ld + d);
-            const double Bf = __ldg(v.Bf + d), Sl = __ldg(v.Sl + d);
-            const int e = L - d;
-#pragma unroll
-            for (int t = 0; t < VW; ++t) {
-                const int m = I + t, k = m - d;
-                if (t < tmax && k >= 0) {
-                    const int lo = m + e;
-                    double P;
-                    if (lo >= n - 1) {
-                        P = lamlast;
-                    } else {
-                        const double th = sum_minus_scaled(__ldg(x + m), __ldg(x + k),
-                                                           __ldg(x + lo), 0);
-                        P = fma(th, __ldg(D + lo), __ldg(lam + lo));
-                    }
-                    if constexpr (K == 2) {
-                        R0[t] = fma(P, __ldg(h + k), R0[t]);
-                    } else {
-                        const double Nk = __ldg(N + k);
-                        if constexpr (K == 0) R0[t] = fma(P, Nk, R0[t]);
-                        if constexpr (K == 1) { R0[t] = fma(P, Nk, R0[t]); R1[t] = fma(P, __ldg(h + k), R1[t]); }
-                        if constexpr (K >= 3) {
-                            const double t1 = P * Nk;
-                            if constexpr (K == 3 || K == 5) R0[t] = fma(t1, Bf, R0[t]);
-                            if constexpr (K == 4 || K == 5) R1[t] = fma(t1, Sl, R1[t]);
-                        }
-                    }
-                }
-            }
-        }
+        // rows in passes of kVPass, each pass two loops over the lags (upper
+        // visits, then lower visits): each hot loop holds kVPass unrolled rows
+        // with the inlined weight emulation, small enough for the
+        // instruction cache
+        vjp_geo_rows<K, 0>(v, I, r_begin, r_end, tmax, lamlast, R0, R1, lane, T);
+        if constexpr (kVPass < VW) vjp_geo_rows<K, kVPass>(v, I, r_begin, r_end, tmax, lamlast, R0, R1, lane, T);
+        if constexpr (2 * kVPass < VW)
+            vjp_geo_rows<K, 2 * kVPass>(v, I, r_begin, r_end, tmax, lamlast, R0, R1, lane, T);
     } else {
         // generic grid: thread `lane` owns the partner chunk [k0, k1) and walks
         // the bracket of x_m + x_k upward along it for every row of the tile
