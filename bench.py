@@ -684,7 +684,7 @@ def summarize(sections: dict, value: float) -> dict:
     if b:
         out["batched_config3"] = {k: b[k] for k in ("cell_steps_per_s", "percell_loop_cell_steps_per_s",
                                                     "speedup_vs_percell_loop", "finite_after_100_steps")}
-        out["batched_config3"]["fp64_pipe_frac"] = b["roofline"]["fp64_pipe_frac"]
+        out["batched_config3"]["roofline_frac"] = b.get("roofline", {}).get("frac")
     a = sections.get("adjoint")
     if a:
         out["adjoint_config4"] = {k: a[k] for k in ("forward_ms", "backward_ms", "gradient_cost_ratio",
