@@ -378,6 +378,32 @@ inline size_t brk_ws_layout(int n, int nq, char* base, BrkWs* ws)
 // The single-instance VJP may split each row tile's partner range into up to
 // this many chunks (separate tasks) to even out the last wave.
 constexpr int kVjpMaxChunks = 8;
+
+// Lane-block VJP tasks on geometric grids (vjp.cu): row block b holds the rows
+// [32 b, 32 b + 32) and meets the lags d in [1, n - 1 - 32 b] (partner
+// k = j + d), cut into chunks of vjp_lane_chunk(n) lags. Task (b, c) has the
+// index sum_{c' < c} vjp_lane_chunk_blocks(c') + b; it stores the 2 x 32 sums
+// of its rows as the smaller member and C + 32 sums of the rows
+// 32 b + c C + i (i < C + 32) as the larger member.
+// C >= 32: a row then lies in the windows of at most two chunks of a block.
+__host__ __device__ constexpr int vjp_lane_chunk(int n) { return lane_chunk_len(n); }
+static_assert(kLaneMinChunk >= 32, "vjp lane chunks must be at least 32 lags");
+// Row blocks that have chunk c (blocks 0 .. cnt-1: the lag range shrinks with b).
+__host__ __device__ constexpr int vjp_lane_chunk_blocks(int n, int c, int C)
+{
+    const long long r = n - 1 - static_cast<long long>(c) * C;   // lags of block 0 from chunk c on
+    return r >= 1 ? static_cast<int>((r - 1) / kLaneBins + 1) : 0;
+}
+__host__ __device__ constexpr int vjp_lane_chunks(int n, int C)
+{
+    return n >= 2 ? (n - 2) / C + 1 : 0;
+}
+__host__ __device__ constexpr long long vjp_lane_tasks(int n, int C)
+{
+    long long s = 0;
+    for (int c = 0; vjp_lane_chunk_blocks(n, c, C) > 0; ++c) s += vjp_lane_chunk_blocks(n, c, C);
+    return s;
+}
 struct VjpWs {
     double* h;         // [n]  x_i N_i
     double* a;         // [n]  x_i^(1/3)
@@ -391,7 +417,9 @@ struct VjpWs {
     double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
     double* gpart;     // [max(ntile, n / 8) * 4] per-task / per-block parameter partials
     double* vpart;     // [ntile * kVjpMaxChunks * 2 kTileW] row sums per (tile, partner chunk)
-    int*    counter;   // [8]
+    double* lup;       // [lane tasks * 64] lane-task sums of the rows as smaller members
+    double* llo;       // [lane tasks * (C + 32)] lane-task sums of the rows as larger members
+    int*    counter;   // [8]: 0 tile tasks, 1 lane tasks
 };
 
 inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
@@ -415,6 +443,10 @@ inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
     w.gpart    = reinterpret_cast<double*>(take(sizeof(double) * 4 * static_cast<size_t>(ntile > nbb ? ntile : nbb)));
     w.vpart    = reinterpret_cast<double*>(take(sizeof(double) * 2 * kTileW * kVjpMaxChunks *
                                                 static_cast<size_t>(ntile)));
+    const int C = vjp_lane_chunk(n);
+    const size_t ltasks = static_cast<size_t>(vjp_lane_tasks(n, C));
+    w.lup      = reinterpret_cast<double*>(take(sizeof(double) * 2 * kLaneBins * ltasks));
+    w.llo      = reinterpret_cast<double*>(take(sizeof(double) * (C + 32) * ltasks));
     w.counter  = reinterpret_cast<int*>(take(sizeof(int) * 8));
     if (ws) *ws = w;
     return off;

@@ -25,6 +25,8 @@
 // (PowerLaw: dS/dalpha = S ln(x/v_ref)), dL/dv_min = 0 (threshold step).
 // =============================================================================
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "pbe_internal.cuh"
 #include "vjp_tile.cuh"
@@ -135,21 +137,24 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
         const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
         ws.mom[10] = (n >= 2 && mx_s <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
         ws.counter[0] = 0;
+        ws.counter[1] = 0;
     }
 }
 
 // Pair sums: task = (row tile, partner chunk); the whole CTA is one group.
 // Each task stores its rows' two sums per chunk; vjp_rows_kernel adds the
 // chunks in order and finishes the rows.
+// lane_on: the lane-block kernel takes geometric grids (this one returns).
 template <int K>
 __global__ void __launch_bounds__(kMainThreads, 2)
 vjp_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
-                const double* __restrict__ lam, VjpWs ws, int n, int ntile, int nch)
+                const double* __restrict__ lam, VjpWs ws, int n, int ntile, int nch, int lane_on)
 {
     extern __shared__ double red[];               // [kVRows][kMainThreads]
     __shared__ VjpShared sm;
     __shared__ int s_task;
 
+    if (lane_on && ws.mom[10] != 0.0) return;
     const int tid = threadIdx.x;
     VjpCellView v;
     v.x = x; v.N = N; v.h = ws.h; v.lam = lam; v.D = ws.D; v.a = ws.a; v.ia = ws.ia;
@@ -179,9 +184,10 @@ template <int K>
 __global__ void __launch_bounds__(256)
 vjp_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
-                int ntile, int nch, double b0, double bbr, double bsh)
+                int ntile, int nch, double b0, double bbr, double bsh, int lane_on)
 {
     __shared__ double fin[8][kVRows];
+    if (lane_on && ws.mom[10] != 0.0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x * 8 + w;
     if (tile >= ntile) return;                    // whole warp
@@ -216,17 +222,276 @@ vjp_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     }
 }
 
-// gp[0..2] += fixed-order sums of the per-tile partials
+// gp[0..nslots) += fixed-order sums of the per-tile partials
 // One block: parameter slot q (< nslots <= 4) summed by warp q over the
-// tasks' partials in a fixed order.
-__global__ void __launch_bounds__(128) vjp_gfin_kernel(int ntile, VjpWs ws, double* gp, int nslots)
+// tasks' partials in a fixed order. nlane > 0: on a geometric grid the lane
+// rows kernel wrote nlane partials instead of ntile.
+__global__ void __launch_bounds__(128) vjp_gfin_kernel(int ntile, VjpWs ws, double* gp, int nslots,
+                                                       int nlane)
 {
     const int q = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (q >= nslots) return;
+    if (nlane > 0 && ws.mom[10] != 0.0) ntile = nlane;
     double s = 0.0;
     for (int b = l; b < ntile; b += 32) s += ws.gpart[b * 4 + q];
     s = warp_sum(s);
     if (l == 0) gp[q] += s;
+}
+
+// -------------------------------------------------------------------------
+// Lane blocks (geometric grids). Lane l of a warp owns row j = 32 b + l and
+// walks the lags d of its share: the pair (j, k = j + d) lands at
+// lo = j + Ld[d], P = lambda_lo + (fl(x_j + x_k) - x_lo) D_lo (lambda_{n-1} when
+// clipped). The row of the smaller member sums in registers (U0, U1: the
+// tile path's sums of the upper visits); the row of the larger member,
+// k = j + d, is the row lane l + 1 held one lag earlier, so its sum W (the
+// whole lower-visit term, parameters included) moves one lane down per lag;
+// lane 0's finished W leaves the warp each lag into a shared window, and
+// every lane's W at the end of the share. Brownian + shear: 7 FP64
+// instructions per pair (P; P Bf, P Sf; two sums of the smaller member; two
+// FMAs into W) against 8 for the two visits of the tile path.
+// Determinism: the windows of the CTA's warps are added in warp order; the
+// rows kernel adds the tasks' sums in a fixed order.
+// -------------------------------------------------------------------------
+#ifndef PBE_VJP_LANE_CTAS
+#define PBE_VJP_LANE_CTAS 3
+#endif
+constexpr int kVLaneCtas = PBE_VJP_LANE_CTAS;
+constexpr int kLaneWarps = kMainThreads / 32;   // warps sharing a task's lags
+constexpr int kVLaneMaxChunks = 64;        // vjp_lane_chunks(n, C) bound (C >= n / 16)
+
+template <int K>
+__global__ void __launch_bounds__(kMainThreads, kVLaneCtas)
+vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                const double* __restrict__ lam, VjpWs ws, int n, int ntasks, int C,
+                double b0, double bbr, double bsh)
+{
+    extern __shared__ double esm[];               // [kLaneWarps][per_max + 32] W windows
+    __shared__ double red[kLaneWarps][2][kLaneBins];
+    __shared__ int s_task;
+
+    if (ws.mom[10] == 0.0) return;                // not geometric: the tile kernel runs
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const double* __restrict__ h = ws.h;
+    const double* __restrict__ D = ws.D;
+    const int* __restrict__ Ld = ws.Ld;
+    const double lamlast = lam[n - 1];
+    const int ew = (C + kLaneWarps - 1) / kLaneWarps + 32;
+    double* eb = esm + w * ew;
+
+    for (;;) {
+        if (tid == 0) s_task = atomicAdd(ws.counter + 1, 1);
+        __syncthreads();
+        const int tix = s_task;
+        __syncthreads();
+        if (tix >= ntasks) break;
+        int b = tix, c = 0;
+        for (;;) {
+            const int cnt = vjp_lane_chunk_blocks(n, c, C);
+            if (b < cnt || cnt == 0) break;
+            b -= cnt;
+            ++c;
+        }
+        const int J = kLaneBins * b;
+        const int dA = 1 + c * C;
+        const int dB = min(dA + C, n - J);        // lags [dA, dB), dB - 1 <= n - 1 - J
+        const int len = dB - dA;
+        const int per = (len + kLaneWarps - 1) / kLaneWarps;
+        const int dw0 = dA + w * per;
+        const int dw1 = min(dB, dw0 + per);
+
+        const int j = J + lane;
+        const bool jv = j < n;
+        const double xj = jv ? __ldg(x + j) : 0.0;
+        const double Nj = jv ? __ldg(N + j) : 0.0;
+        const double hj = jv ? h[j] : 0.0;
+        // lane constants of the lower-visit term
+        double cN = 0.0, cH = 0.0;
+        if constexpr (K == 0) cN = b0 * Nj;
+        if constexpr (K == 1) { cN = b0 * Nj; cH = b0 * hj; }
+        if constexpr (K == 2) cH = b0 * hj;
+        if constexpr (K == 3) cN = bbr * Nj;
+        if constexpr (K == 4) cH = bsh * hj;
+        if constexpr (K == 5) { cN = bbr * Nj; cH = bsh * hj; }
+        const int jtop = n - 1 - j;               // lo >= n - 1 <=> Ld[d] >= jtop
+
+        double U0 = 0.0, U1 = 0.0, W = 0.0;
+        for (int d = dw0; d < dw1; ++d) {
+            // lane 0's row (j + d - 1) is complete: out; every row moves one lane down
+            const double Wd = __shfl_down_sync(0xffffffffu, W, 1);
+            if (lane == 0) eb[d - dw0] = W;
+            W = (lane == 31) ? 0.0 : Wd;
+            const int L = __ldg(Ld + d);
+            double Bf = 0.0, Sf = 0.0;
+            if constexpr (K == 3 || K == 5) Bf = __ldg(ws.Bf + d);
+            if constexpr (K == 4 || K == 5) Sf = __ldg(ws.Sf + d);
+            const int k = j + d;
+            if (k < n) {
+                const double xk = __ldg(x + k);
+                double P = lamlast;
+                if (L < jtop) {
+                    const int lo = j + L;
+                    P = fma(sum_minus_scaled(xk, xj, __ldg(x + lo), 0), D[lo], lam[lo]);
+                }
+                if constexpr (K == 0) {
+                    U0 = fma(P, __ldg(N + k), U0);
+                    W = fma(P, cN, W);
+                } else if constexpr (K == 1) {
+                    U0 = fma(P, __ldg(N + k), U0);
+                    U1 = fma(P, h[k], U1);
+                    W = fma(P, fma(cN, xk, cH), W);
+                } else if constexpr (K == 2) {
+                    U0 = fma(P, h[k], U0);
+                    W = fma(P * xk, cH, W);
+                } else {
+                    const double Nk = __ldg(N + k);
+                    if constexpr (K == 3 || K == 5) {
+                        const double u0 = P * Bf;
+                        U0 = fma(u0, Nk, U0);
+                        W = fma(u0, cN, W);
+                    }
+                    if constexpr (K == 4 || K == 5) {
+                        const double u1 = P * Sf;
+                        U1 = fma(u1, Nk, U1);
+                        W = fma(u1, cH, W);
+                    }
+                }
+            }
+        }
+        if (dw1 > dw0) eb[dw1 - dw0 + lane] = W;  // rows j + dw1 - 1
+        red[w][0][lane] = U0;
+        red[w][1][lane] = U1;
+        __syncthreads();
+        if (w == 0) {
+            double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+            for (int q = 0; q < kLaneWarps; ++q) {
+                s0 += red[q][0][lane];
+                s1 += red[q][1][lane];
+            }
+            ws.lup[static_cast<size_t>(tix) * 2 * kLaneBins + lane] = s0;
+            ws.lup[static_cast<size_t>(tix) * 2 * kLaneBins + kLaneBins + lane] = s1;
+        }
+        // the task's window: entry i is row J + dA - 1 + i, i < len + 32; warp q's
+        // window starts at i = q per and holds its share's length + 32 entries
+        double* seg = ws.llo + static_cast<size_t>(tix) * (C + 32);
+        for (int i = tid; i < len + 32; i += kMainThreads) {
+            double sum = 0.0;
+            for (int q = 0; q < kLaneWarps; ++q) {
+                const int q0 = q * per, q1 = min(len, q0 + per);
+                if (q1 <= q0) break;
+                const int o = i - q0;
+                if (o >= 0 && o < q1 - q0 + 32) sum += esm[q * ew + o];
+            }
+            seg[i] = sum;
+        }
+        __syncthreads();
+    }
+}
+
+// Rows of the lane path: one CTA per row block b (rows 32 b + lane). Warp g
+// adds the larger-member sums of the row blocks b' = g, g + 8, ... <= b (the
+// chunk holding lag d = m - 32 b' and, for the first 32 lags of a chunk, the
+// tail of the chunk before); warp 0 adds the eight in order, the block's own
+// smaller-member sums chunk by chunk, the diagonal pair, the death moments,
+// and stores dL/dN_m and the block's parameter partials.
+template <int K>
+__global__ void __launch_bounds__(256)
+vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
+                     const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
+                     int C, double b0, double bbr, double bsh)
+{
+    __shared__ double lw[kLaneWarps][kLaneBins];
+    __shared__ int base[kVLaneMaxChunks + 1];
+    if (ws.mom[10] == 0.0) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x;
+    const int m = kLaneBins * b + lane;
+    const int nchunks = vjp_lane_chunks(n, C);
+    if (threadIdx.x == 0) {
+        int sacc = 0;
+        for (int c = 0; c < nchunks; ++c) {
+            base[c] = sacc;
+            sacc += vjp_lane_chunk_blocks(n, c, C);
+        }
+    }
+    __syncthreads();
+    const size_t S = static_cast<size_t>(C) + 32;
+    double acc = 0.0;
+    if (m < n) {
+        for (int bp = w; bp <= b; bp += kLaneWarps) {
+            const int d = m - kLaneBins * bp;
+            if (d < 1) continue;
+            const int nch = (n - 1 - kLaneBins * bp + C - 1) / C;
+            const int c1 = d / C, idx = d - c1 * C;
+            if (c1 >= 1 && idx < 32) acc += __ldcg(ws.llo + (base[c1 - 1] + bp) * S + C + idx);
+            if (c1 < nch) acc += __ldcg(ws.llo + (base[c1] + bp) * S + idx);
+        }
+    }
+    lw[w][lane] = acc;
+    __syncthreads();
+    if (w != 0) return;
+
+    double gB = 0.0, gS = 0.0;
+    if (m < n) {
+        double Wm = 0.0;
+#pragma unroll
+        for (int q = 0; q < kLaneWarps; ++q) Wm += lw[q][lane];
+        const int dmax = n - 1 - kLaneBins * b;
+        const int nchb = dmax >= 1 ? (dmax + C - 1) / C : 0;
+        double U0 = 0.0, U1 = 0.0;
+        for (int c = 0; c < nchb; ++c) {
+            const double* up = ws.lup + static_cast<size_t>(base[c] + b) * 2 * kLaneBins;
+            U0 += __ldcg(up + lane);
+            U1 += __ldcg(up + kLaneBins + lane);
+        }
+        // diagonal pair (m, m), counted once
+        const double xm = x[m], Nm = N[m], hm = ws.h[m], lm = lam[m];
+        const int L0 = ws.Ld[0];
+        double P = lam[n - 1];
+        if (L0 < n - 1 - m) {
+            const int lo = m + L0;
+            P = fma(sum_minus_scaled(xm, xm, x[lo], 0), ws.D[lo], lam[lo]);
+        }
+        double d0 = 0.0, d1 = 0.0;
+        if constexpr (K == 0) d0 = P * Nm;
+        if constexpr (K == 1) { d0 = P * Nm; d1 = P * hm; }
+        if constexpr (K == 2) d0 = P * hm;
+        if constexpr (K == 3 || K == 5) d0 = (P * Nm) * ws.Bf[0];
+        if constexpr (K == 4 || K == 5) d1 = (P * Nm) * ws.Sf[0];
+        U0 += d0;
+        U1 += d1;
+        // Tv: the smaller-member sums (diagonal included) weighted as the kernel
+        // factor f(m, k) N_k; Td: the diagonal's share
+        double Tv0 = U0, Td0 = d0, Tv1 = 0.0, Td1 = 0.0;
+        if constexpr (K == 1) { Tv0 = fma(xm, U0, U1); Td0 = fma(xm, d0, d1); }
+        if constexpr (K == 2) { Tv0 = xm * U0; Td0 = xm * d0; }
+        if constexpr (K == 4 || K == 5) { Tv1 = xm * U1; Td1 = xm * d1; }
+        const double am = ws.a[m], iam = ws.ia[m];
+        const double* M = ws.mom;
+        const double* Lm = ws.mom + 5;
+        double g = Wm;
+        if constexpr (K != 4) {
+            const double dth0 = fma(lm, moment_factor<K, 0>(xm, am, iam, M), moment_factor<K, 0>(xm, am, iam, Lm));
+            const double coef = (K <= 2) ? b0 : bbr;
+            g = fma(coef, Tv0 - dth0, g);
+            gB = Nm * Tv0 - 0.5 * Nm * (Td0 + dth0);
+        }
+        if constexpr (K == 4 || K == 5) {
+            const double dth1 = fma(lm, moment_factor<K, 1>(xm, am, iam, M), moment_factor<K, 1>(xm, am, iam, Lm));
+            g = fma(bsh, Tv1 - dth1, g);
+            gS = Nm * Tv1 - 0.5 * Nm * (Td1 + dth1);
+        }
+        gN[m] += g;
+    }
+    const double s0 = warp_sum(gB);
+    const double s1 = warp_sum(gS);
+    if (lane == 0) {
+        // slots: 0 beta0, 1 beta_br, 2 beta_sh
+        ws.gpart[b * 4 + 0] = (K <= 2) ? s0 : 0.0;
+        ws.gpart[b * 4 + 1] = (K == 3 || K == 5) ? s0 : 0.0;
+        ws.gpart[b * 4 + 2] = (K == 4 || K == 5) ? s1 : 0.0;
+    }
 }
 
 // -------------------------------------------------------------------------
@@ -311,6 +576,17 @@ int vjp_chunks(int ntile, int num_sms, int n)
     return best;
 }
 
+// Aggregation VJP pair sums on geometric grids: lane blocks (default) or the
+// row tiles of every grid. PBE_GB300_VJP_PATH=tile selects the tiles.
+int vjp_lane_mode()
+{
+    static const int mode = []() {
+        const char* e = std::getenv("PBE_GB300_VJP_PATH");
+        return (e && std::strcmp(e, "tile") == 0) ? 0 : 1;
+    }();
+    return mode;
+}
+
 template <int K>
 cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStream_t s)
 {
@@ -324,12 +600,26 @@ cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStr
     cudaError_t e = cudaFuncSetAttribute(vjp_main_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+    const int C = vjp_lane_chunk(n);
+    const long long ltasks = vjp_lane_tasks(n, C);
+    const int lane_on = (vjp_lane_mode() && ltasks > 0 && vjp_lane_chunks(n, C) <= kVLaneMaxChunks) ? 1 : 0;
     vjp_prep_kernel<<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
     vjp_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
-    vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, ws, n, ntile, nch);
+    const int nrb = (n + kLaneBins - 1) / kLaneBins;
+    if (lane_on) {
+        const size_t lsmem = sizeof(double) * kLaneWarps * ((C + kLaneWarps - 1) / kLaneWarps + 32);
+        const int lgrid = static_cast<int>(ltasks < kVLaneCtas * num_sms ? ltasks : kVLaneCtas * num_sms);
+        vjp_lane_kernel<K><<<lgrid, kMainThreads, lsmem, s>>>(a.N, a.x, a.lam, ws, n,
+                                                              static_cast<int>(ltasks), C,
+                                                              a.beta0, a.beta_br, a.beta_sh);
+    }
+    vjp_main_kernel<K><<<grid, kMainThreads, smem, s>>>(a.N, a.x, a.lam, ws, n, ntile, nch, lane_on);
     vjp_rows_kernel<K><<<(ntile + 7) / 8, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, nch,
-                                                       a.beta0, a.beta_br, a.beta_sh);
-    vjp_gfin_kernel<<<1, 128, 0, s>>>(ntile, ws, a.gp, 3);
+                                                       a.beta0, a.beta_br, a.beta_sh, lane_on);
+    if (lane_on)
+        vjp_lane_rows_kernel<K><<<nrb, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, C, a.beta0,
+                                                    a.beta_br, a.beta_sh);
+    vjp_gfin_kernel<<<1, 128, 0, s>>>(ntile, ws, a.gp, 3, lane_on ? nrb : 0);
     return cudaGetLastError();
 }
 
@@ -341,7 +631,7 @@ cudaError_t brk_vjp_f(const BrkVjpArgs& a, const VjpWs& ws, cudaStream_t s)
     const int nb = static_cast<int>((static_cast<long long>(a.n) * nqp + 255) / 256);
     brk_vjp_kernel<F><<<nb, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.lam, a.gN, ws.gpart, a.n,
                                          a.n_quad, nqp, a.S0, a.v_ref, a.alpha, a.v_min);
-    vjp_gfin_kernel<<<1, 128, 0, s>>>(nb, ws, a.gp, 4);
+    vjp_gfin_kernel<<<1, 128, 0, s>>>(nb, ws, a.gp, 4, 0);
     return cudaGetLastError();
 }
 

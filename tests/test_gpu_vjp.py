@@ -130,3 +130,72 @@ def test_vjp_matches_finite_differences_of_gpu_forward():
         setattr(pm, name, base - hp)
         fd = (L(N, pp) - L(N, pm)) / (2 * hp)
         assert abs(fd - gp[idx]) <= 1e-6 * abs(gp[idx]) + 1e-9 * Labs / hp, (name, fd, gp[idx])
+
+
+@pytest.mark.parametrize("kernel,b0,bbr,bsh", AGG_KERNELS, ids=[str(k[0]) for k in AGG_KERNELS])
+def test_aggregation_vjp_matches_oracle_many_lag_chunks(kernel, b0, bbr, bsh):
+    """n = 4500 on a geometric grid: the lane-block path with 18 lag chunks
+    of 256 lags, 141 row blocks (the last one partial), rows whose larger-member
+    sums come from two chunks of a block."""
+    rng = np.random.default_rng(700 + kernel)
+    n = 4500
+    x = pg.grids.geometric_pow2(n, 1e-21, 256.0)
+    N = make_N("random", x, rng)
+    lam = rng.normal(size=n)
+    p = agg_params(n, kernel, b0, bbr, bsh, x)
+    code, gN, gp = gpu_agg_vjp(N, x, lam, p)
+    assert code == 0, pg.error_string(code)
+    rN, rp, sN, sp, _ = pyoracle.aggregation_rhs_vjp(N, x, lam, kernel, b0, bbr, bsh, p.log_x0,
+                                                     p.inv_log_r, exact_bracket=True,
+                                                     with_scale=True)
+    assert_close(gN, rN, sN, "dL/dN k=%d n=%d" % (kernel, n))
+    assert_close(gp, rp, sp, "dL/dbeta k=%d n=%d" % (kernel, n))
+
+
+def test_aggregation_vjp_lane_and_tile_paths_agree_at_16384():
+    """The bench's n = 16384 Brownian + shear case through the lane-block path
+    (this process) and the row-tile path (a child process with
+    PBE_GB300_VJP_PATH=tile): the same sums in another order, so within
+    1e-12 of each entry's scale (the sum of |terms|, from the oracle at this
+    size)."""
+    import os
+    import subprocess
+    import sys
+    import tempfile
+
+    n = 16384
+    x = pg.grids.geometric_pow2(n, 1e-21, 512.0)
+    N = pg.grids.lognormal_ic(x, 2048, 1.0, 1e14)
+    lam = np.random.default_rng(11).normal(size=n)
+    p = agg_params(n, 5, 0.0, 6.73e-18, 66.67, x)
+    code, gN, gp = gpu_agg_vjp(N, x, lam, p)
+    assert code == 0
+    here = os.path.dirname(os.path.abspath(__file__))
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "in.npz")
+        dst = os.path.join(d, "out.npz")
+        np.savez(src, N=N, x=x, lam=lam, log_x0=p.log_x0, inv_log_r=p.inv_log_r)
+        child = (
+            "import sys; sys.path[:0] = [%r, %r, %r]\n"
+            "import numpy as np, torch, pbe_gb300 as pg\n"
+            "from gpu_util import agg_params, t\n"
+            "z = np.load(%r)\n"
+            "n = len(z['x'])\n"
+            "p = agg_params(n, 5, 0.0, 6.73e-18, 66.67, z['x'])\n"
+            "gN = torch.zeros(n, dtype=torch.float64, device='cuda')\n"
+            "gp = torch.zeros(3, dtype=torch.float64, device='cuda')\n"
+            "assert pg.aggregation_rhs_vjp(t(z['N']), t(z['x']), t(z['lam']), gN, gp, p) == 0\n"
+            "np.savez(%r, gN=gN.cpu().numpy(), gp=gp.cpu().numpy())\n"
+            % (here, os.path.join(os.path.dirname(here), "pbe-fixed-pivot-cuda_gb300"),
+               os.path.join(os.path.dirname(here), "oracle"), src, dst))
+        env = dict(os.environ, PBE_GB300_VJP_PATH="tile")
+        subprocess.run([sys.executable, "-c", child], env=env, check=True, timeout=600)
+        o = np.load(dst)
+        tN, tp = o["gN"], o["gp"]
+    rN, rp, sN, sp, _ = pyoracle.aggregation_rhs_vjp(N, x, lam, 5, 0.0, 6.73e-18, 66.67, p.log_x0,
+                                                     p.inv_log_r, exact_bracket=True,
+                                                     with_scale=True)
+    assert_close(gN, tN, sN, "lane vs tile dL/dN")
+    assert_close(gp, tp, sp, "lane vs tile dL/dbeta")
+    assert_close(gN, rN, sN, "lane vs oracle dL/dN")
+    assert_close(gp, rp, sp, "lane vs oracle dL/dbeta")
