@@ -253,16 +253,6 @@ __device__ __forceinline__ int first_parent_near(const double* __restrict__ x, i
     return b;
 }
 
-// log2 of a positive normal double in FP32 (exponent from the bits, the
-// mantissa's log2 by the SFU): a few 1e-5 absolute, enough to guess an index.
-__device__ __forceinline__ float log2_approx(double v)
-{
-    const long long b = dbits(v);
-    const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
-    const float m = __int_as_float(0x3f800000 | static_cast<int>((b >> 29) & 0x7fffff));   // [1, 2)
-    return static_cast<float>(e) + __log2f(m);
-}
-
 // Starting point for a warp: the first parent of bin ib, guessed where a
 // geometric grid through x[0] and x[n-1] would put x[ib] / t_q (FP32 logs on
 // the integer / SFU pipes, no FP64), finished exactly by first_parent_near

@@ -189,6 +189,31 @@ __device__ __forceinline__ int frag_bracket(const double* __restrict__ x, int n,
     return bracket_lo(x, n, v);
 }
 
+// log2 of a positive normal double in FP32 (exponent from the bits, the
+// mantissa's log2 by the SFU): a few 1e-5 absolute, enough to guess an index.
+__device__ __forceinline__ float log2_approx(double v)
+{
+    const long long b = dbits(v);
+    const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+    const float m = __int_as_float(0x3f800000 | static_cast<int>((b >> 29) & 0x7fffff));   // [1, 2)
+    return static_cast<float>(e) + __log2f(m);
+}
+
+// frag_bracket, started where a geometric grid through x[0] and x[n-1] would
+// put v (lx0 = log2_approx(x[0]), inv_span = (n - 1) / (log2 x[n-1] - lx0)),
+// then galloping to the exact bracket: one or two loads on a geometric grid,
+// a logarithmic number on any other.
+__device__ __forceinline__ int frag_bracket_guess(const double* __restrict__ x, int n, double v,
+                                                  float lx0, float inv_span)
+{
+    if (dbits(v) <= dbits(__ldg(x)) || !(v > 0.0)) return -1;
+    if (dbits(v) >= dbits(__ldg(x + n - 1))) return n - 1;
+    float gf = (log2_approx(v) - lx0) * inv_span;
+    gf = fminf(fmaxf(gf, 0.0f), static_cast<float>(n - 2));
+    const int g = static_cast<int>(gf);
+    return dbits(__ldg(x + g)) <= dbits(v) ? bracket_from(x, n, v, g) : bracket_down(x, v, g - 1);
+}
+
 // frag_bracket of a v at or below a volume whose frag_bracket is `above`.
 __device__ __forceinline__ int frag_bracket_below(const double* __restrict__ x, int n, double v,
                                                   int above)
@@ -385,9 +410,21 @@ constexpr int kVjpMaxChunks = 8;
 // index sum_{c' < c} vjp_lane_chunk_blocks(c') + b; it stores the 2 x 32 sums
 // of its rows as the smaller member and C + 32 sums of the rows
 // 32 b + c C + i (i < C + 32) as the larger member.
-// C >= 32: a row then lies in the windows of at most two chunks of a block.
-__host__ __device__ constexpr int vjp_lane_chunk(int n) { return lane_chunk_len(n); }
-static_assert(kLaneMinChunk >= 32, "vjp lane chunks must be at least 32 lags");
+// Chunk length: at least n / PBE_VJP_CHUNK_DIV lags, a multiple of 64, at least
+// kLaneMinChunk. C >= 32: a row then lies in the windows of at most two chunks
+// of a block.
+#ifndef PBE_VJP_CHUNK_DIV
+#define PBE_VJP_CHUNK_DIV 16
+#endif
+#ifndef PBE_VJP_MIN_CHUNK
+#define PBE_VJP_MIN_CHUNK 256
+#endif
+__host__ __device__ constexpr int vjp_lane_chunk(int n)
+{
+    const int c = (((n + PBE_VJP_CHUNK_DIV - 1) / PBE_VJP_CHUNK_DIV) + 63) / 64 * 64;
+    return c < PBE_VJP_MIN_CHUNK ? PBE_VJP_MIN_CHUNK : c;
+}
+static_assert(PBE_VJP_MIN_CHUNK >= 32, "vjp lane chunks must be at least 32 lags");
 // Row blocks that have chunk c (blocks 0 .. cnt-1: the lag range shrinks with b).
 __host__ __device__ constexpr int vjp_lane_chunk_blocks(int n, int c, int C)
 {

@@ -258,7 +258,10 @@ __global__ void __launch_bounds__(128) vjp_gfin_kernel(int ntile, VjpWs ws, doub
 #endif
 constexpr int kVLaneCtas = PBE_VJP_LANE_CTAS;
 constexpr int kLaneWarps = kMainThreads / 32;   // warps sharing a task's lags
-constexpr int kVLaneMaxChunks = 64;        // vjp_lane_chunks(n, C) bound (C >= n / 16)
+#ifdef PBE_VJP_UNROLL
+constexpr int kVjpUnroll = PBE_VJP_UNROLL;
+#endif
+constexpr int kVLaneMaxChunks = 64;        // vjp_lane_chunks(n, C) bound
 
 template <int K>
 __global__ void __launch_bounds__(kMainThreads, kVLaneCtas)
@@ -316,6 +319,9 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
         const int jtop = n - 1 - j;               // lo >= n - 1 <=> Ld[d] >= jtop
 
         double U0 = 0.0, U1 = 0.0, W = 0.0;
+#ifdef PBE_VJP_UNROLL
+#pragma unroll kVjpUnroll
+#endif
         for (int d = dw0; d < dw1; ++d) {
             // lane 0's row (j + d - 1) is complete: out; every row moves one lane down
             const double Wd = __shfl_down_sync(0xffffffffu, W, 1);
@@ -390,18 +396,20 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
 }
 
 // Rows of the lane path: one CTA per row block b (rows 32 b + lane). Warp g
-// adds the larger-member sums of the row blocks b' = g, g + 8, ... <= b (the
+// adds the larger-member sums of the row blocks b' = g, g + 32, ... <= b (the
 // chunk holding lag d = m - 32 b' and, for the first 32 lags of a chunk, the
-// tail of the chunk before); warp 0 adds the eight in order, the block's own
+// tail of the chunk before); warp 0 adds the 32 in order, the block's own
 // smaller-member sums chunk by chunk, the diagonal pair, the death moments,
 // and stores dL/dN_m and the block's parameter partials.
+constexpr int kVRowsWarps = 32;
+
 template <int K>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kVRowsWarps * 32)
 vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
                      const double* __restrict__ lam, double* __restrict__ gN, VjpWs ws, int n,
                      int C, double b0, double bbr, double bsh)
 {
-    __shared__ double lw[kLaneWarps][kLaneBins];
+    __shared__ double lw[kVRowsWarps][kLaneBins];
     __shared__ int base[kVLaneMaxChunks + 1];
     if (ws.mom[10] == 0.0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -419,13 +427,18 @@ vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     const size_t S = static_cast<size_t>(C) + 32;
     double acc = 0.0;
     if (m < n) {
-        for (int bp = w; bp <= b; bp += kLaneWarps) {
+        // the loads of several row blocks in flight: addresses do not depend on acc
+#pragma unroll 4
+        for (int bp = w; bp <= b; bp += kVRowsWarps) {
             const int d = m - kLaneBins * bp;
-            if (d < 1) continue;
             const int nch = (n - 1 - kLaneBins * bp + C - 1) / C;
             const int c1 = d / C, idx = d - c1 * C;
-            if (c1 >= 1 && idx < 32) acc += __ldcg(ws.llo + (base[c1 - 1] + bp) * S + C + idx);
-            if (c1 < nch) acc += __ldcg(ws.llo + (base[c1] + bp) * S + idx);
+            double v = 0.0;
+            if (d >= 1) {
+                if (c1 >= 1 && idx < 32) v = __ldcg(ws.llo + (base[c1 - 1] + bp) * S + C + idx);
+                if (c1 < nch) v += __ldcg(ws.llo + (base[c1] + bp) * S + idx);
+            }
+            acc += v;
         }
     }
     lw[w][lane] = acc;
@@ -436,7 +449,7 @@ vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (m < n) {
         double Wm = 0.0;
 #pragma unroll
-        for (int q = 0; q < kLaneWarps; ++q) Wm += lw[q][lane];
+        for (int q = 0; q < kVRowsWarps; ++q) Wm += lw[q][lane];
         const int dmax = n - 1 - kLaneBins * b;
         const int nchb = dmax >= 1 ? (dmax + C - 1) / C : 0;
         double U0 = 0.0, U1 = 0.0;
@@ -514,6 +527,9 @@ brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
     double S = 0.0, Nj = 0.0, xj = 1.0;
     bool on = false;
     double acc = 0.0;
+    const float lx0 = log2_approx(__ldg(x));
+    const float span = log2_approx(__ldg(x + n - 1)) - lx0;
+    const float inv_span = (n > 1 && span > 0.0f) ? static_cast<float>(n - 1) / span : 0.0f;
     if (j < n) {
         xj = x[j];
         Nj = N[j];
@@ -522,7 +538,7 @@ brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
         if (on) {
             for (int q = l; q < nq; q += nqp) {
                 const double v = xj * t_q[q];
-                const int lo = frag_bracket(x, n, v);
+                const int lo = frag_bracket_guess(x, n, v, lx0, inv_span);
                 double P;
                 if (lo < 0) P = lam[0];
                 else if (lo >= n - 1) P = lam[n - 1];
@@ -617,7 +633,7 @@ cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStr
     vjp_rows_kernel<K><<<(ntile + 7) / 8, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, ntile, nch,
                                                        a.beta0, a.beta_br, a.beta_sh, lane_on);
     if (lane_on)
-        vjp_lane_rows_kernel<K><<<nrb, 256, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, C, a.beta0,
+        vjp_lane_rows_kernel<K><<<nrb, kVRowsWarps * 32, 0, s>>>(a.N, a.x, a.lam, a.gN, ws, n, C, a.beta0,
                                                     a.beta_br, a.beta_sh);
     vjp_gfin_kernel<<<1, 128, 0, s>>>(ntile, ws, a.gp, 3, lane_on ? nrb : 0);
     return cudaGetLastError();
