@@ -100,6 +100,22 @@ def fp64_instr_per_launch(x) -> int:
 LANE_BINS, LANE_WARPS, LANE_MIN_CHUNK, LAG_CLIP = 32, 8, 256, 0x3fffffff
 
 
+def vjp_lane_fp64_instr(x) -> int:
+    """FP64 instructions of the lane-block aggregation VJP (Brownian + shear)
+    on a geometric grid: 7 per pair j < k (P, P Bf, P Sf, two sums of row j,
+    two FMAs into the sum of row k), 6 when the pair is clipped at x[n-1]
+    (P = lambda_{n-1}, no FMA)."""
+    n = len(x)
+    v = x[0] + x
+    L = np.searchsorted(x, v, side="right") - 1
+    L = np.where(v >= x[-1], LAG_CLIP, L)[1:]
+    d = np.arange(1, n)
+    nj = n - d                                            # rows j = 0 .. n-1-d
+    jclip = np.where(L >= LAG_CLIP, 0, np.maximum(0, n - 1 - L))
+    clipped = int(np.maximum(0, nj - jclip).sum())
+    return 7 * int(nj.sum()) - clipped
+
+
 def lane_fp64_instr_per_launch(x) -> int:
     n = len(x)
     v = x[0] + x
@@ -677,6 +693,8 @@ def summarize(sections: dict, value: float) -> dict:
         out["reference_kernels_sm103a"] = rk
     if "vjp" in sections:
         out["vjp_rhs_ratio_n16384"] = sections["vjp"]["vjp_rhs_ratio"]
+        if "roofline" in sections["vjp"]:
+            out["vjp_roofline_frac"] = sections["vjp"]["roofline"].get("frac")
     if "other_mode" in sections:
         om = sections["other_mode"]
         out["other_mode"] = {"mode": om["mode"], "evals_per_s": om["evals_per_s"]}
@@ -1097,8 +1115,19 @@ def main():
                                   "ms_per_step": round(other_ms, 5),
                                   "what": "the same step in the other accumulation mode, "
                                           "device-resident, L2 flushed"}
+        vjp_instr = vjp_lane_fp64_instr(x)
+        vjp_ach = vjp_instr / (vjp_ms * 1e-3) / 1e12
+        vjp_frac = round(vjp_ach / slots_peak, 4) if slots_peak else None
         sections["vjp"] = {"ms_per_eval": round(vjp_ms, 5),
                            "vjp_rhs_ratio": round(vjp_ms / (total_ms / args.steps), 4),
+                           "roofline": {"bound": "fp64", "kernel": "vjp_lane_kernel<5>",
+                                        "achieved": round(vjp_ach, 4),
+                                        "peak": round(slots_peak, 4) if slots_peak else None,
+                                        "unit": "T FP64 instr/s",
+                                        "frac": vjp_frac,
+                                        "fp64_instr_per_eval": vjp_instr,
+                                        "time": "the whole aggregation + breakage VJP step "
+                                                "(the pair kernel is ~93 % of it)"},
                            "what": "aggregation + breakage VJP (dL/dN and parameter gradients) "
                                    "of the same n=16384 step, device-resident, L2 flushed"}
     if n_gpus == 1 and not args.no_extras:

@@ -27,3 +27,23 @@ def test_summary_of_a_real_sections_file():
 
 def test_summary_of_no_sections():
     assert _bench().summarize({}, 1.0) == {}
+
+
+def test_vjp_instruction_model_counts_pairs_and_clips():
+    """vjp_lane_fp64_instr: 7 FP64 instructions per pair j < k, one fewer when
+    the pair's bracket j + Ld[k - j] reaches n - 1 (clipped), on a small
+    geometric grid, against a direct count over the pairs."""
+    import numpy as np
+
+    b = _bench()
+    for n, q in ((300, 16.0), (257, 4.0), (64, 1.0)):
+        x = 1e-21 * np.exp2(np.arange(n) / q)
+        v = x[0] + x
+        L = np.searchsorted(x, v, side="right") - 1
+        L = np.where(v >= x[-1], b.LAG_CLIP, L)
+        want = 0
+        for j in range(n):
+            for k in range(j + 1, n):
+                clipped = L[k - j] >= b.LAG_CLIP or j + L[k - j] >= n - 1
+                want += 6 if clipped else 7
+        assert b.vjp_lane_fp64_instr(x) == want
