@@ -161,17 +161,27 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 }
 
 // ---------------------------------------------------------------------------
-// Gather in one pass (the drop-in calls): block = 32 consecutive output bins
-// x W warps (W = min(n_quad, 16)); warp w takes the quadrature points
-// q = w, w + W, ..., lane l the bin i = i0 + l. For (i, q) the parents whose
-// fragment x_j t_q has bracket i - 1 or i form the index ranges [fa, fb) and
-// [fb, fc), fb = first_parent(i) (brackets grow with j for t_q > 0); the
-// thread walks them and forms each fragment's share from 1/dx staged in
-// shared memory. Bin 0 also takes the fragments clipped below x[0], summed
-// by each warp's lanes. Sums run in a fixed order (fragments by j, points by
-// q within a warp, warps in order): bitwise reproducible.
+// Gather in one pass (the drop-in calls): block = 32 brackets c = i0 - 1 + lane
+// x W warps (W = min(n_quad, 8)); warp w takes the quadrature points
+// q = w, w + W, ..., and the block writes the 31 bins i0 .. i0 + 30. A lane walks the parents whose
+// fragment x_j t_q has bracket c -- the index range [f(c), f(c + 1)), f(c) the
+// first parent whose fragment reaches bracket c (brackets grow with j for
+// t_q > 0), guessed from FP32 logs and confirmed by exact tests of the guess
+// and its neighbours; f(c + 1) from the next lane -- and forms each
+// fragment's two shares once:
+// the lower one for bin c, the upper one for bin c + 1 (6 FP64 instructions
+// per fragment). Bin i = i0 + lane adds its own upper shares and the next
+// lane's lower shares. Bracket -1 holds the fragments at or below x[0], all
+// of them bin 0's: sum_q fbw_q U(f_q(0)) with U(f) the sum of the parents'
+// factors u_j, j < f, from one prefix of u over block 0's threads (a walk by
+// one warp per point was the kernel's long pole: ~4000 parents per point on
+// a 512-bins-per-doubling grid); bracket n - 1
+// those at or above x[n-1], all of them bin n - 1's. Sums run in a fixed
+// order (fragments by j, points by q within a warp, warps in order): bitwise
+// reproducible.
 // ---------------------------------------------------------------------------
 constexpr int kBinWarpsMax = 8;
+constexpr int kBrkBins = 31;            // bins written per block (32 brackets)
 
 // S_j N_j with the reference's guard (S != 0, N_j > 2.2e-308), from the
 // cache `SN` when the selection needs it (Linear, PowerLaw), else inline.
@@ -253,19 +263,76 @@ __device__ __forceinline__ int first_parent_near(const double* __restrict__ x, i
     return b;
 }
 
-// Starting point for a warp: the first parent of bin ib, guessed where a
-// geometric grid through x[0] and x[n-1] would put x[ib] / t_q (FP32 logs on
-// the integer / SFU pipes, no FP64), finished exactly by first_parent_near
-// (on a geometric grid the guess is within a bin; elsewhere the gallop
-// corrects it in a logarithmic number of tests).
-__device__ __forceinline__ int first_parent(const double* __restrict__ x, int n, int ib, double tq,
-                                            float lx0, float inv_span)
+// first_parent of bin ib from a guess, testing the guess and both neighbours
+// at once (three independent loads and products): the answer when it is one
+// of them -- on a geometric grid it is -- else the gallop of
+// first_parent_near. Also returns the fragment volumes fl(x_f t_q) of the
+// answer f and, when it was formed, of f + 1.
+struct FirstParent {
+    int f;
+    bool has_v1;
+    double v, v1;
+};
+__device__ __forceinline__ FirstParent first_parent_spec(const double* __restrict__ x, int n, int ib,
+                                                         double tq, int guess)
 {
-    if (ib >= n) return n;
-    const float ly = log2_approx(__ldg(x + ib)) - __log2f(static_cast<float>(tq));
-    float gf = (ly - lx0) * inv_span;
+    FirstParent r{n, false, 0.0, 0.0};
+    if (ib >= n) return r;
+    const long long xb = dbits(__ldg(x + ib));
+    auto P = [&](double v) {                   // bracket of a fragment volume >= ib
+        const long long vb = dbits(v);
+        return ib == 0 ? (vb > xb && vb > 0) : vb >= xb;
+    };
+    const int g = guess < 0 ? 0 : (guess > n - 1 ? n - 1 : guess);
+    const double vm = __ldg(x + (g >= 1 ? g - 1 : 0)) * tq;
+    const double v0 = __ldg(x + g) * tq;
+    const double vp = __ldg(x + (g + 1 < n ? g + 1 : g)) * tq;
+    const bool pm = g >= 1 && P(vm);
+    const bool p0 = P(v0);
+    const bool pp = g + 1 >= n || P(vp);       // P(n) := true
+    if (!pm && p0) {
+        r.f = g; r.v = v0; r.v1 = vp; r.has_v1 = g + 1 < n;
+    } else if (!p0 && pp) {
+        r.f = g + 1; r.v = vp;                 // f = n when no parent reaches ib
+    } else {
+        r.f = first_parent_near(x, n, ib, tq, 0, g);
+        if (r.f < n) r.v = __ldg(x + r.f) * tq;
+    }
+    return r;
+}
+
+// Index guess of the first parent of bin ib for the point with log2(t_q) = ltq
+// (geometric grid through x[0] and x[n-1]), from lxb = log2_approx(x[ib]).
+__device__ __forceinline__ int first_parent_guess(float lxb, float ltq, float lx0, float inv_span, int n)
+{
+    float gf = (lxb - ltq - lx0) * inv_span;
     gf = fminf(fmaxf(gf, 0.0f), static_cast<float>(n));
-    return first_parent_near(x, n, ib, tq, 0, static_cast<int>(gf));
+    return static_cast<int>(gf);
+}
+
+// One (bracket, point): the parents [f0, f1), v0 the fragment volume of parent
+// f0. Adds sum u_j bw to A (the whole contribution) and, for c in [0, n-2],
+// sum u_j bw (v - x_c) to H (the upper share before the factor 1/dx_c); the
+// lower share is A - H/dx_c. c = n - 1: all of it is bin n-1's (H stays 0).
+template <int F>
+__device__ __forceinline__ void bracket_shares(const double* __restrict__ N, const double* __restrict__ x,
+                                               const double* __restrict__ SN, double v_min, int f0,
+                                               int f1, double v0, double tq, double bw, double xc,
+                                               bool mid, bool top, double& A, double& H)
+{
+    if (f0 >= f1) return;
+    if (mid) {
+        const double a0 = bin_unit<F>(N, x, SN, f0, v_min) * bw;
+        H = fma(a0, v0 - xc, H);
+        A += a0;
+        for (int j = f0 + 1; j < f1; ++j) {
+            const double a = bin_unit<F>(N, x, SN, j, v_min) * bw;
+            H = fma(a, __ldg(x + j) * tq - xc, H);
+            A += a;
+        }
+    } else if (top) {
+        for (int j = f0; j < f1; ++j) A = fma(bin_unit<F>(N, x, SN, j, v_min), bw, A);
+    }
 }
 
 template <int F>
@@ -276,87 +343,151 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
                double S0, double v_ref, double alpha, double v_min)
 {
     if ((F == 0 || F == 3) && S0 == 0.0) return;     // S = 0 everywhere: no breakage at all
-    __shared__ double s_inv[34];                      // 1/(x[b+1] - x[b]), b = i0 - 1 .. i0 + 32
     __shared__ double s_acc[kBinWarpsMax][32];
-    const int i0 = blockIdx.x * 32;
+    __shared__ int s_fmax[kBinWarpsMax];              // block 0 only: bracket -1
+    __shared__ double s_wtot[kBinWarpsMax];
+    __shared__ double s_pre[32 * kBinWarpsMax];
+    __shared__ double s_clip;
+    const int i0 = blockIdx.x * kBrkBins;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
-    for (int k = threadIdx.x; k < 34; k += blockDim.x) {
-        const int b = i0 - 1 + k;
-        s_inv[k] = (b >= 0 && b < n - 1) ? 1.0 / (__ldg(x + b + 1) - __ldg(x + b)) : 0.0;
-    }
-    __syncthreads();
     // index of a volume on the geometric grid through x[0] and x[n-1] (guesses only)
     const float lx0 = log2_approx(__ldg(x));
     const float span = log2_approx(__ldg(x + n - 1)) - lx0;
     const float inv_span = (n > 1 && span > 0.0f) ? static_cast<float>(n - 1) / span : 0.0f;
 
-    const int i = i0 + lane;
-    const bool live = i < n;
-    const double xi = live ? __ldg(x + i) : 0.0;
-    const double xlo = (live && i >= 1) ? __ldg(x + i - 1) : 0.0;     // x[i-1]
-    const double xhi = (live && i <= n - 2) ? __ldg(x + i + 1) : 0.0;  // x[i+1]
-    const double inv_lo = s_inv[lane];        // 1/(x[i] - x[i-1]): bracket i-1
-    const double inv_hi = s_inv[lane + 1];    // 1/(x[i+1] - x[i]): bracket i
-    // selections with a per-bin S of S0 or 0 (Constant, Threshold): the share
-    // factor S0 bw / dx is per lane and quadrature point, the parent adds N_j
+    const int c = i0 - 1 + lane;               // this lane's bracket
+    const bool mid = c >= 0 && c <= n - 2;     // x[c] <= v < x[c+1]
+    const bool top = c == n - 1;               // v >= x[n-1]: all to bin n-1
+    const int ib = c < 0 ? 0 : (c < n ? c : n - 1);
+    const double xc = __ldg(x + ib);
+    const double xc1 = mid ? __ldg(x + c + 1) : 0.0;
+    const double inv = mid ? 1.0 / (xc1 - xc) : 0.0;
+    const float lxc = log2_approx(xc);
+    // lane 31 also needs f(i0 + 31)
+    const int ibt = min(i0 + 31, n - 1);
+    const float lxt = log2_approx(__ldg(x + ibt));
+    // selections with a per-bin S of S0 or 0 (Constant, Threshold): the parent
+    // adds N_j, S0 multiplies the lane's sums once at the end, as 1/dx_c does
     constexpr bool kS0 = (F == 0 || F == 3);
-    double acc = 0.0;
+    double A = 0.0, H = 0.0;                   // this warp's points, in q order
+    const int cb = max(c, 0);                  // bracket -1 takes f(0)
+    const long long xb = dbits(xc);            // threshold of bracket cb (c < n)
     for (int q = w; q < nq; q += W) {
         const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q);
-        const double fbw = kS0 ? S0 * bw : bw;
-        const double k_lo = fbw * inv_lo, k_hi = fbw * inv_hi;
-        // fb of bins i0 - 1 + lane and, for lanes 0 and 1, of i0 + 31 and i0 + 32:
-        // the warp's bin ib0 by a uniform bisection, the others near ib0's
-        // parent plus their bin offset
-        const int ib0 = max(i0 - 1, 0);
-        const int g0 = first_parent(x, n, ib0, tq, lx0, inv_span);
-        const int ibl = max(i0 - 1 + lane, 0);
-        const int f0 = first_parent_near(x, n, ibl, tq, g0, g0 + (ibl - ib0));
-        int f1 = 0;
-        if (lane < 2) f1 = first_parent_near(x, n, i0 + 31 + lane, tq, g0, g0 + (i0 + 31 + lane - ib0));
+        const float ltq = __log2f(static_cast<float>(tq));
+        // f(c) from a guess g: the tests of g - 1, g, g + 1 need three fragment
+        // volumes; on a geometric grid the neighbour lanes' guesses are g - 1
+        // and g + 1, so one product per lane plus one more (the ends of the
+        // warp, misaligned guesses) covers them
+        int g = first_parent_guess(lxc, ltq, lx0, inv_span, n);
+        g = g > n - 1 ? n - 1 : g;
+        const double v0 = __ldg(x + g) * tq;
+        const int gl = __shfl_up_sync(0xffffffffu, g, 1);
+        const double vl = __shfl_up_sync(0xffffffffu, v0, 1);
+        const int gr = __shfl_down_sync(0xffffffffu, g, 1);
+        const double vr = __shfl_down_sync(0xffffffffu, v0, 1);
+        const bool have_m = lane > 0 && gl == g - 1;
+        const bool have_p = lane < 31 && gr == g + 1;
+        const int e = !have_m ? g - 1 : g + 1;
+        const double ve = __ldg(x + min(max(e, 0), n - 1)) * tq;
+        double vm = have_m ? vl : ve;
+        double vp = have_p ? vr : ve;
+        if (!have_m && !have_p && g + 1 < n) vp = __ldg(x + g + 1) * tq;   // rare
+        int f = n;
+        bool has_v1 = false;
+        double v = 0.0, v1 = 0.0;
+        if (c < n) {
+            auto P = [&](double vv) {            // fragment bracket >= cb
+                const long long vb = dbits(vv);
+                return cb == 0 ? (vb > xb && vb > 0) : vb >= xb;
+            };
+            const bool pm = g >= 1 && P(vm);
+            const bool p0 = P(v0);
+            const bool pp = g + 1 >= n || P(vp);  // P(n) := true
+            if (!pm && p0) {
+                f = g; v = v0; v1 = vp; has_v1 = g + 1 < n;
+            } else if (!p0 && pp) {
+                f = g + 1; v = vp;
+            } else {
+                f = first_parent_near(x, n, cb, tq, 0, g);
+                if (f < n) v = __ldg(x + f) * tq;
+            }
+        }
+        // lane 31 also needs f(c + 1): from its own volumes when they decide it
+        int ft = n;
+        if (lane == 31 && c + 1 < n && f < n) {
+            const long long xb1 = dbits(__ldg(x + c + 1));
+            if (dbits(v) >= xb1) ft = f;
+            else if (has_v1 && dbits(v1) >= xb1) ft = f + 1;
+            else ft = first_parent_near(x, n, c + 1, tq, f, f + 2);
+        }
         // every lane runs every shuffle (full mask), then selects
-        const int fa = (i0 - 1 + lane < 0) ? 0 : f0;            // first parent with bracket >= i-1
-        const int up1 = __shfl_down_sync(0xffffffffu, f0, 1);
-        const int up2 = __shfl_down_sync(0xffffffffu, f0, 2);
-        const int e30 = __shfl_sync(0xffffffffu, f1, 0);
-        const int e31 = __shfl_sync(0xffffffffu, f1, 1);
-        const int fb = (lane < 31) ? up1 : e30;                 // bracket >= i
-        const int fc = (lane < 30) ? up2 : (lane == 30 ? e30 : e31);   // bracket >= i+1
-        double a = 0.0;
-        if (live) {
-            if (i >= 1) {                                       // bracket i-1: the upper share
-                for (int j = fa; j < fb; ++j) {
-                    const double u = bin_unit<F>(N, x, SN, j, v_min);
-                    const double v = __ldg(x + j) * tq;
-                    a = fma(u * k_lo, v - xlo, a);
-                }
-            }
-            for (int j = fb; j < fc; ++j) {                     // bracket i: the lower share
-                const double u = bin_unit<F>(N, x, SN, j, v_min);
-                if (i <= n - 2) {
-                    const double v = __ldg(x + j) * tq;
-                    a = fma(u * k_hi, xhi - v, a);
-                } else {
-                    a = fma(u, fbw, a);                         // clipped at x[n-1]: all of it
-                }
-            }
-        }
-        if (i0 == 0) {
-            // bin 0 also takes the fragments at or below x[0], the parents
-            // [0, fb(0)): lanes stride over them, a fixed butterfly adds
-            const int fz = __shfl_sync(0xffffffffu, f0, 1);      // lane 1 computed fb(0)
-            double cz = 0.0;
-            for (int j = lane; j < fz; j += 32) cz = fma(bin_unit<F>(N, x, SN, j, v_min), fbw, cz);
-            cz = warp_sum(cz);
-            if (lane == 0) a += cz;
-        }
-        acc += a;
+        const int up = __shfl_down_sync(0xffffffffu, f, 1);
+        const int fn = (lane < 31) ? up : ft;                   // f(c + 1)
+        bracket_shares<F>(N, x, SN, v_min, f, fn, v, tq, bw, xc, mid, top, A, H);
     }
+    // bin c: the lower shares A - H/dx_c; bin c + 1: the upper shares H/dx_c
+    const double s0 = kS0 ? S0 : 1.0;
+    const double hi = mid ? H * inv * s0 : 0.0;
+    const double lo = A * s0 - hi;
+    const double lo_next = __shfl_down_sync(0xffffffffu, lo, 1);
+    const double acc = hi + lo_next;                           // bin i0 + lane (lane < 31)
     s_acc[w][lane] = acc;
     __syncthreads();
-    if (w == 0 && live) {
+    if (i0 == 0) {
+        // bracket -1, all of it bin 0's: sum_q fbw_q U(f_q(0)), U(f) = sum_{j < f} u_j
+        // (the parents whose fragment is at or below x[0]), from one block-wide
+        // prefix of u over [0, max_q f_q(0)): contiguous chunks per thread, a
+        // warp scan by a fixed shuffle pattern, warp totals in order
+        const int tid = threadIdx.x, T = blockDim.x;
+        auto fz_of = [&](int q) {
+            const double tq = __ldg(t_q + q);
+            return first_parent_spec(x, n, 0, tq, first_parent_guess(lx0, __log2f(static_cast<float>(tq)),
+                                                                      lx0, inv_span, n)).f;
+        };
+        int fm = 0;
+        for (int q = tid; q < nq; q += T) fm = max(fm, fz_of(q));
+        for (int o = 16; o > 0; o >>= 1) fm = max(fm, __shfl_xor_sync(0xffffffffu, fm, o));
+        if (lane == 0) s_fmax[w] = fm;
+        __syncthreads();
+        int fmax = 0;
+        for (int k = 0; k < W; ++k) fmax = max(fmax, s_fmax[k]);
+        const int chunk = (fmax + T - 1) / T;
+        const int j0 = min(fmax, tid * chunk), j1 = min(fmax, j0 + chunk);
+        double cs = 0.0;
+        for (int j = j0; j < j1; ++j) cs += bin_unit<F>(N, x, SN, j, v_min);
+        double sc = cs;                                        // inclusive scan in the warp
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xffffffffu, sc, o);
+            if (lane >= o) sc += t;
+        }
+        double ex = __shfl_up_sync(0xffffffffu, sc, 1);        // exclusive
+        if (lane == 0) ex = 0.0;
+        if (lane == 31) s_wtot[w] = sc;
+        __syncthreads();
+        double wbase = 0.0;
+        for (int k = 0; k < w; ++k) wbase += s_wtot[k];
+        s_pre[tid] = wbase + ex;                               // sum of u_j, j < j0
+        __syncthreads();
+        double term = 0.0;
+        if (chunk > 0) {
+            for (int q = tid; q < nq; q += T) {
+                const int f = fz_of(q);
+                const int t = min(f / chunk, T - 1);
+                double pre = s_pre[t];
+                for (int j = t * chunk; j < f; ++j) pre += bin_unit<F>(N, x, SN, j, v_min);
+                term = fma(__ldg(bw_q + q), pre, term);
+            }
+        }
+        const double clip = block_sum(term, s_wtot) * (kS0 ? S0 : 1.0);
+        if (tid == 0) s_clip = clip;
+        __syncthreads();
+    }
+    const int i = i0 + lane;
+    if (w == 0 && lane < kBrkBins && i < n) {
         double t = 0.0;
-        for (int k = 0; k < W; ++k) t += s_acc[k][lane];
+        for (int kq = 0; kq < W; ++kq) t += s_acc[kq][lane];
+        if (i == 0) t += s_clip;
         double sn_i;
         if constexpr (F == 1 || F == 2) sn_i = SN[i];
         else sn_i = bin_sn<F>(N, x, SN, i, S0, v_min);
@@ -428,7 +559,7 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
                 brk_sn_kernel<F><<<(a.n + 255) / 256, 256, 0, s>>>(a.N, a.x, a.n, ws.SN, a.S0,
                                                                   a.v_ref, a.alpha, a.v_min);
             const int W = a.n_quad < kBinWarpsMax ? a.n_quad : kBinWarpsMax;
-            brk_bin_kernel<F><<<(a.n + 31) / 32, 32 * W, 0, s>>>(
+            brk_bin_kernel<F><<<(a.n + kBrkBins - 1) / kBrkBins, 32 * W, 0, s>>>(
                 a.N, a.x, a.t_q, a.bw_q, a.rhs, a.n, a.n_quad, ws.SN, a.S0, a.v_ref, a.alpha,
                 a.v_min);
             return cudaGetLastError();
