@@ -161,24 +161,20 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 }
 
 // ---------------------------------------------------------------------------
-// Gather in one pass (the drop-in calls): block = 32 brackets c = i0 - 1 + lane
-// x W warps (W = min(n_quad, 8)); warp w takes the quadrature points
-// q = w, w + W, ..., and the block writes the 31 bins i0 .. i0 + 30. A lane walks the parents whose
-// fragment x_j t_q has bracket c -- the index range [f(c), f(c + 1)), f(c) the
-// first parent whose fragment reaches bracket c (brackets grow with j for
-// t_q > 0), guessed from FP32 logs and confirmed by exact tests of the guess
-// and its neighbours; f(c + 1) from the next lane -- and forms each
-// fragment's two shares once:
-// the lower one for bin c, the upper one for bin c + 1 (6 FP64 instructions
-// per fragment). Bin i = i0 + lane adds its own upper shares and the next
-// lane's lower shares. Bracket -1 holds the fragments at or below x[0], all
-// of them bin 0's: sum_q fbw_q U(f_q(0)) with U(f) the sum of the parents'
-// factors u_j, j < f, from one prefix of u over block 0's threads (a walk by
-// one warp per point was the kernel's long pole: ~4000 parents per point on
-// a 512-bins-per-doubling grid); bracket n - 1
-// those at or above x[n-1], all of them bin n - 1's. Sums run in a fixed
-// order (fragments by j, points by q within a warp, warps in order): bitwise
-// reproducible.
+// Gather in one pass (the drop-in calls): block b >= 1 = 32 brackets
+// c = i0 - 1 + lane, i0 = 1 + 31 (b - 1), x W warps (W = min(n_quad, 8)); warp
+// w takes the quadrature points q = w, w + W, ..., and the block writes the 31
+// bins i0 .. i0 + 30. A lane walks the parents whose fragment x_j t_q has
+// bracket c -- the index range [f(c), f(c + 1)), f(c) the first parent whose
+// fragment reaches bracket c (brackets grow with j for t_q > 0), guessed from
+// FP32 logs and confirmed by exact tests of the guess and its neighbours; f(c + 1)
+// from the next lane -- and forms each fragment's two shares once: the lower
+// one for bin c, the upper one for bin c + 1 (4 FP64 instructions per
+// fragment and 2 per test). Bin i = i0 + lane adds its own upper shares and
+// the next lane's lower shares; bracket n - 1 (fragments at or above x[n-1])
+// is all bin n-1's. Block 0 writes bin 0 alone (brk_bin0). Sums run in a
+// fixed order (fragments by j, points by q within a warp, warps in order):
+// bitwise reproducible.
 // ---------------------------------------------------------------------------
 constexpr int kBinWarpsMax = 8;
 constexpr int kBrkBins = 31;            // bins written per block (32 brackets)
@@ -335,6 +331,91 @@ __device__ __forceinline__ void bracket_shares(const double* __restrict__ N, con
     }
 }
 
+// Block 0: bin 0 alone -- the fragments at or below x[0] (bracket -1, all of
+// them bin 0's) and the lower shares of bracket 0 (or, when n = 1, all of
+// bracket 0). Thread q takes point q (q = tid, tid + T, ...): f_q(0), f_q(1)
+// and bracket 0's fragments; the fragments of bracket -1 are the parents
+// j < f_q(0), summed as bw_q U(f_q(0)) with U(f) = sum_{j < f} u_j from one
+// block-wide prefix of u over [0, max_q f_q(0)) (contiguous chunks per
+// thread, a warp scan by a fixed shuffle pattern, warp totals in order). A
+// warp walking those parents point by point was the kernel's long pole
+// (~4000 parents per point on a 512-bins-per-doubling grid).
+template <int F>
+__device__ __forceinline__ void brk_bin0(const double* __restrict__ N, const double* __restrict__ x,
+                                         const double* __restrict__ t_q, const double* __restrict__ bw_q,
+                                         double* __restrict__ rhs, int n, int nq,
+                                         const double* __restrict__ SN, double S0, double v_min,
+                                         float lx0, float inv_span)
+{
+    __shared__ int s_fmax[kBinWarpsMax];
+    __shared__ double s_wtot[kBinWarpsMax];
+    __shared__ double s_pre[32 * kBinWarpsMax];
+    constexpr bool kS0 = (F == 0 || F == 3);
+    const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, w = tid >> 5, W = T >> 5;
+    const bool mid0 = n >= 2;                  // bracket 0 is [x0, x1); else all of it is bin 0's
+    const double x1 = mid0 ? __ldg(x + 1) : 0.0;
+    const double inv0 = mid0 ? 1.0 / (x1 - __ldg(x)) : 0.0;
+    const float lx1 = mid0 ? log2_approx(x1) : 0.0f;
+    auto f0_of = [&](double tq, float ltq) {
+        return first_parent_spec(x, n, 0, tq, first_parent_guess(lx0, ltq, lx0, inv_span, n)).f;
+    };
+    int fm = 0;
+    double term = 0.0;
+    for (int q = tid; q < nq; q += T) {
+        const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q);
+        const float ltq = __log2f(static_cast<float>(tq));
+        const int f0 = f0_of(tq, ltq);
+        const int f1 = mid0 ? first_parent_spec(x, n, 1, tq, first_parent_guess(lx1, ltq, lx0, inv_span, n)).f
+                            : n;
+        fm = max(fm, f0);
+        double lo = 0.0;
+        for (int j = f0; j < f1; ++j) {
+            const double u = bin_unit<F>(N, x, SN, j, v_min);
+            lo = mid0 ? fma(u, (x1 - __ldg(x + j) * tq) * inv0, lo) : lo + u;
+        }
+        term = fma(bw, lo, term);
+    }
+    for (int o = 16; o > 0; o >>= 1) fm = max(fm, __shfl_xor_sync(0xffffffffu, fm, o));
+    if (lane == 0) s_fmax[w] = fm;
+    __syncthreads();
+    int fmax = 0;
+    for (int k = 0; k < W; ++k) fmax = max(fmax, s_fmax[k]);
+    const int chunk = (fmax + T - 1) / T;
+    const int j0 = min(fmax, tid * chunk), j1 = min(fmax, j0 + chunk);
+    double cs = 0.0;
+    for (int j = j0; j < j1; ++j) cs += bin_unit<F>(N, x, SN, j, v_min);
+    double sc = cs;                                            // inclusive scan in the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, sc, o);
+        if (lane >= o) sc += t;
+    }
+    double ex = __shfl_up_sync(0xffffffffu, sc, 1);            // exclusive
+    if (lane == 0) ex = 0.0;
+    if (lane == 31) s_wtot[w] = sc;
+    __syncthreads();
+    double wbase = 0.0;
+    for (int k = 0; k < w; ++k) wbase += s_wtot[k];
+    s_pre[tid] = wbase + ex;                                   // sum of u_j, j < tid * chunk
+    __syncthreads();
+    if (chunk > 0) {
+        for (int q = tid; q < nq; q += T) {
+            const double tq = __ldg(t_q + q);
+            const int f = f0_of(tq, __log2f(static_cast<float>(tq)));
+            const int t = min(f / chunk, T - 1);
+            double pre = s_pre[t];
+            for (int j = t * chunk; j < f; ++j) pre += bin_unit<F>(N, x, SN, j, v_min);
+            term = fma(__ldg(bw_q + q), pre, term);
+        }
+    }
+    const double total = block_sum(term, s_wtot) * (kS0 ? S0 : 1.0);
+    if (tid == 0) {
+        double sn0;
+        if constexpr (F == 1 || F == 2) sn0 = SN[0];
+        else sn0 = bin_sn<F>(N, x, SN, 0, S0, v_min);
+        rhs[0] = (rhs[0] - sn0) + total;
+    }
+}
+
 template <int F>
 __global__ void __launch_bounds__(32 * kBinWarpsMax)
 brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
@@ -344,21 +425,21 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
 {
     if ((F == 0 || F == 3) && S0 == 0.0) return;     // S = 0 everywhere: no breakage at all
     __shared__ double s_acc[kBinWarpsMax][32];
-    __shared__ int s_fmax[kBinWarpsMax];              // block 0 only: bracket -1
-    __shared__ double s_wtot[kBinWarpsMax];
-    __shared__ double s_pre[32 * kBinWarpsMax];
-    __shared__ double s_clip;
-    const int i0 = blockIdx.x * kBrkBins;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
     // index of a volume on the geometric grid through x[0] and x[n-1] (guesses only)
     const float lx0 = log2_approx(__ldg(x));
     const float span = log2_approx(__ldg(x + n - 1)) - lx0;
     const float inv_span = (n > 1 && span > 0.0f) ? static_cast<float>(n - 1) / span : 0.0f;
+    if (blockIdx.x == 0) {
+        brk_bin0<F>(N, x, t_q, bw_q, rhs, n, nq, SN, S0, v_min, lx0, inv_span);
+        return;
+    }
+    const int i0 = 1 + (blockIdx.x - 1) * kBrkBins;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
 
-    const int c = i0 - 1 + lane;               // this lane's bracket
-    const bool mid = c >= 0 && c <= n - 2;     // x[c] <= v < x[c+1]
+    const int c = i0 - 1 + lane;               // this lane's bracket (>= 0)
+    const bool mid = c <= n - 2;               // x[c] <= v < x[c+1]
     const bool top = c == n - 1;               // v >= x[n-1]: all to bin n-1
-    const int ib = c < 0 ? 0 : (c < n ? c : n - 1);
+    const int ib = c < n ? c : n - 1;
     const double xc = __ldg(x + ib);
     const double xc1 = mid ? __ldg(x + c + 1) : 0.0;
     const double inv = mid ? 1.0 / (xc1 - xc) : 0.0;
@@ -370,8 +451,8 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
     // adds N_j, S0 multiplies the lane's sums once at the end, as 1/dx_c does
     constexpr bool kS0 = (F == 0 || F == 3);
     double A = 0.0, H = 0.0;                   // this warp's points, in q order
-    const int cb = max(c, 0);                  // bracket -1 takes f(0)
-    const long long xb = dbits(xc);            // threshold of bracket cb (c < n)
+    const int cb = c;
+    const long long xb = dbits(xc);            // threshold of bracket c (c < n)
     for (int q = w; q < nq; q += W) {
         const double tq = __ldg(t_q + q), bw = __ldg(bw_q + q);
         const float ltq = __log2f(static_cast<float>(tq));
@@ -434,60 +515,10 @@ brk_bin_kernel(const double* __restrict__ N, const double* __restrict__ x,
     const double acc = hi + lo_next;                           // bin i0 + lane (lane < 31)
     s_acc[w][lane] = acc;
     __syncthreads();
-    if (i0 == 0) {
-        // bracket -1, all of it bin 0's: sum_q fbw_q U(f_q(0)), U(f) = sum_{j < f} u_j
-        // (the parents whose fragment is at or below x[0]), from one block-wide
-        // prefix of u over [0, max_q f_q(0)): contiguous chunks per thread, a
-        // warp scan by a fixed shuffle pattern, warp totals in order
-        const int tid = threadIdx.x, T = blockDim.x;
-        auto fz_of = [&](int q) {
-            const double tq = __ldg(t_q + q);
-            return first_parent_spec(x, n, 0, tq, first_parent_guess(lx0, __log2f(static_cast<float>(tq)),
-                                                                      lx0, inv_span, n)).f;
-        };
-        int fm = 0;
-        for (int q = tid; q < nq; q += T) fm = max(fm, fz_of(q));
-        for (int o = 16; o > 0; o >>= 1) fm = max(fm, __shfl_xor_sync(0xffffffffu, fm, o));
-        if (lane == 0) s_fmax[w] = fm;
-        __syncthreads();
-        int fmax = 0;
-        for (int k = 0; k < W; ++k) fmax = max(fmax, s_fmax[k]);
-        const int chunk = (fmax + T - 1) / T;
-        const int j0 = min(fmax, tid * chunk), j1 = min(fmax, j0 + chunk);
-        double cs = 0.0;
-        for (int j = j0; j < j1; ++j) cs += bin_unit<F>(N, x, SN, j, v_min);
-        double sc = cs;                                        // inclusive scan in the warp
-        for (int o = 1; o < 32; o <<= 1) {
-            const double t = __shfl_up_sync(0xffffffffu, sc, o);
-            if (lane >= o) sc += t;
-        }
-        double ex = __shfl_up_sync(0xffffffffu, sc, 1);        // exclusive
-        if (lane == 0) ex = 0.0;
-        if (lane == 31) s_wtot[w] = sc;
-        __syncthreads();
-        double wbase = 0.0;
-        for (int k = 0; k < w; ++k) wbase += s_wtot[k];
-        s_pre[tid] = wbase + ex;                               // sum of u_j, j < j0
-        __syncthreads();
-        double term = 0.0;
-        if (chunk > 0) {
-            for (int q = tid; q < nq; q += T) {
-                const int f = fz_of(q);
-                const int t = min(f / chunk, T - 1);
-                double pre = s_pre[t];
-                for (int j = t * chunk; j < f; ++j) pre += bin_unit<F>(N, x, SN, j, v_min);
-                term = fma(__ldg(bw_q + q), pre, term);
-            }
-        }
-        const double clip = block_sum(term, s_wtot) * (kS0 ? S0 : 1.0);
-        if (tid == 0) s_clip = clip;
-        __syncthreads();
-    }
     const int i = i0 + lane;
     if (w == 0 && lane < kBrkBins && i < n) {
         double t = 0.0;
         for (int kq = 0; kq < W; ++kq) t += s_acc[kq][lane];
-        if (i == 0) t += s_clip;
         double sn_i;
         if constexpr (F == 1 || F == 2) sn_i = SN[i];
         else sn_i = bin_sn<F>(N, x, SN, i, S0, v_min);
@@ -559,7 +590,7 @@ cudaError_t launch_f(const BrkArgs& a, bool scatter, void* ws_base, cudaStream_t
                 brk_sn_kernel<F><<<(a.n + 255) / 256, 256, 0, s>>>(a.N, a.x, a.n, ws.SN, a.S0,
                                                                   a.v_ref, a.alpha, a.v_min);
             const int W = a.n_quad < kBinWarpsMax ? a.n_quad : kBinWarpsMax;
-            brk_bin_kernel<F><<<(a.n + kBrkBins - 1) / kBrkBins, 32 * W, 0, s>>>(
+            brk_bin_kernel<F><<<1 + (a.n - 1 + kBrkBins - 1) / kBrkBins, 32 * W, 0, s>>>(
                 a.N, a.x, a.t_q, a.bw_q, a.rhs, a.n, a.n_quad, ws.SN, a.S0, a.v_ref, a.alpha,
                 a.v_min);
             return cudaGetLastError();
