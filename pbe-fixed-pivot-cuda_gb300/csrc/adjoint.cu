@@ -176,13 +176,16 @@ cudaError_t vjp(pbe_rk4_tape* t, int m, const double* Yq, double* g_agg, double*
         const pbe_agg_params_t& p = t->agg[m];
         AggVjpArgs a{Yq, t->x, t->a, t->mu, g_agg + 3 * m, t->n, t->kernel, p.beta0, p.beta_br,
                      p.beta_sh};
-        e = agg_vjp_launch(a, t->vjp_ws, t->num_sms, s);
+        e = agg_vjp_stage_launch(a, t->vjp_ws, t->num_sms, s);
     }
     if (e == cudaSuccess && t->selection >= 0) {
         const pbe_brk_params_t& p = t->brk[m];
         BrkVjpArgs b{Yq, t->x, t->t_q, t->bw_q, t->a, t->mu, g_brk + 4 * m, t->n, t->nq,
                      t->selection, p.S0, p.v_ref, p.alpha, p.v_min};
-        e = brk_vjp_launch(b, t->vjp_ws, s);
+        // the set's breakage tables (written by tables()): S per bin, fragment brackets
+        BrkWs bw;
+        brk_ws_layout(t->n, t->nq, static_cast<char*>(t->brk_ws[m]), &bw);
+        e = brk_vjp_launch(b, t->vjp_ws, s, bw.Ssel, bw.lo);
     }
     return e;
 }
@@ -209,6 +212,13 @@ cudaError_t enqueue_backward(pbe_rk4_tape* t, const double* lamT, double* gN0, d
     double* lam = t->lam;
     double* lsum = t->lsum;
     cudaError_t e = tables(t, t->ckpt, s);
+    if (e == cudaSuccess && t->kernel >= 0) {
+        // the VJP's grid-only tables (they depend on the pivots alone)
+        const pbe_agg_params_t& p = t->agg[0];
+        AggVjpArgs a{t->ckpt, t->x, lam, t->mu, g_agg, t->n, t->kernel, p.beta0, p.beta_br,
+                     p.beta_sh};
+        e = agg_vjp_tables_launch(a, t->vjp_ws, t->num_sms, s);
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(lam, lamT, sizeof(double) * un, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess && t->kernel >= 0)

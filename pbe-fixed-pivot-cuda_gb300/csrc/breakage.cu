@@ -162,7 +162,7 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 
 // ---------------------------------------------------------------------------
 // Gather in one pass (the drop-in calls): block b >= 1 = 32 brackets
-// c = i0 - 1 + lane, i0 = 1 + 31 (b - 1), x W warps (W = min(n_quad, 8)); warp
+// c = i0 - 1 + lane, i0 = 1 + 31 (b - 1), x W warps (W = min(n_quad, 4)); warp
 // w takes the quadrature points q = w, w + W, ..., and the block writes the 31
 // bins i0 .. i0 + 30. A lane walks the parents whose fragment x_j t_q has
 // bracket c -- the index range [f(c), f(c + 1)), f(c) the first parent whose
@@ -176,7 +176,7 @@ brk_gather_kernel(double* __restrict__ rhs, int n, int nq, BrkWs ws)
 // fixed order (fragments by j, points by q within a warp, warps in order):
 // bitwise reproducible.
 // ---------------------------------------------------------------------------
-constexpr int kBinWarpsMax = 8;
+constexpr int kBinWarpsMax = 4;
 constexpr int kBrkBins = 31;            // bins written per block (32 brackets)
 
 // S_j N_j with the reference's guard (S != 0, N_j > 2.2e-308), from the

@@ -499,7 +499,18 @@ struct BrkVjpArgs {
     int n; int n_quad; int selection; double S0, v_ref, alpha, v_min;
 };
 cudaError_t agg_vjp_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s);
-cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s);
+// For callers that keep a VJP workspace per set of pivots (the RK4 tape):
+// agg_vjp_tables_launch writes the grid-only tables (cube roots, lag tables,
+// bracket offsets, geometric flag); agg_vjp_stage_launch then runs the VJP for
+// any N and lambda on that workspace, with the result of agg_vjp_launch.
+cudaError_t agg_vjp_tables_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s);
+cudaError_t agg_vjp_stage_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s);
+// Ssel / lo_tab (nullable): the selection function per bin and the fragment
+// brackets [q n + j] of a breakage table workspace (brk_tables_launch) for the
+// same pivots, quadrature and parameters; the kernel then skips their
+// computation (same values).
+cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s,
+                           const double* Ssel = nullptr, const int* lo_tab = nullptr);
 
 // ---- profiling hook ----------------------------------------------------------
 // When both are non-null the aggregation launcher records g_prof_start right

@@ -52,7 +52,14 @@ constexpr int VW = kVW;                 // rows per task
 // prep: per-bin values, lag factors (no beta, no diagonal 1/2), moments of N
 // and lambda*N, geometric deviation. Moment slots per block (stride 16):
 // 0..4 sum N{1/a, 1, a, a^2, x}, 5..9 the same of lambda*N, 10 max dev.
+// Modes: kVjpFull everything; kVjpTables the grid-only part (cube roots, lag
+// tables, bracket offsets, deviation) for callers that keep the workspace for
+// one set of pivots (the RK4 tape); kVjpStage the N- and lambda-dependent
+// part (x N, D, moments) on such a workspace, with kVjpFull's arithmetic.
 // -------------------------------------------------------------------------
+enum { kVjpFull = 0, kVjpTables = 1, kVjpStage = 2 };
+
+template <int MODE>
 __global__ void __launch_bounds__(kPrepThreads)
 vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 const double* __restrict__ lam, int n, VjpWs ws)
@@ -61,59 +68,78 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
     __shared__ double ax0_s;
     __shared__ GeoFit fit_s;
     const int i = blockIdx.x * kPrepThreads + threadIdx.x;
+    if constexpr (MODE != kVjpStage) {
+        if (threadIdx.x == 0) {
+            ax0_s = cbrt(x[0]);
+            fit_s = geo_fit(x[0], x[n - 1], n);
+        }
+        __syncthreads();
+    }
     double m[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) m[q] = 0.0;
-    if (threadIdx.x == 0) {
-        ax0_s = cbrt(x[0]);
-        fit_s = geo_fit(x[0], x[n - 1], n);
-    }
-    __syncthreads();
     double dev = 0.0;
     if (i < n) {
-        const double xi = x[i], Ni = N[i], li = lam[i];
-        const double ai = cbrt(xi), iai = 1.0 / ai;
-        ws.h[i] = xi * Ni;
-        ws.a[i] = ai;
-        ws.ia[i] = iai;
-        ws.D[i] = (i < n - 1) ? (lam[i + 1] - li) / (x[i + 1] - xi) : 0.0;
-        const double w[5] = {iai, 1.0, ai, ai * ai, xi};
-#pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            m[q] = w[q] * Ni;
-            m[5 + q] = w[q] * (li * Ni);
+        const double xi = x[i];
+        double ai, iai;
+        if constexpr (MODE == kVjpStage) {
+            ai = ws.a[i];
+            iai = ws.ia[i];
+        } else {
+            ai = cbrt(xi);
+            iai = 1.0 / ai;
+            ws.a[i] = ai;
+            ws.ia[i] = iai;
+            const double x0 = x[0];
+            const double rho = ai / ax0_s;
+            ws.Bf[i] = rho + 1.0 / rho + 2.0;
+            const double s = 1.0 + rho;
+            ws.Sf[i] = (s * s) * s;
+            ws.Sl[i] = (s * s) * s * (x0 / xi);
+            const double v = x0 + xi;
+            ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
+            if (n >= 2) {
+                dev = geo_dev(fit_s, xi, i);
+                if (!(dev == dev)) dev = 1.0;
+            }
         }
-        const double x0 = x[0];
-        const double rho = ai / ax0_s;
-        ws.Bf[i] = rho + 1.0 / rho + 2.0;
-        const double s = 1.0 + rho;
-        ws.Sf[i] = (s * s) * s;
-        ws.Sl[i] = (s * s) * s * (x0 / xi);
-        const double v = x0 + xi;
-        ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
-        if (n >= 2) {
-            dev = geo_dev(fit_s, xi, i);
-            if (!(dev == dev)) dev = 1.0;
+        if constexpr (MODE != kVjpTables) {
+            const double Ni = N[i], li = lam[i];
+            ws.h[i] = xi * Ni;
+            ws.D[i] = (i < n - 1) ? (lam[i + 1] - li) / (x[i + 1] - xi) : 0.0;
+            const double w[5] = {iai, 1.0, ai, ai * ai, xi};
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                m[q] = w[q] * Ni;
+                m[5 + q] = w[q] * (li * Ni);
+            }
         }
     }
+    if constexpr (MODE != kVjpTables) {
 #pragma unroll
-    for (int q = 0; q < 10; ++q) {
-        const double s = block_sum(m[q], sh);
-        if (threadIdx.x == 0) ws.mom_part[blockIdx.x * 16 + q] = s;
+        for (int q = 0; q < 10; ++q) {
+            const double s = block_sum(m[q], sh);
+            if (threadIdx.x == 0) ws.mom_part[blockIdx.x * 16 + q] = s;
+        }
     }
-    dev = warp_max(dev);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double mx = 0.0;
-        for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
-        ws.mom_part[blockIdx.x * 16 + 10] = mx;
+    if constexpr (MODE != kVjpStage) {
+        dev = warp_max(dev);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = dev;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double mx = 0.0;
+            for (int w = 0; w < kPrepThreads / 32; ++w) mx = fmax(mx, sh[w]);
+            ws.mom_part[blockIdx.x * 16 + 10] = mx;
+        }
     }
 }
 
-// One block: the eleven reductions over the prep blocks' partials, one per
-// warp and round (lanes stride over the blocks, fixed butterflies).
+// One block: the reductions over the prep blocks' partials, one per warp and
+// round (lanes stride over the blocks, fixed butterflies): the ten moments
+// (kVjpFull, kVjpStage) and the geometric flag (kVjpFull, kVjpTables); resets
+// the task counters (kVjpFull, kVjpStage).
+template <int MODE>
 __global__ void __launch_bounds__(256)
 vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
 {
@@ -123,10 +149,12 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
     for (int r = wq; r < 11; r += 8) {
         double t = 0.0;
         if (r < 10) {
+            if (MODE == kVjpTables) continue;
             for (int b = lq; b < nb; b += 32) t += ws.mom_part[b * 16 + r];
             t = warp_sum(t);
             if (lq == 0) ws.mom[r] = t;
         } else {
+            if (MODE == kVjpStage) continue;
             for (int b = lq; b < nb; b += 32) t = fmax(t, ws.mom_part[b * 16 + 10]);
             t = warp_max(t);
             if (lq == 0) mx_s = t;
@@ -134,10 +162,14 @@ vjp_fin_kernel(const double* __restrict__ x, int n, VjpWs ws)
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
-        ws.mom[10] = (n >= 2 && mx_s <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
-        ws.counter[0] = 0;
-        ws.counter[1] = 0;
+        if (MODE != kVjpStage) {
+            const bool ratio_ok = n >= 2 && x[1] <= 64.0 * x[0];
+            ws.mom[10] = (n >= 2 && mx_s <= kGeoTol && ratio_ok) ? 1.0 : 0.0;
+        }
+        if (MODE != kVjpTables) {
+            ws.counter[0] = 0;
+            ws.counter[1] = 0;
+        }
     }
 }
 
@@ -401,7 +433,10 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
 // tail of the chunk before); warp 0 adds the 32 in order, the block's own
 // smaller-member sums chunk by chunk, the diagonal pair, the death moments,
 // and stores dL/dN_m and the block's parameter partials.
-constexpr int kVRowsWarps = 32;
+#ifndef PBE_VROWS_WARPS
+#define PBE_VROWS_WARPS 32
+#endif
+constexpr int kVRowsWarps = PBE_VROWS_WARPS;
 
 template <int K>
 __global__ void __launch_bounds__(kVRowsWarps * 32)
@@ -413,7 +448,7 @@ vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     __shared__ int base[kVLaneMaxChunks + 1];
     if (ws.mom[10] == 0.0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b = blockIdx.x;
+    const int b = gridDim.x - 1 - blockIdx.x;      // top row blocks (the most lower blocks) first
     const int m = kLaneBins * b + lane;
     const int nchunks = vjp_lane_chunks(n, C);
     if (threadIdx.x == 0) {
@@ -428,15 +463,20 @@ vjp_lane_rows_kernel(const double* __restrict__ N, const double* __restrict__ x,
     double acc = 0.0;
     if (m < n) {
         // the loads of several row blocks in flight: addresses do not depend on acc
+        const float invC = 1.0f / static_cast<float>(C);
 #pragma unroll 4
         for (int bp = w; bp <= b; bp += kVRowsWarps) {
             const int d = m - kLaneBins * bp;
-            const int nch = (n - 1 - kLaneBins * bp + C - 1) / C;
-            const int c1 = d / C, idx = d - c1 * C;
+            // c1 = d / C: the float quotient, corrected by one either way
+            int c1 = __float2int_rz(static_cast<float>(d) * invC);
+            c1 -= (c1 * C > d) ? 1 : 0;
+            c1 += ((c1 + 1) * C <= d) ? 1 : 0;
+            const int idx = d - c1 * C;
             double v = 0.0;
             if (d >= 1) {
                 if (c1 >= 1 && idx < 32) v = __ldcg(ws.llo + (base[c1 - 1] + bp) * S + C + idx);
-                if (c1 < nch) v += __ldcg(ws.llo + (base[c1] + bp) * S + idx);
+                // chunk c1 exists for block bp when its first lag 1 + c1 C <= n - 1 - 32 bp
+                if (1 + c1 * C <= n - 1 - kLaneBins * bp) v += __ldcg(ws.llo + (base[c1] + bp) * S + idx);
             }
             acc += v;
         }
@@ -518,7 +558,8 @@ __global__ void __launch_bounds__(256)
 brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
                const double* __restrict__ t_q, const double* __restrict__ bw_q,
                const double* __restrict__ lam, double* __restrict__ gN, double* part, int n,
-               int nq, int nqp, double S0, double v_ref, double alpha, double v_min)
+               int nq, int nqp, double S0, double v_ref, double alpha, double v_min,
+               const double* __restrict__ Ssel, const int* __restrict__ lo_tab)
 {
     __shared__ double sh[8];
     const int l = threadIdx.x % nqp;
@@ -533,12 +574,13 @@ brk_vjp_kernel(const double* __restrict__ N, const double* __restrict__ x,
     if (j < n) {
         xj = x[j];
         Nj = N[j];
-        S = selection<F>(xj, S0, v_ref, alpha, v_min);
+        S = Ssel ? Ssel[j] : selection<F>(xj, S0, v_ref, alpha, v_min);
         on = (S != 0.0) && (Nj > kBreakageNMin);
         if (on) {
             for (int q = l; q < nq; q += nqp) {
                 const double v = xj * t_q[q];
-                const int lo = frag_bracket_guess(x, n, v, lx0, inv_span);
+                const int lo = lo_tab ? lo_tab[static_cast<size_t>(q) * n + j]
+                                      : frag_bracket_guess(x, n, v, lx0, inv_span);
                 double P;
                 if (lo < 0) P = lam[0];
                 else if (lo >= n - 1) P = lam[n - 1];
@@ -604,7 +646,7 @@ int vjp_lane_mode()
 }
 
 template <int K>
-cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStream_t s)
+cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStream_t s, int kind)
 {
     const int n = a.n;
     const int nb = (n + kPrepThreads - 1) / kPrepThreads;
@@ -619,8 +661,18 @@ cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStr
     const int C = vjp_lane_chunk(n);
     const long long ltasks = vjp_lane_tasks(n, C);
     const int lane_on = (vjp_lane_mode() && ltasks > 0 && vjp_lane_chunks(n, C) <= kVLaneMaxChunks) ? 1 : 0;
-    vjp_prep_kernel<<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
-    vjp_fin_kernel<<<1, 256, 0, s>>>(a.x, n, ws);
+    if (kind == kVjpTables) {
+        vjp_prep_kernel<kVjpTables><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
+        vjp_fin_kernel<kVjpTables><<<1, 256, 0, s>>>(a.x, n, ws);
+        return cudaGetLastError();
+    }
+    if (kind == kVjpStage) {
+        vjp_prep_kernel<kVjpStage><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
+        vjp_fin_kernel<kVjpStage><<<1, 256, 0, s>>>(a.x, n, ws);
+    } else {
+        vjp_prep_kernel<kVjpFull><<<nb, kPrepThreads, 0, s>>>(a.N, a.x, a.lam, n, ws);
+        vjp_fin_kernel<kVjpFull><<<1, 256, 0, s>>>(a.x, n, ws);
+    }
     const int nrb = (n + kLaneBins - 1) / kLaneBins;
     if (lane_on) {
         const size_t lsmem = sizeof(double) * kLaneWarps * ((C + kLaneWarps - 1) / kLaneWarps + 32);
@@ -640,43 +692,61 @@ cudaError_t agg_vjp_k(const AggVjpArgs& a, const VjpWs& ws, int num_sms, cudaStr
 }
 
 template <int F>
-cudaError_t brk_vjp_f(const BrkVjpArgs& a, const VjpWs& ws, cudaStream_t s)
+cudaError_t brk_vjp_f(const BrkVjpArgs& a, const VjpWs& ws, cudaStream_t s, const double* Ssel,
+                      const int* lo_tab)
 {
     int nqp = 1;
     while (nqp < a.n_quad && nqp < 32) nqp <<= 1;
     const int nb = static_cast<int>((static_cast<long long>(a.n) * nqp + 255) / 256);
     brk_vjp_kernel<F><<<nb, 256, 0, s>>>(a.N, a.x, a.t_q, a.bw_q, a.lam, a.gN, ws.gpart, a.n,
-                                         a.n_quad, nqp, a.S0, a.v_ref, a.alpha, a.v_min);
+                                         a.n_quad, nqp, a.S0, a.v_ref, a.alpha, a.v_min, Ssel,
+                                         lo_tab);
     vjp_gfin_kernel<<<1, 128, 0, s>>>(nb, ws, a.gp, 4, 0);
     return cudaGetLastError();
 }
 
 } // namespace
 
-cudaError_t agg_vjp_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+namespace {
+cudaError_t agg_vjp_dispatch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s, int kind)
 {
     VjpWs ws;
     vjp_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
     switch (a.kernel) {
-    case 0: return agg_vjp_k<0>(a, ws, num_sms, s);
-    case 1: return agg_vjp_k<1>(a, ws, num_sms, s);
-    case 2: return agg_vjp_k<2>(a, ws, num_sms, s);
-    case 3: return agg_vjp_k<3>(a, ws, num_sms, s);
-    case 4: return agg_vjp_k<4>(a, ws, num_sms, s);
-    case 5: return agg_vjp_k<5>(a, ws, num_sms, s);
+    case 0: return agg_vjp_k<0>(a, ws, num_sms, s, kind);
+    case 1: return agg_vjp_k<1>(a, ws, num_sms, s, kind);
+    case 2: return agg_vjp_k<2>(a, ws, num_sms, s, kind);
+    case 3: return agg_vjp_k<3>(a, ws, num_sms, s, kind);
+    case 4: return agg_vjp_k<4>(a, ws, num_sms, s, kind);
+    case 5: return agg_vjp_k<5>(a, ws, num_sms, s, kind);
     default: return cudaErrorInvalidValue;
     }
 }
+} // namespace
 
-cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s)
+cudaError_t agg_vjp_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+{
+    return agg_vjp_dispatch(a, ws_base, num_sms, s, kVjpFull);
+}
+cudaError_t agg_vjp_tables_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+{
+    return agg_vjp_dispatch(a, ws_base, num_sms, s, kVjpTables);
+}
+cudaError_t agg_vjp_stage_launch(const AggVjpArgs& a, void* ws_base, int num_sms, cudaStream_t s)
+{
+    return agg_vjp_dispatch(a, ws_base, num_sms, s, kVjpStage);
+}
+
+cudaError_t brk_vjp_launch(const BrkVjpArgs& a, void* ws_base, cudaStream_t s, const double* Ssel,
+                           const int* lo_tab)
 {
     VjpWs ws;
     vjp_ws_layout(a.n, static_cast<char*>(ws_base), &ws);
     switch (a.selection) {
-    case 0: return brk_vjp_f<0>(a, ws, s);
-    case 1: return brk_vjp_f<1>(a, ws, s);
-    case 2: return brk_vjp_f<2>(a, ws, s);
-    case 3: return brk_vjp_f<3>(a, ws, s);
+    case 0: return brk_vjp_f<0>(a, ws, s, Ssel, lo_tab);
+    case 1: return brk_vjp_f<1>(a, ws, s, Ssel, lo_tab);
+    case 2: return brk_vjp_f<2>(a, ws, s, Ssel, lo_tab);
+    case 3: return brk_vjp_f<3>(a, ws, s, Ssel, lo_tab);
     default: return cudaErrorInvalidValue;
     }
 }
