@@ -275,11 +275,14 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 // Lane-block pair tasks (agg_lane.cuh): blocks of kLaneBins output bins
 // aligned to the top of the grid, cut into lag chunks of lane_chunk_len(n)
-// lags (at least n / 16, so at most 17 chunks per block). Task (block t,
+// lags (at least n / 16 by default, so at most 17 chunks per block). Task (block t,
 // chunk c) has the index sum_{c' < c} lane_chunk_blocks(c') + t; its chunk
 // partial (R, TH of 32 slots) is stored under that index.
 constexpr int kLaneBins = 32;
-constexpr int kLaneMinChunk = 256;                  // shortest lag chunk
+#ifndef PBE_LANE_MIN_CHUNK
+#define PBE_LANE_MIN_CHUNK 256
+#endif
+constexpr int kLaneMinChunk = PBE_LANE_MIN_CHUNK;   // shortest lag chunk
 
 __host__ __device__ constexpr int lane_blocks(int n) { return (n + kLaneBins - 1) / kLaneBins; }
 // Highest slot of block t (slots exist up to n - 2); < 0 when the block has none.
@@ -287,10 +290,15 @@ __host__ __device__ constexpr int lane_block_smax(int n, int t)
 {
     return (n - kLaneBins * t - 1) < n - 2 ? (n - kLaneBins * t - 1) : n - 2;
 }
-// Lag chunk length: at least n / 16, a multiple of 64, at least kLaneMinChunk.
+// Lag chunk length: at least n / PBE_LANE_CHUNK_DIV (16), a multiple of 64, at
+// least kLaneMinChunk. At n = 3840 the chunk lengths 128 to 512 measured
+// within 2 % of each other; at n = 16384, 576 to 1408 within 1 %.
+#ifndef PBE_LANE_CHUNK_DIV
+#define PBE_LANE_CHUNK_DIV 16
+#endif
 __host__ __device__ constexpr int lane_chunk_len(int n)
 {
-    const int c = (((n + 15) / 16) + 63) / 64 * 64;
+    const int c = (((n + PBE_LANE_CHUNK_DIV - 1) / PBE_LANE_CHUNK_DIV) + 63) / 64 * 64;
     return c < kLaneMinChunk ? kLaneMinChunk : c;
 }
 // Chunks of block t: every block has chunk 0; chunk c >= 1 when c C <= smax_t.
