@@ -133,7 +133,8 @@ __device__ void lane_task(const AggCellView& v, const AggWs& ws, const LaneArgs&
     // (Ld is nondecreasing; clipped lags hold kLagClipAll)
     const int dA = c * C;
     int dB = min(dA + C, smax + 1);
-    if (dB > dA) {
+    // most chunks end below the cut: one load settles it, else bisect
+    if (dB > dA && __ldg(v.Ld + dB - 1) > smax) {
         int lo = dA, hi = dB;
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
