@@ -185,6 +185,8 @@ __device__ void lane_task(const AggCellView& v, const AggWs& ws, const LaneArgs&
     const bool slot = (s >= smin && s <= smax);
     const double xs = slot ? __ldg(v.x + s) : 0.0;
     const int St = slot ? -ilogb(xs) : 0;
+    const EwOperandC pc = ew_operand_c(xs, St);       // the slot pivot, decoded once
+    EwOperandA pa = ew_operand_a(0.0);                // x_k of the current run
     double R = 0.0, TH = 0.0, Q = 0.0, QT = 0.0;
     double F = 0.0, xk = 0.0, Nk = 0.0, hk = 0.0;
     int e_cur = -1;
@@ -204,6 +206,7 @@ __device__ void lane_task(const AggCellView& v, const AggWs& ws, const LaneArgs&
                 const bool kin = slot && k >= 0;
                 F = kin ? __ldg(v.Fs + k) : 0.0;
                 xk = kin ? __ldg(v.x + k) : 0.0;
+                pa = ew_operand_a(xk);
                 if constexpr (K == 1) {
                     Nk = kin ? __ldg(v.Nk + k) : 0.0;
                     hk = kin ? __ldg(v.Hk + k) : 0.0;
@@ -214,7 +217,7 @@ __device__ void lane_task(const AggCellView& v, const AggWs& ws, const LaneArgs&
             if (slot && j >= 0) {
                 const double Nj = pN[j];
                 const double hj = NeedH<K>::j ? pH[j] : 0.0;
-                const double th = sum_minus_scaled(xk, pX[j], xs, St);
+                const double th = sum_minus_scaled_pre(pa, pX[j], pc);
                 if constexpr (K != 1) {
                     const double q = q_slot<K>(B, S, Nj, hj);
                     Q += q;

@@ -61,20 +61,46 @@ PBE_HD int ew_clz64(uint64_t v)
 #endif
 }
 
-// Returns (fl(a + b) - c) * 2^St.
-PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
+// The operands that stay fixed over runs of calls in the pair loops, decoded
+// once: a (the larger addend) as its 63-bit fixed-point significand and
+// biased exponent, c (the subtrahend) with the result's scale St.
+struct EwOperandA {
+    uint64_t A;    // significand with the hidden bit, shifted left by 10 guard bits
+    int ea;        // biased exponent
+};
+struct EwOperandC {
+    uint64_t mc;   // significand with the hidden bit
+    int ec;        // biased exponent
+    int St;
+};
+PBE_HD EwOperandA ew_operand_a(double a)
 {
     constexpr uint64_t kM52 = (1ull << 52) - 1;
     constexpr uint64_t kH53 = 1ull << 52;
-    const uint64_t ua = ew_bits(a), ub = ew_bits(b), uc = ew_bits(c);
-    const int ea = static_cast<int>(ua >> 52), eb = static_cast<int>(ub >> 52);
-    const int ec = static_cast<int>(uc >> 52);
-    const uint64_t ma = (ua & kM52) | kH53, mb = (ub & kM52) | kH53, mc = (uc & kM52) | kH53;
+    const uint64_t ua = ew_bits(a);
+    return EwOperandA{((ua & kM52) | kH53) << 10, static_cast<int>(ua >> 52)};
+}
+PBE_HD EwOperandC ew_operand_c(double c, int St)
+{
+    constexpr uint64_t kM52 = (1ull << 52) - 1;
+    constexpr uint64_t kH53 = 1ull << 52;
+    const uint64_t uc = ew_bits(c);
+    return EwOperandC{(uc & kM52) | kH53, static_cast<int>(uc >> 52), St};
+}
+
+// (fl(a + b) - c) * 2^St from the decoded a and c.
+PBE_HD double sum_minus_scaled_pre(const EwOperandA& pa, double b, const EwOperandC& pc)
+{
+    constexpr uint64_t kM52 = (1ull << 52) - 1;
+    constexpr uint64_t kH53 = 1ull << 52;
+    const uint64_t ub = ew_bits(b);
+    const int eb = static_cast<int>(ub >> 52);
+    const uint64_t mb = (ub & kM52) | kH53;
 
     // ---- s = fl(a + b), round to nearest even --------------------------------
     // a and b as 63-bit fixed point with 10 guard bits below a's last place.
-    const int d = ea - eb;                       // >= 0 because b <= a
-    const uint64_t A = ma << 10;
+    const int d = pa.ea - eb;                    // >= 0 because b <= a
+    const uint64_t A = pa.A;
     uint64_t B;
     bool sticky;
     if (d >= 64) {
@@ -88,7 +114,7 @@ PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
     const uint64_t S = A + B;                    // < 2^64 since B <= A < 2^63
     const int carry = static_cast<int>(S >> 63); // sum reached the next binade
     const int rs = 10 + carry;
-    int es = ea + carry;
+    int es = pa.ea + carry;
     uint64_t ms = S >> rs;                       // 53 significant bits
     const uint64_t rem = S & ((1ull << rs) - 1);
     const uint64_t half = 1ull << (rs - 1);
@@ -97,13 +123,14 @@ PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
     if (ms >> 53) { ms >>= 1; ++es; }            // rounding carried into a new binade
 
     // ---- t = s - c exactly (integers on the smaller of the two exponents) -----
+    const int ec = pc.ec;
     const int e0 = es < ec ? es : ec;
-    const int64_t T = static_cast<int64_t>(ms << (es - e0)) - static_cast<int64_t>(mc << (ec - e0));
+    const int64_t T = static_cast<int64_t>(ms << (es - e0)) - static_cast<int64_t>(pc.mc << (ec - e0));
     if (T == 0) return 0.0;
     const uint64_t sign = T < 0 ? (1ull << 63) : 0ull;
     uint64_t m = T < 0 ? static_cast<uint64_t>(-T) : static_cast<uint64_t>(T);
     const int p = 63 - ew_clz64(m);              // leading bit, < 53 + kMaxExpGap
-    int E = e0 + p - 52 + St;                    // biased exponent of the result
+    int E = e0 + p - 52 + pc.St;                 // biased exponent of the result
     if (p <= 52) {
         m <<= (52 - p);
     } else {                                     // more than 53 bits: round to nearest even
@@ -116,6 +143,12 @@ PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
         }
     }
     return ew_double(sign | (static_cast<uint64_t>(E) << 52) | (m & kM52));
+}
+
+// Returns (fl(a + b) - c) * 2^St.
+PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
+{
+    return sum_minus_scaled_pre(ew_operand_a(a), b, ew_operand_c(c, St));
 }
 
 } // namespace pbe_gb300
