@@ -88,18 +88,28 @@ PBE_HD EwOperandC ew_operand_c(double c, int St)
     return EwOperandC{(uc & kM52) | kH53, static_cast<int>(uc >> 52), St};
 }
 
-// (fl(a + b) - c) * 2^St from the decoded a and c.
-PBE_HD double sum_minus_scaled_pre(const EwOperandA& pa, double b, const EwOperandC& pc)
+// b (the smaller addend) decoded: significand with the hidden bit, shifted
+// left by 10 guard bits, and biased exponent.
+struct EwOperandB {
+    uint64_t bw;
+    int eb;
+};
+PBE_HD EwOperandB ew_operand_b(double b)
 {
     constexpr uint64_t kM52 = (1ull << 52) - 1;
     constexpr uint64_t kH53 = 1ull << 52;
     const uint64_t ub = ew_bits(b);
-    const int eb = static_cast<int>(ub >> 52);
-    const uint64_t mb = (ub & kM52) | kH53;
+    return EwOperandB{((ub & kM52) | kH53) << 10, static_cast<int>(ub >> 52)};
+}
+
+// (fl(a + b) - c) * 2^St from the decoded operands.
+PBE_HD double sum_minus_scaled_dec(const EwOperandA& pa, const EwOperandB& pb, const EwOperandC& pc)
+{
+    constexpr uint64_t kM52 = (1ull << 52) - 1;
 
     // ---- s = fl(a + b), round to nearest even --------------------------------
     // a and b as 63-bit fixed point with 10 guard bits below a's last place.
-    const int d = pa.ea - eb;                    // >= 0 because b <= a
+    const int d = pa.ea - pb.eb;                 // >= 0 because b <= a
     const uint64_t A = pa.A;
     uint64_t B;
     bool sticky;
@@ -107,7 +117,7 @@ PBE_HD double sum_minus_scaled_pre(const EwOperandA& pa, double b, const EwOpera
         B = 0;
         sticky = true;                           // b != 0 lies entirely below
     } else {
-        const uint64_t bw = mb << 10;
+        const uint64_t bw = pb.bw;
         B = bw >> d;
         sticky = d > 0 && (bw << (64 - d)) != 0;
     }
@@ -145,10 +155,16 @@ PBE_HD double sum_minus_scaled_pre(const EwOperandA& pa, double b, const EwOpera
     return ew_double(sign | (static_cast<uint64_t>(E) << 52) | (m & kM52));
 }
 
+// The same with a and c decoded (b varies from call to call).
+PBE_HD double sum_minus_scaled_pre(const EwOperandA& pa, double b, const EwOperandC& pc)
+{
+    return sum_minus_scaled_dec(pa, ew_operand_b(b), pc);
+}
+
 // Returns (fl(a + b) - c) * 2^St.
 PBE_HD double sum_minus_scaled(double a, double b, double c, int St)
 {
-    return sum_minus_scaled_pre(ew_operand_a(a), b, ew_operand_c(c, St));
+    return sum_minus_scaled_dec(ew_operand_a(a), ew_operand_b(b), ew_operand_c(c, St));
 }
 
 } // namespace pbe_gb300

@@ -349,6 +349,7 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
         if constexpr (K == 4) cH = bsh * hj;
         if constexpr (K == 5) { cN = bbr * Nj; cH = bsh * hj; }
         const int jtop = n - 1 - j;               // lo >= n - 1 <=> Ld[d] >= jtop
+        const EwOperandB pb = ew_operand_b(jv ? xj : 1.0);   // the row's pivot, decoded once
 
         double U0 = 0.0, U1 = 0.0, W = 0.0;
 #ifdef PBE_VJP_UNROLL
@@ -369,7 +370,8 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
                 double P = lamlast;
                 if (L < jtop) {
                     const int lo = j + L;
-                    P = fma(sum_minus_scaled(xk, xj, __ldg(x + lo), 0), D[lo], lam[lo]);
+                    P = fma(sum_minus_scaled_dec(ew_operand_a(xk), pb, ew_operand_c(__ldg(x + lo), 0)),
+                            D[lo], lam[lo]);
                 }
                 if constexpr (K == 0) {
                     U0 = fma(P, __ldg(N + k), U0);
