@@ -78,7 +78,8 @@ SELECTIONS = [  # (selection, S0, v_ref bin, alpha, v_min bin)
 def test_breakage_matches_oracle(sel, S0, vref, alpha, vmin, daughter, grid, mode):
     rng = np.random.default_rng(77 + sel)
     t_q, bw_q = DAUGHTERS[daughter]
-    for n in (1, 2, 5, 64, 1000):
+    # 31, 32, 33, 62, 63: around the gather kernel's blocks (bin 0 alone, then 31 bins each)
+    for n in (1, 2, 5, 31, 32, 33, 62, 63, 64, 1000):
         x = make_grid(grid, n, rng)
         N = make_N("random", x, rng)
         N[rng.random(n) < 0.05] = 1e-310    # below the 2.2e-308 guard
@@ -89,6 +90,25 @@ def test_breakage_matches_oracle(sel, S0, vref, alpha, vmin, daughter, grid, mod
         assert code == 0, pg.error_string(code)
         ref, scale, _ = oracle_brk(N, x, t_q, bw_q, p)
         assert_close(got, ref, scale, "sel=%d %s grid=%s n=%d" % (sel, daughter, grid, n))
+
+
+@pytest.mark.parametrize("grid", ["geo_fine", "generic"])
+@pytest.mark.parametrize("sel", [0, 2])
+def test_breakage_gather_many_points(sel, grid):
+    """136 quadrature points: in the gather kernel each warp takes 34 points and
+    block 0's threads more than one point each (the prefix over the parents at
+    or below x[0] and its per-point lookups)."""
+    rng = np.random.default_rng(91 + sel)
+    t_q, bw_q = pg.quadrature.uniform(136)
+    for n in (3, 200, 2000):
+        x = make_grid(grid, n, rng)
+        N = make_N("random", x, rng)
+        mid = float(x[n // 2])
+        p = pg.BreakageParams(n=n, n_quad=len(t_q), selection=sel, S0=1e-3, v_ref=mid, alpha=1.5)
+        code, got = gpu_brk(N, x, t_q, bw_q, p, pg.MODE_GATHER)
+        assert code == 0, pg.error_string(code)
+        ref, scale, _ = oracle_brk(N, x, t_q, bw_q, p)
+        assert_close(got, ref, scale, "sel=%d grid=%s n=%d n_quad=136" % (sel, grid, n))
 
 
 @pytest.mark.parametrize("mode", MODES, ids=["gather", "scatter"])

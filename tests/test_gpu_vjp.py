@@ -40,7 +40,9 @@ def gpu_brk_vjp(N, x, t_q, bw_q, lam, p):
 @pytest.mark.parametrize("kernel,b0,bbr,bsh", AGG_KERNELS, ids=[str(k[0]) for k in AGG_KERNELS])
 def test_aggregation_vjp_matches_oracle(kernel, b0, bbr, bsh, grid):
     rng = np.random.default_rng(500 + kernel)
-    for n in (1, 2, 17, 300, 1000):
+    # 32, 33, 34, 65: around the lane path's row blocks of 32 (a last block
+    # with one row and no lags, or with one lag)
+    for n in (1, 2, 17, 32, 33, 34, 65, 300, 1000):
         if grid == "geo_coarse" and n > 700:
             continue   # x_n ~ 2^n: beta0 x_j x_k would overflow in the reference formula
         x = make_grid(grid, n, rng)
