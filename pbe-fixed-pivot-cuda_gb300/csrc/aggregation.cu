@@ -104,6 +104,26 @@ agg_prep_kernel(const double* __restrict__ N, const double* __restrict__ x, int 
         m[0] = iai * Ni; m[1] = Ni; m[2] = ai * Ni; m[3] = (ai * ai) * Ni; m[4] = hi;
         if (i < agg_tiles(n)) { ws.tticket[i] = 0; ws.cticket[i] = 0; }
         if constexpr (FULL) {
+            // launch order of the lane tasks: entry i < full is a full chunk
+            // (chunk by chunk), entry full + rank(t) block t's last chunk
+            const int C = lane_chunk_len(n);
+            const int full = lane_full_tasks(n, C);
+            if (i < full) {
+                int r = i, c = 0;
+                for (;;) {
+                    const int cnt = lane_chunk_blocks(n, c + 1, C);
+                    if (r < cnt) break;
+                    r -= cnt;
+                    ++c;
+                }
+                ws.ltask[2 * i] = r;
+                ws.ltask[2 * i + 1] = c;
+            }
+            if (i < lane_blocks(n)) {
+                const int k = full + lane_last_rank(n, i, C);
+                ws.ltask[2 * k] = i;
+                ws.ltask[2 * k + 1] = lane_block_chunks(n, i, C) - 1;
+            }
             ws.xcp[i] = xi;
             ws.a[i] = ai;
             ws.ia[i] = iai;
@@ -492,15 +512,9 @@ agg_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
             continue;
         }
         task -= nclip;
-        int c = 0, cnt = 0;
-        for (;;) {
-            cnt = lane_chunk_blocks(n, c, lane_C);
-            if (cnt == 0 || task < cnt) break;
-            task -= cnt;
-            ++c;
-        }
-        if (cnt == 0) continue;
-        lane_task<K, SCATTER, STAGE>(v, ws, la, rhs, task, c, nclip, lsm, &s_bar, phase, &s_flag);
+        // largest first (the prep's launch order)
+        const int t = __ldg(ws.ltask + 2 * task), c = __ldg(ws.ltask + 2 * task + 1);
+        lane_task<K, SCATTER, STAGE>(v, ws, la, rhs, t, c, nclip, lsm, &s_bar, phase, &s_flag);
     }
 }
 

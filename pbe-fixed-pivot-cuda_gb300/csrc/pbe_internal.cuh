@@ -251,6 +251,7 @@ struct AggWs {
     double* Ncp;       // [n + 2] copy of N, 256-byte aligned (bulk-copy source)
     double* xcp;       // [n + 2] copy of x, 256-byte aligned (bulk-copy source)
     double* lpart;     // [lane_partial_doubles(n)] lane-task chunk partials
+    int*    ltask;     // [2 lane_tasks(n)] lane tasks in launch order, (block, chunk) pairs
 };
 
 constexpr int agg_prep_blocks(int n) { return (n + kPrepThreads - 1) / kPrepThreads; }
@@ -320,6 +321,48 @@ __host__ __device__ constexpr long long lane_tasks(int n, int C)
     for (int c = 0; lane_chunk_blocks(n, c, C) > 0; ++c) s += lane_chunk_blocks(n, c, C);
     return s;
 }
+// Launch order of the lane tasks (largest first, so the last wave is filled
+// with the shortest tasks): first every chunk that is not its block's last
+// (all C lags long), chunk by chunk; then each block's last chunk, longest
+// first (ties: lower block first). Entry k of the order is lane_task_at(k).
+// Full chunks: chunk c of the blocks that also have chunk c + 1.
+__host__ __device__ constexpr int lane_full_tasks(int n, int C)
+{
+    int s = 0;
+    for (int c = 0; lane_chunk_blocks(n, c + 1, C) > 0; ++c) s += lane_chunk_blocks(n, c + 1, C);
+    return s;
+}
+// Lags of block t's last chunk (before the cut where Ld passes its top slot).
+__host__ __device__ constexpr int lane_last_chunk_len(int n, int t, int C)
+{
+    return lane_block_smax(n, t) + 1 - (lane_block_chunks(n, t, C) - 1) * C;
+}
+
+#if defined(__CUDACC__)
+// Position of block t's last chunk among the last chunks (longest first, then
+// lower block first). For t >= 1 the block's top slot is n - 1 - 32 t, so its
+// last chunk has ((n - 33 - 32 (t - 1)) mod C) + 1 lags: blocks whose t - 1
+// agree mod P = C / 32 share a length. Counts per class, P steps.
+__device__ __forceinline__ int lane_last_rank(int n, int t, int C)
+{
+    const int nblk = lane_blocks(n);
+    const int Lt = max(0, lane_last_chunk_len(n, t, C));
+    const int L0 = max(0, lane_last_chunk_len(n, 0, C));
+    int rank = (L0 > Lt || (L0 == Lt && 0 < t)) ? 1 : 0;
+    if (nblk >= 2) {
+        const int P = C / kLaneBins;
+        const int r1 = (n - 33) % C;             // n >= 33 when there are two blocks
+        for (int u = 0; u < P && u <= nblk - 2; ++u) {
+            int rem = (r1 - kLaneBins * u) % C;
+            if (rem < 0) rem += C;
+            if (rem + 1 > Lt) rank += (nblk - 2 - u) / P + 1;   // blocks 1 + u + P k
+        }
+        if (t >= 1) rank += (t - 1) / P;         // same length, lower block
+    }
+    return rank;
+}
+#endif
+
 // Doubles of lane-task chunk partials: tasks x (R, TH) x kLaneBins.
 __host__ __device__ constexpr size_t lane_partial_doubles(int n)
 {
@@ -342,7 +385,8 @@ constexpr size_t agg_ws_bytes(int n)
          + align256(sizeof(int) * static_cast<size_t>(agg_tiles(n)))
          + align256(sizeof(int) * 8)
          + 2 * align256(sizeof(double) * (static_cast<size_t>(n) + 2))
-         + align256(sizeof(double) * lane_partial_doubles(n));
+         + align256(sizeof(double) * lane_partial_doubles(n))
+         + align256(sizeof(int) * 2 * static_cast<size_t>(lane_tasks(n, lane_chunk_len(n))));
 }
 
 // Carves the aggregation scratch out of `base` (may be null to query the size).
@@ -373,6 +417,8 @@ inline size_t agg_ws_layout(int n, char* base, AggWs* ws)
     w.Ncp       = reinterpret_cast<double*>(take(sizeof(double) * (static_cast<size_t>(n) + 2)));
     w.xcp       = reinterpret_cast<double*>(take(sizeof(double) * (static_cast<size_t>(n) + 2)));
     w.lpart     = reinterpret_cast<double*>(take(sizeof(double) * lane_partial_doubles(n)));
+    w.ltask     = reinterpret_cast<int*>(take(sizeof(int) * 2 *
+                                              static_cast<size_t>(lane_tasks(n, lane_chunk_len(n)))));
     if (ws) *ws = w;
     return off;
 }
@@ -449,6 +495,36 @@ __host__ __device__ constexpr long long vjp_lane_tasks(int n, int C)
     for (int c = 0; vjp_lane_chunk_blocks(n, c, C) > 0; ++c) s += vjp_lane_chunk_blocks(n, c, C);
     return s;
 }
+// Launch order (largest first, as the forward's lane tasks): every chunk that is
+// not its row block's last, chunk by chunk, then each block's last chunk,
+// longest first (ties: lower block first).
+__host__ __device__ constexpr int vjp_lane_full_tasks(int n, int C)
+{
+    int s = 0;
+    for (int c = 0; vjp_lane_chunk_blocks(n, c + 1, C) > 0; ++c) s += vjp_lane_chunk_blocks(n, c + 1, C);
+    return s;
+}
+#if defined(__CUDACC__)
+// Position of row block b's last chunk among the last chunks: block b meets
+// the lags [1, n - 1 - 32 b], so its last chunk has ((n - 2 - 32 b) mod C) + 1
+// lags; blocks that agree mod P = C / 32 share a length.
+__device__ __forceinline__ int vjp_lane_last_rank(int n, int b, int C)
+{
+    const int nvb = vjp_lane_chunk_blocks(n, 0, C);     // blocks with at least one lag
+    const int P = C / kLaneBins;
+    const int r0 = (n - 2) % C;
+    auto len = [&](int u) {
+        int rem = (r0 - kLaneBins * u) % C;
+        if (rem < 0) rem += C;
+        return rem + 1;
+    };
+    const int Lb = len(b % P);
+    int rank = b / P;                                   // same length, lower block
+    for (int u = 0; u < P && u < nvb; ++u)
+        if (len(u) > Lb) rank += (nvb - 1 - u) / P + 1;  // blocks u + P k
+    return rank;
+}
+#endif
 struct VjpWs {
     double* h;         // [n]  x_i N_i
     double* a;         // [n]  x_i^(1/3)
@@ -462,6 +538,7 @@ struct VjpWs {
     double* mom;       // [16] 0..4 moments of N, 5..9 of lambda*N, 10 geo flag
     double* gpart;     // [max(ntile, n / 8) * 4] per-task / per-block parameter partials
     double* vpart;     // [ntile * kVjpMaxChunks * 2 kTileW] row sums per (tile, partner chunk)
+    int*    ltask;     // [2 lane tasks] lane tasks in launch order, (row block, chunk) pairs
     double* lup;       // [lane tasks * 64] lane-task sums of the rows as smaller members
     double* llo;       // [lane tasks * (C + 32)] lane-task sums of the rows as larger members
     int*    counter;   // [8]: 0 tile tasks, 1 lane tasks
@@ -490,6 +567,7 @@ inline size_t vjp_ws_layout(int n, char* base, VjpWs* ws)
                                                 static_cast<size_t>(ntile)));
     const int C = vjp_lane_chunk(n);
     const size_t ltasks = static_cast<size_t>(vjp_lane_tasks(n, C));
+    w.ltask    = reinterpret_cast<int*>(take(sizeof(int) * 2 * ltasks));
     w.lup      = reinterpret_cast<double*>(take(sizeof(double) * 2 * kLaneBins * ltasks));
     w.llo      = reinterpret_cast<double*>(take(sizeof(double) * (C + 32) * ltasks));
     w.counter  = reinterpret_cast<int*>(take(sizeof(int) * 8));

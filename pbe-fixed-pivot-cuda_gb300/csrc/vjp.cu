@@ -98,6 +98,27 @@ vjp_prep_kernel(const double* __restrict__ N, const double* __restrict__ x,
             ws.Sl[i] = (s * s) * s * (x0 / xi);
             const double v = x0 + xi;
             ws.Ld[i] = (dbits(v) >= dbits(x[n - 1])) ? kLagClipAll : bracket_from(x, n, v, i);
+            // launch order of the lane tasks: entry i < full is a full chunk
+            // (chunk by chunk), entry full + rank(b) row block b's last chunk
+            const int C = vjp_lane_chunk(n);
+            const int full = vjp_lane_full_tasks(n, C);
+            if (i < full) {
+                int r = i, c = 0;
+                for (;;) {
+                    const int cnt = vjp_lane_chunk_blocks(n, c + 1, C);
+                    if (r < cnt) break;
+                    r -= cnt;
+                    ++c;
+                }
+                ws.ltask[2 * i] = r;
+                ws.ltask[2 * i + 1] = c;
+            }
+            if (i < vjp_lane_chunk_blocks(n, 0, C)) {
+                const int dmax = n - 1 - kLaneBins * i;
+                const int k = full + vjp_lane_last_rank(n, i, C);
+                ws.ltask[2 * k] = i;
+                ws.ltask[2 * k + 1] = (dmax + C - 1) / C - 1;
+            }
             if (n >= 2) {
                 dev = geo_dev(fit_s, xi, i);
                 if (!(dev == dev)) dev = 1.0;
@@ -317,16 +338,14 @@ vjp_lane_kernel(const double* __restrict__ N, const double* __restrict__ x,
     for (;;) {
         if (tid == 0) s_task = atomicAdd(ws.counter + 1, 1);
         __syncthreads();
-        const int tix = s_task;
+        const int task = s_task;
         __syncthreads();
-        if (tix >= ntasks) break;
-        int b = tix, c = 0;
-        for (;;) {
-            const int cnt = vjp_lane_chunk_blocks(n, c, C);
-            if (b < cnt || cnt == 0) break;
-            b -= cnt;
-            ++c;
-        }
+        if (task >= ntasks) break;
+        // largest first (the prep's launch order); the sums are stored under the
+        // chunk-major index sum_{c' < c} blocks(c') + b that the rows kernel reads
+        const int b = __ldg(ws.ltask + 2 * task), c = __ldg(ws.ltask + 2 * task + 1);
+        int tix = b;
+        for (int q = 0; q < c; ++q) tix += vjp_lane_chunk_blocks(n, q, C);
         const int J = kLaneBins * b;
         const int dA = 1 + c * C;
         const int dB = min(dA + C, n - J);        // lags [dA, dB), dB - 1 <= n - 1 - J
