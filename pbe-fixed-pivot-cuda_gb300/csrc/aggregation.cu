@@ -438,8 +438,10 @@ agg_main_kernel(const double* __restrict__ N, const double* __restrict__ x,
 
 // ---------------------------------------------------------------------------
 // lane: persistent CTAs pulling lane-block tasks (agg_lane.cuh) on verified
-// geometric grids -- clip tasks first, then (block, lag chunk) tasks chunk by
-// chunk, top blocks first. Returns at once on other grids (the tile kernel
+// geometric grids -- clip tasks first, then (block, lag chunk) tasks largest
+// first in the order of the prep's table ws.ltask (the full chunks, then each
+// block's last chunk by length, so the last wave holds the shortest tasks).
+// Returns at once on other grids (the tile kernel
 // launched after it takes them). It needs fewer registers than the tile
 // kernel, so more CTAs fit on an SM.
 // ---------------------------------------------------------------------------
