@@ -338,16 +338,16 @@ __host__ __device__ constexpr int lane_last_chunk_len(int n, int t, int C)
     return lane_block_smax(n, t) + 1 - (lane_block_chunks(n, t, C) - 1) * C;
 }
 
-#if defined(__CUDACC__)
 // Position of block t's last chunk among the last chunks (longest first, then
 // lower block first). For t >= 1 the block's top slot is n - 1 - 32 t, so its
 // last chunk has ((n - 33 - 32 (t - 1)) mod C) + 1 lags: blocks whose t - 1
 // agree mod P = C / 32 share a length. Counts per class, P steps.
-__device__ __forceinline__ int lane_last_rank(int n, int t, int C)
+__host__ __device__ inline int lane_last_rank(int n, int t, int C)
 {
     const int nblk = lane_blocks(n);
-    const int Lt = max(0, lane_last_chunk_len(n, t, C));
-    const int L0 = max(0, lane_last_chunk_len(n, 0, C));
+    const int lt = lane_last_chunk_len(n, t, C), l0 = lane_last_chunk_len(n, 0, C);
+    const int Lt = lt > 0 ? lt : 0;
+    const int L0 = l0 > 0 ? l0 : 0;
     int rank = (L0 > Lt || (L0 == Lt && 0 < t)) ? 1 : 0;
     if (nblk >= 2) {
         const int P = C / kLaneBins;
@@ -361,7 +361,6 @@ __device__ __forceinline__ int lane_last_rank(int n, int t, int C)
     }
     return rank;
 }
-#endif
 
 // Doubles of lane-task chunk partials: tasks x (R, TH) x kLaneBins.
 __host__ __device__ constexpr size_t lane_partial_doubles(int n)
@@ -504,11 +503,10 @@ __host__ __device__ constexpr int vjp_lane_full_tasks(int n, int C)
     for (int c = 0; vjp_lane_chunk_blocks(n, c + 1, C) > 0; ++c) s += vjp_lane_chunk_blocks(n, c + 1, C);
     return s;
 }
-#if defined(__CUDACC__)
 // Position of row block b's last chunk among the last chunks: block b meets
 // the lags [1, n - 1 - 32 b], so its last chunk has ((n - 2 - 32 b) mod C) + 1
 // lags; blocks that agree mod P = C / 32 share a length.
-__device__ __forceinline__ int vjp_lane_last_rank(int n, int b, int C)
+__host__ __device__ inline int vjp_lane_last_rank(int n, int b, int C)
 {
     const int nvb = vjp_lane_chunk_blocks(n, 0, C);     // blocks with at least one lag
     const int P = C / kLaneBins;
@@ -524,7 +522,6 @@ __device__ __forceinline__ int vjp_lane_last_rank(int n, int b, int C)
         if (len(u) > Lb) rank += (nvb - 1 - u) / P + 1;  // blocks u + P k
     return rank;
 }
-#endif
 struct VjpWs {
     double* h;         // [n]  x_i N_i
     double* a;         // [n]  x_i^(1/3)
