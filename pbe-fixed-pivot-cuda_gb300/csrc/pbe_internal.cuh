@@ -351,11 +351,14 @@ __host__ __device__ inline int lane_last_rank(int n, int t, int C)
     int rank = (L0 > Lt || (L0 == Lt && 0 < t)) ? 1 : 0;
     if (nblk >= 2) {
         const int P = C / kLaneBins;
-        const int r1 = (n - 33) % C;             // n >= 33 when there are two blocks
-        for (int u = 0; u < P && u <= nblk - 2; ++u) {
-            int rem = (r1 - kLaneBins * u) % C;
+        const int M = nblk - 2;                  // class u has the blocks 1 + u + P k <= nblk - 1
+        int rem = (n - 33) % C;                  // (n - 33 - 32 u) mod C; n >= 33 here
+        int q = M / P, rq = M - q * P;           // M - u = q P + rq
+        for (int u = 0; u < P && u <= M; ++u) {
+            if (rem + 1 > Lt) rank += q + 1;
+            rem -= kLaneBins;
             if (rem < 0) rem += C;
-            if (rem + 1 > Lt) rank += (nblk - 2 - u) / P + 1;   // blocks 1 + u + P k
+            if (--rq < 0) { rq += P; --q; }
         }
         if (t >= 1) rank += (t - 1) / P;         // same length, lower block
     }
@@ -511,15 +514,19 @@ __host__ __device__ inline int vjp_lane_last_rank(int n, int b, int C)
     const int nvb = vjp_lane_chunk_blocks(n, 0, C);     // blocks with at least one lag
     const int P = C / kLaneBins;
     const int r0 = (n - 2) % C;
-    auto len = [&](int u) {
-        int rem = (r0 - kLaneBins * u) % C;
-        if (rem < 0) rem += C;
-        return rem + 1;
-    };
-    const int Lb = len(b % P);
+    int remb = (r0 - kLaneBins * (b % P)) % C;
+    if (remb < 0) remb += C;
+    const int Lb = remb + 1;
     int rank = b / P;                                   // same length, lower block
-    for (int u = 0; u < P && u < nvb; ++u)
-        if (len(u) > Lb) rank += (nvb - 1 - u) / P + 1;  // blocks u + P k
+    const int M = nvb - 1;                              // class u has the blocks u + P k <= nvb - 1
+    int rem = r0;                                       // (r0 - 32 u) mod C
+    int q = M / P, rq = M - q * P;                      // M - u = q P + rq
+    for (int u = 0; u < P && u <= M; ++u) {
+        if (rem + 1 > Lb) rank += q + 1;
+        rem -= kLaneBins;
+        if (rem < 0) rem += C;
+        if (--rq < 0) { rq += P; --q; }
+    }
     return rank;
 }
 struct VjpWs {
