@@ -303,8 +303,9 @@ __global__ void __launch_bounds__(128) vjp_gfin_kernel(int ntile, VjpWs ws, doub
 // every lane's W at the end of the share. Brownian + shear: 7 FP64
 // instructions per pair (P; P Bf, P Sf; two sums of the smaller member; two
 // FMAs into W) against 8 for the two visits of the tile path.
-// Determinism: the windows of the CTA's warps are added in warp order; the
-// rows kernel adds the tasks' sums in a fixed order.
+// Tasks (row block, lag chunk) run largest first from the prep's launch-order
+// table. Determinism: the windows of the CTA's warps are added in warp order;
+// the rows kernel adds the tasks' sums in a fixed order.
 // -------------------------------------------------------------------------
 #ifndef PBE_VJP_LANE_CTAS
 #define PBE_VJP_LANE_CTAS 3
